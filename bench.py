@@ -1,0 +1,414 @@
+"""Benchmark: batched 2-D IM spectra/s on one GB300.
+
+Workload: 4096 independent Demographics2D.IM integrations (parameters drawn
+from numpy default_rng(0): s ~ U(.05,.95); nu1, nu2 log-uniform on [.01,100];
+T log-uniform on [.01,2]; m12, m21 ~ U(0,10)), each on the default grids
+pts [80, 90, 100], from_phi at ns (40,40), quadratic Richardson extrapolation
+and the Poisson log-likelihood against synthetic data
+Poisson(5e4 * model(first parameter set)).  A step is one pass of the batched
+engine over the whole 4096-instance batch.  Synthetic data stands in for an
+observed spectrum (none is used by the reference's benchmark).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` times the engine with the parameters already on the device; `e2e`
+times the public API call (host parameter and data arrays in, host spectra and
+likelihoods out).  --impl reference times the CPU integrator restatement
+(the reference's algorithm: Python time loop over C sweeps) on all host
+cores over a bounded sample and scales it to the workload by point-sweeps.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+
+METRIC = ("2D IM spectra/s batched vs plain on GB300 @≤1e-9 rel err; "
+          "served p50/p99 latency")
+PTS_L = (80, 90, 100)
+NS = (40, 40)
+NINST = 4096
+BYTES_PER_PS = 16      # algorithmic HBM bytes per point-sweep (phi read + write)
+FLOPS_PER_PS = 30      # algorithmic FP64 flops per point-sweep (reference formulation)
+FP64_INSTR_PER_PS = 10  # FP64 pipe instructions per point-sweep in k_integrate2d
+
+
+def im_draws(n, seed):
+    rng = np.random.default_rng(seed)
+    s = rng.uniform(0.05, 0.95, n)
+    nu1 = np.exp(rng.uniform(np.log(0.01), np.log(100), n))
+    nu2 = np.exp(rng.uniform(np.log(0.01), np.log(100), n))
+    T = np.exp(rng.uniform(np.log(0.01), np.log(2), n))
+    m12 = rng.uniform(0, 10, n)
+    m21 = rng.uniform(0, 10, n)
+    return np.stack([s, nu1, nu2, T, m12, m21], axis=1)
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# FP64 FMA peak measured on this machine's GB300 with a DFMA throughput loop
+# (1.89 DFMA/clk/SM at 2070 MHz, 152 SMs): see profiles/fp64_pipe_peak.md.
+FP64_PEAK_TFLOPS = 1.19
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        busy = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": float(np.median(busy)), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("BENCH_BACKEND") != "gloo" else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(torch, world, x):
+    if world == 1:
+        return x
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def point_sweeps(steps, pts_l):
+    return int(np.sum(steps)) * int(sum(2 * L * L for L in pts_l))
+
+
+# ------------------------------------------------------------------ CPU arm
+
+def _cpu_one(args):
+    """One extrapolated IM spectrum on the CPU restatement (Python time loop
+    over the C sweeps, as the reference runs)."""
+    p, pts_l, ns = args
+    from oracle import numerics as onum
+    t = time.perf_counter()
+    onum.extrap_model(onum.IM, p, ns, pts_l)
+    return time.perf_counter() - t
+
+
+def cpu_rate(draws, steps_all, budget_s, cores):
+    """Spectra/s of the CPU restatement on `cores` processes, measured on a
+    sample of instances and scaled to the workload by point-sweeps."""
+    import multiprocessing as mp
+    from oracle import clib
+    clib.build()
+    ps_per_inst = steps_all * sum(2 * L * L for L in PTS_L)
+    total_ps = float(np.sum(ps_per_inst))
+    # a sample spread over the cost distribution, sized to the budget
+    rng = np.random.default_rng(123)
+    idx = rng.permutation(len(draws))
+    ns_per_ps = 25e-9  # rough single-core cost, only to size the sample
+    chosen, work = [], 0.0
+    for i in idx:
+        c = ps_per_inst[i] * ns_per_ps
+        if c > budget_s * cores / 4:
+            continue
+        chosen.append(i)
+        work += c
+        if work > budget_s * cores * 0.8:
+            break
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        pool.map(_cpu_one, [(draws[i], PTS_L, NS) for i in chosen], chunksize=1)
+    wall = time.perf_counter() - t0
+    sample_ps = float(np.sum(ps_per_inst[chosen]))
+    ps_rate = sample_ps / wall
+    value = len(draws) * ps_rate / total_ps
+    return value, len(chosen), wall, sample_ps
+
+
+def run_reference(a, world, rank):
+    if rank != 0:
+        return 0
+    from dadi_gb300 import batch
+    draws = im_draws(NINST, 0)
+    steps = batch.count_steps(batch.im_instances(draws))
+    cores = os.cpu_count() or 1
+    vals = []
+    for it in range(a.warmup + a.steps):
+        v, n, wall, sps = cpu_rate(draws, steps, a.cpu_budget, cores)
+        if it >= a.warmup:
+            vals.append((v, n, wall, sps))
+    v = float(np.mean([x[0] for x in vals]))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "spectra/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": float(np.mean([x[2] for x in vals])) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seed-0 IM parameter draws)",
+        "config": {"workload": "batched 2-D IM, 4096 instances, pts [80,90,100], ns (40,40), "
+                               "extrapolated + Poisson ll", "global_batch": NINST,
+                   "pts_l": list(PTS_L), "ns": list(NS)},
+        "cpu_baseline": {"value": v, "unit": "spectra/s", "cores": cores, "kind": "port",
+                         "sample": "%d seed-0 instances per step (%.3g point-sweeps, %.1f s on "
+                                   "%d processes), scaled to the 4096-instance workload by "
+                                   "point-sweeps" % (vals[-1][1], vals[-1][3], vals[-1][2], cores)},
+        "e2e": {"value": v, "unit": "spectra/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def run_ours(a, world, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    from dadi_gb300 import batch, build
+    build.build()
+    from oracle import numerics as onum  # noqa: F401  (checker only: cpu_baseline leg)
+    draws = im_draws(NINST, rank)
+    rec = batch.im_instances(draws)
+    steps = batch.count_steps(rec)
+    ps = point_sweeps(steps, PTS_L)
+    eng = batch.Batch2D(PTS_L, NS, gam_placement=a.gam)
+    # synthetic observed data: Poisson(5e4 * model(set 0)), as a device tensor
+    fs0, _, _ = eng.run(im_draws(1, 0))
+    obs = np.random.default_rng(0).poisson(5e4 * fs0.cpu().numpy()[0]).astype(np.float64)
+    d_obs = torch.from_numpy(obs).cuda()
+    flush = torch.empty(256 * 1024 * 1024 // 8, dtype=torch.float64, device="cuda")
+    order_cache = {}
+
+    def step_device():
+        # parameters resident on the device side of the API: the records and
+        # the work order are prepared once; the step integrates, contracts,
+        # extrapolates and scores everything on the GPU.
+        if "order" not in order_cache:
+            cost = (steps[:, None] * np.array(PTS_L)[None, :] ** 2).ravel()
+            order_cache["order"] = np.argsort(-cost, kind="stable").astype(np.int32)
+        phis, status = eng.integrate(rec, order=order_cache["order"])
+        fs = eng.extrapolate(eng.spectra(phis))
+        ll = eng.loglik(fs, d_obs, 5e4)
+        return fs, ll, status
+
+    # warm-up
+    for _ in range(a.warmup):
+        step_device()
+    torch.cuda.synchronize()
+
+    # timed region: device-resident inputs, per-kernel events for the roofline
+    clocks = ClockSampler(local)
+    clocks.start()
+    kern_ms = []
+    barrier(world)
+    torch.cuda.synchronize()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    total_ms = 0.0
+    for _ in range(a.steps):
+        flush.fill_(1.0)  # L2 flush between iterations (256 MB > 129 MB L2)
+        torch.cuda.synchronize()
+        t_start.record()
+        k0 = torch.cuda.Event(enable_timing=True)
+        k1 = torch.cuda.Event(enable_timing=True)
+        k0.record()
+        phis, status = eng.integrate(rec, order=order_cache["order"])
+        k1.record()
+        fs = eng.extrapolate(eng.spectra(phis))
+        ll = eng.loglik(fs, d_obs, 5e4)
+        t_end.record()
+        torch.cuda.synchronize()
+        total_ms += t_start.elapsed_time(t_end)
+        kern_ms.append(k0.elapsed_time(k1))
+    barrier(world)
+    clk = clocks.stop()
+    total_ms = max_over_ranks(torch, world, total_ms)
+    ms_per_step = total_ms / a.steps
+    value = world * NINST / (ms_per_step / 1e3)
+    bad = int((status != 0).sum())
+
+    # end to end through the public API (host arrays in and out)
+    e2e_ms = 0.0
+    h2d = draws.nbytes + obs.nbytes
+    d2h = 0
+    for _ in range(max(1, a.steps)):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fs_d, ll_d, st_d = eng.run(draws, data=obs, scale=5e4)
+        fs_h = fs_d.cpu().numpy()
+        ll_h = ll_d.cpu().numpy()
+        e2e_ms += (time.perf_counter() - t0) * 1e3
+        d2h = fs_h.nbytes + ll_h.nbytes
+    e2e_ms = max_over_ranks(torch, world, e2e_ms / max(1, a.steps))
+    e2e_value = world * NINST / (e2e_ms / 1e3)
+
+    # plain one-at-a-time drop-in path on a sample, scaled by point-sweeps
+    plain = None
+    if rank == 0 and not a.no_plain:
+        from dadi_gb300 import models, numerics
+        f = numerics.make_extrap_func(models.IM)
+        rng = np.random.default_rng(7)
+        sample = [i for i in rng.permutation(NINST) if 500 <= steps[i] <= 3000][:3]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in sample:
+            f(draws[i], NS, list(PTS_L))
+        wall = time.perf_counter() - t0
+        sps = point_sweeps(steps[sample], PTS_L)
+        plain = {"value": NINST * (sps / wall) / ps, "unit": "spectra/s",
+                 "sample": "%d seed-0 instances through the one-at-a-time drop-in "
+                           "(two_pops per grid), scaled by point-sweeps" % len(sample)}
+
+    # CPU baseline (oracle restatement, bounded sample), rank 0 only
+    cpu = None
+    if rank == 0 and not a.no_cpu:
+        cores = os.cpu_count() or 1
+        v, n, wall, sps = cpu_rate(draws, steps, a.cpu_budget, cores)
+        cpu = {"value": v, "unit": "spectra/s", "cores": cores, "kind": "port",
+               "sample": "%d seed-0 instances (%.3g point-sweeps) on %d processes in %.1f s, "
+                         "scaled to the 4096-instance workload by point-sweeps"
+                         % (n, sps, cores, wall)}
+
+    if rank != 0:
+        return 0
+    peak, src = load_peaks()
+    kmean = float(np.mean(kern_ms)) / 1e3
+    achieved = ps * BYTES_PER_PS / kmean / 1e9
+    traffic = None
+    tr_file = os.path.join(ROOT, "profiles", "traffic_integrate2d.json")
+    if os.path.exists(tr_file):
+        with open(tr_file) as fh:
+            tr = json.load(fh)
+        traffic = tr.get("bytes_per_point_sweep", 0) * ps
+    fp64_achieved = ps * FLOPS_PER_PS / kmean / 1e12
+    fp64_instr = ps * FP64_INSTR_PER_PS * 2 / kmean / 1e12
+    line = {
+        "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seed-%d IM parameter draws; observed spectrum Poisson(5e4*model))"
+                % rank,
+        "config": {"workload": "batched 2-D IM, 4096 instances, pts [80,90,100], ns (40,40), "
+                               "extrapolated + Poisson ll",
+                   "global_batch": NINST * world, "pts_l": list(PTS_L), "ns": list(NS),
+                   "point_sweeps_per_step": ps, "parallelism": "replicas x%d" % world,
+                   "l2": "flushed between iterations (256 MB write); phi outputs 803 MB > L2",
+                   "gam_placement": a.gam},
+        "e2e": {"value": e2e_value, "unit": "spectra/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": src,
+                     "kernel": "k_integrate2d",
+                     "note": "FP64-pipe bound: phi stays in shared memory, so HBM carries "
+                             "little; see fp64"},
+        "fp64": {"algorithmic_tflops": fp64_achieved,
+                 "pipe_tflops": fp64_instr, "peak_tflops": FP64_PEAK_TFLOPS,
+                 "frac": fp64_instr / FP64_PEAK_TFLOPS,
+                 "note": "pipe_tflops counts %d FP64 instructions (as FMAs) per point-sweep"
+                         % FP64_INSTR_PER_PS},
+        "kernel_ms_per_step": kmean * 1e3,
+        "clocks": clk,
+        "gpu_launches": a.steps,
+        "failed_instances": bad,
+        "plain": plain,
+        "batched_over_plain": (value / plain["value"]) if plain else None,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0,
+                    help="seconds of CPU work per CPU measurement")
+    ap.add_argument("--gam", type=int, default=0, help="0 auto, 1 shared, 2 workspace")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    a = ap.parse_args()
+    world, rank, local = dist_init()
+    if a.impl == "reference":
+        rc = run_reference(a, world, rank)
+    else:
+        rc = run_ours(a, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,144 @@
+"""ctypes binding of libdadi_gb300.so, the C ABI declared in include/dadi_gb300.h.
+
+There is no CPU fallback: importing the package works without a GPU (so the
+library and its symbols can be inspected), but every compute call requires
+the compiled library and a CUDA device and raises otherwise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libdadi_gb300.so")
+
+DGB_OK = 0
+DGB_ERR_ARG = -1
+DGB_ERR_CUDA = -2
+DGB_ERR_UNSUPPORTED = -3
+DGB_ERR_WORKSPACE = -4
+
+PF_CONST, PF_EXPGROW, PF_EXPLOG, PF_LINEAR = 0, 1, 2, 3
+ST_BADPARAM, ST_STEPCAP, ST_NONFINITE, ST_ZERODT = 1, 2, 4, 8
+
+#: Every entry point the header declares (checked by the test suite).
+EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
+           "dgb_tridiag_batch", "dgb_implicit_sweep", "dgb_implicit_precalc_sweep",
+           "dgb_integrate_table", "dgb_integrate_precalc", "dgb_batch2d_integrate",
+           "dgb_batch2d_count_steps"]
+
+
+class PForm(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("pad_", ctypes.c_int),
+                ("a", ctypes.c_double), ("b", ctypes.c_double), ("c", ctypes.c_double)]
+
+
+class Inst2D(ctypes.Structure):
+    _fields_ = [("T", ctypes.c_double), ("initial_t", ctypes.c_double),
+                ("nu", PForm * 2), ("m12", PForm), ("m21", PForm), ("gamma", PForm * 2),
+                ("h", PForm * 2), ("theta0", PForm),
+                ("frozen_mask", ctypes.c_int), ("nomut_mask", ctypes.c_int)]
+
+
+class Settings(ctypes.Structure):
+    _fields_ = [("timescale_factor", ctypes.c_double), ("old_timescale_factor", ctypes.c_double),
+                ("use_old_timestep", ctypes.c_int), ("use_delj_trick", ctypes.c_int),
+                ("gam_placement", ctypes.c_int), ("pad_", ctypes.c_int)]
+
+
+class DgbError(RuntimeError):
+    """A libdadi_gb300 call returned a non-zero status."""
+
+    def __init__(self, status, what):
+        self.status = status
+        super().__init__("%s failed: %s (status %d)" % (what, status_string(status), status))
+
+
+_lib = None
+_vp = ctypes.c_void_p
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _declare(L):
+    i, d, sz, lg = ctypes.c_int, ctypes.c_double, ctypes.c_size_t, ctypes.c_long
+    sig = {
+        "dgb_abi_version": (i, []),
+        "dgb_status_string": (ctypes.c_char_p, [i]),
+        "dgb_workspace_bytes": (sz, [i, i, i, lg]),
+        "dgb_tridiag_batch": (i, [_vp, _vp, _vp, _vp, _vp, i, i, _vp, sz, _vp]),
+        "dgb_implicit_sweep": (i, [_vp, i, i, i, _vp, d, _dp, d, d, d, d, i, _vp, sz, _vp]),
+        "dgb_implicit_precalc_sweep": (i, [_vp, i, i, i, _vp, _vp, _vp, d, _vp, sz, _vp]),
+        "dgb_integrate_table": (i, [_vp, i, i, _vp, _vp, i, i, i, i, _vp, sz, _vp]),
+        "dgb_integrate_precalc": (i, [_vp, i, i, _vp, _vp, _vp, i, d, i, i, _vp, sz, _vp]),
+        "dgb_batch2d_integrate": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp,
+                                      _vp, _vp, lg, ctypes.POINTER(Settings), _vp, sz, _vp]),
+        "dgb_batch2d_count_steps": (i, [ctypes.POINTER(Inst2D), i, ctypes.POINTER(Settings), lg,
+                                        ctypes.POINTER(ctypes.c_long)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+
+
+def lib():
+    """The loaded library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libdadi_gb300.so is not built (%s); run "
+                              "`python -c 'import __graft_entry__ as g; g.build()'` or "
+                              "`python dadi_gb300/build.py`" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def status_string(status):
+    try:
+        return lib().dgb_status_string(int(status)).decode()
+    except ImportError:
+        return "status %d" % status
+
+
+def check(status, what):
+    if status != DGB_OK:
+        raise DgbError(status, what)
+
+
+# ---------------------------------------------------------------- devices
+
+def require_cuda():
+    """torch with a visible CUDA device, or a RuntimeError (no CPU fallback)."""
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("dadi_gb300 needs a CUDA device; none is visible")
+    lib()
+    return torch
+
+
+def stream_handle(torch):
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def dptr(t):
+    """Device pointer of a contiguous torch tensor."""
+    assert t.is_contiguous()
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def to_device(torch, arr, dtype=None):
+    a = np.ascontiguousarray(arr, dtype=dtype if dtype is not None else np.float64)
+    return torch.from_numpy(a).to("cuda", non_blocking=False)
+
+
+def workspace(torch, nbytes):
+    n = max(int(nbytes), 1)
+    return torch.empty(n, dtype=torch.uint8, device="cuda"), n
+
+
+def settings_struct(timescale_factor=1e-3, old_timescale_factor=0.1, use_old_timestep=False,
+                    use_delj_trick=False, gam_placement=0):
+    return Settings(float(timescale_factor), float(old_timescale_factor),
+                    int(bool(use_old_timestep)), int(bool(use_delj_trick)), int(gam_placement), 0)

@@ -1,0 +1,181 @@
+"""Batched 2-population engine: thousands of integrations in one launch.
+
+Each (instance, grid) pair is one work item of a persistent kernel
+(dgb_batch2d_integrate): the parametric schedule is evaluated on the device
+with the reference's operation order (dadi/Integration.py:147-176, 355-386),
+phi stays in shared memory for the whole loop, and CTAs pull items
+longest-first from an atomic counter, so instances with 11 or 20,000 steps
+balance across the SMs.  The spectra, their Richardson extrapolation and the
+Poisson likelihood are computed on the device afterwards, so only parameters
+go in and spectra / likelihoods come out.
+
+This is the GPU form of evaluating dadi.Numerics.make_extrap_func(model) for
+many parameter sets (dadi/Numerics.py:334-475; the reference parallelises such
+work with host processes, dadi/DFE/Cache2D_mod.py:117-167).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib, integration, numerics, phimanip, spectrum
+
+INST_DTYPE = np.dtype({
+    "names": ["T", "initial_t", "nu", "m12", "m21", "gamma", "h", "theta0", "frozen", "nomut"],
+    "formats": ["f8", "f8", ("f8", (2, 4)), ("f8", 4), ("f8", 4), ("f8", (2, 4)),
+                ("f8", (2, 4)), ("f8", 4), "i4", "i4"],
+    "offsets": [0, 8, 16, 80, 112, 144, 208, 272, 304, 308],
+    "itemsize": 312})
+
+
+def _pf(kind, a=0.0, b=0.0, c=0.0):
+    """A dgb_pform packed as 4 doubles (kind stored in the first int)."""
+    v = np.zeros(4)
+    v.view(np.int32)[0] = kind
+    v[1], v[2], v[3] = a, b, c
+    return v
+
+
+def _pf_array(kind, a, b=None, c=None):
+    n = len(a)
+    out = np.zeros((n, 4))
+    out.view(np.int32)[:, 0] = kind
+    out[:, 1] = a
+    if b is not None:
+        out[:, 2] = b
+    if c is not None:
+        out[:, 3] = c
+    return out
+
+
+def im_instances(params, initial_t=0.0, theta0=1.0):
+    """dgb_inst2d records of Demographics2D.IM (dadi/Demographics2D.py:297-307)
+    for rows (s, nu1, nu2, T, m12, m21): nu1(t) = s (nu1/s)**(t/T),
+    nu2(t) = (1-s) (nu2/(1-s))**(t/T), constant migration."""
+    p = np.asarray(params, dtype=np.float64).reshape(-1, 6)
+    n = len(p)
+    s, nu1, nu2, T, m12, m21 = p.T
+    rec = np.zeros(n, dtype=INST_DTYPE)
+    rec["T"] = T
+    rec["initial_t"] = initial_t
+    rec["nu"][:, 0] = _pf_array(_lib.PF_EXPGROW, s, nu1, T)
+    rec["nu"][:, 1] = _pf_array(_lib.PF_EXPGROW, 1 - s, nu2, T)
+    rec["m12"] = _pf_array(_lib.PF_CONST, m12)
+    rec["m21"] = _pf_array(_lib.PF_CONST, m21)
+    rec["gamma"][:, 0] = _pf_array(_lib.PF_CONST, np.zeros(n))
+    rec["gamma"][:, 1] = _pf_array(_lib.PF_CONST, np.zeros(n))
+    rec["h"][:, 0] = _pf_array(_lib.PF_CONST, np.full(n, 0.5))
+    rec["h"][:, 1] = _pf_array(_lib.PF_CONST, np.full(n, 0.5))
+    rec["theta0"] = _pf_array(_lib.PF_CONST, np.full(n, theta0))
+    return rec
+
+
+def settings_from_globals(gam_placement=0):
+    tsf, otsf, old, delj = integration.current_settings()
+    return _lib.settings_struct(tsf, otsf, old, delj, gam_placement)
+
+
+def count_steps(rec, settings=None, max_steps=10 ** 8):
+    """Steps each instance takes (host C, used to order work longest-first)."""
+    rec = np.ascontiguousarray(rec, dtype=INST_DTYPE)
+    out = np.zeros(len(rec), dtype=np.int64)
+    st = settings or settings_from_globals()
+    rc = _lib.lib().dgb_batch2d_count_steps(
+        rec.ctypes.data_as(ctypes.POINTER(_lib.Inst2D)), len(rec), ctypes.byref(st),
+        int(max_steps), out.ctypes.data_as(ctypes.POINTER(ctypes.c_long)))
+    _lib.check(rc, "dgb_batch2d_count_steps")
+    return out
+
+
+class Batch2D:
+    """Fixed grids and sample sizes; `run` integrates a batch of instances.
+
+    pts_l: grid sizes (default grids, dadi/Numerics.py:215-233) used for the
+    Richardson extrapolation; ns: sample sizes of the spectra.  The initial
+    density is the equilibrium phi_1D split to 2-D (dadi/PhiManip.py:12-234),
+    shared by every instance.
+    """
+
+    def __init__(self, pts_l=(80, 90, 100), ns=(40, 40), max_steps=10 ** 7, gam_placement=0):
+        self.torch = _lib.require_cuda()
+        torch = self.torch
+        self.pts_l = list(pts_l)
+        self.ns = tuple(ns)
+        self.max_steps = int(max_steps)
+        self.gam_placement = gam_placement
+        self.xxs = [numerics.default_grid(p) for p in self.pts_l]
+        phi0 = [phimanip.phi_1D_to_2D(xx, phimanip.phi_1D(xx)) for xx in self.xxs]
+        self.d_xx = _lib.to_device(torch, np.concatenate(self.xxs))
+        self.d_phi0 = _lib.to_device(torch, np.concatenate([p.ravel() for p in phi0]))
+        self.Ls = (ctypes.c_int * len(self.pts_l))(*self.pts_l)
+        self.x_l = [xx[1] for xx in self.xxs]
+        self.mask = np.zeros((ns[0] + 1, ns[1] + 1), dtype=bool)
+        self.mask.flat[0] = self.mask.flat[-1] = True
+
+    def integrate(self, rec, order=None):
+        """Run the integrations of dgb_inst2d records `rec` (host structured
+        array).  Returns (list of per-grid phi tensors (n, L, L), status)."""
+        torch = self.torch
+        n = len(rec)
+        ng = len(self.pts_l)
+        st = settings_from_globals(self.gam_placement)
+        if order is None:
+            steps = count_steps(rec, st, self.max_steps)
+            cost = (steps[:, None] * np.array(self.pts_l)[None, :] ** 2).ravel()
+            order = np.argsort(-cost, kind="stable").astype(np.int32)
+        d_rec = torch.from_numpy(np.ascontiguousarray(rec).view(np.uint8)).to("cuda")
+        d_order = torch.from_numpy(np.ascontiguousarray(order, dtype=np.int32)).to("cuda")
+        total = sum(n * L * L for L in self.pts_l)
+        d_out = torch.empty(total, dtype=torch.float64, device="cuda")
+        d_status = torch.zeros(n, dtype=torch.int32, device="cuda")
+        nws = _lib.lib().dgb_workspace_bytes(1, 2, max(self.pts_l), n * ng)
+        ws, nws = _lib.workspace(torch, nws)
+        rc = _lib.lib().dgb_batch2d_integrate(
+            _lib.dptr(d_rec), n, self.Ls, ng, _lib.dptr(self.d_xx), _lib.dptr(self.d_phi0),
+            _lib.dptr(d_out), _lib.dptr(d_order), _lib.dptr(d_status), self.max_steps,
+            ctypes.byref(st), _lib.dptr(ws), nws, _lib.stream_handle(torch))
+        _lib.check(rc, "dgb_batch2d_integrate")
+        phis, off = [], 0
+        for L in self.pts_l:
+            phis.append(d_out[off:off + n * L * L].view(n, L, L))
+            off += n * L * L
+        return phis, d_status
+
+    def spectra(self, phis):
+        """Per-grid raw spectra (n, n1+1, n2+1) on the device."""
+        return [spectrum.from_phi_2D_batch(self.torch, p, self.ns[0], self.ns[1], xx)
+                for p, xx in zip(phis, self.xxs)]
+
+    def extrapolate(self, fs_l, fail_mag=10):
+        """Richardson extrapolation with the fail_mag guard
+        (dadi/Numerics.py:425-464) on the device."""
+        torch = self.torch
+        x = self.x_l
+        if len(fs_l) == 1:
+            return fs_l[0].clone()
+        if len(fs_l) == 2:
+            ex = numerics.linear_extrap(fs_l, x)
+        else:
+            ex = numerics.quadratic_extrap(fs_l, x)
+        best = fs_l[int(np.argmin(x))]
+        failed = torch.abs(torch.log10(ex / best)) > fail_mag
+        return torch.where(failed, best, ex)
+
+    def loglik(self, fs, data, scale=1.0):
+        """Poisson log-likelihood of scale*fs against data over unmasked entries
+        with positive model (dadi/Inference.py:466-509); shape (n,)."""
+        torch = self.torch
+        model = scale * fs
+        d = data if torch.is_tensor(data) else _lib.to_device(torch, data)
+        ok = (~torch.from_numpy(self.mask).to(model.device)) & (model > 0)
+        term = -model + d * torch.log(torch.where(ok, model, torch.ones_like(model))) \
+            - torch.lgamma(d + 1.0)
+        return torch.where(ok, term, torch.zeros_like(term)).sum(dim=(1, 2))
+
+    def run(self, params, data=None, scale=1.0):
+        """IM parameter rows -> (extrapolated spectra (n, n1+1, n2+1), ll or
+        None, status), all CUDA tensors."""
+        rec = im_instances(params)
+        phis, status = self.integrate(rec)
+        fs = self.extrapolate(self.spectra(phis))
+        ll = self.loglik(fs, data, scale) if data is not None else None
+        return fs, ll, status

@@ -1,0 +1,578 @@
+// Fused per-axis ADI sweep for 1-D, 3-D and 4-D densities (and 2-D grids too
+// large for the shared-memory-resident kernel), the constant-coefficient
+// sweep, a batched tridiagonal solver, and the C ABI entry points that drive
+// them.
+//
+// A sweep kernel launch handles every line of one axis.  Each CTA stages a
+// tile of NT lines x L points in shared memory ([point][line] layout, pitch
+// NT+1, so line-parallel accesses are bank-conflict free): strided axes load
+// with one coalesced row of NT lines per point, the contiguous axis with a
+// linear cooperative copy of its NT*L contiguous doubles.  Coefficients are
+// rebuilt from per-axis vectors (see dgb_common.cuh), mutation injection is
+// fused into the first sweep of a step, and the Thomas gam scratch stays in
+// shared memory, so a sweep reads and writes phi exactly once.
+//
+// Reference: implicit_1Dx / implicit_3D{x,y,z} / implicit_4D{x,y,z,a}
+// (dadi/integration1D.c:7-66, integration3D.c:13-239, integration4D.c:13-321),
+// implicit_precalc_* (integration2D.c:162-217, integration3D.c:241-345),
+// tridiag_premalloc (dadi/tridiag.c:14-34).
+#include <algorithm>
+#include <cstring>
+
+#include "dgb_common.cuh"
+#include "dgb_internal.h"
+
+namespace dgb {
+
+struct NDArgs {
+    double *phi;
+    const double *xx;
+    int ndim, L, axis;
+    long nlines, S, LS; // lines, stride of the axis, L*S
+    // parameters: from table row `step` when table != null, else explicit
+    const double *table;
+    long step;
+    double nu, gamma, h, beta, dt, theta0;
+    double mig[DGB_MAX_DIM];
+    int inject_mask; // populations whose mutations are injected by this sweep
+    // constant-coefficient mode
+    const double *ca, *cb, *cc;
+    const double *dts;
+};
+
+__host__ __device__ inline size_t nd_smem_doubles(int L, int nt, bool delj)
+{
+    return (size_t)L * (nt + 1) + (size_t)L * nt + (size_t)(delj ? 10 : 5) * L + 6 * (size_t)L;
+}
+
+struct NDShared {
+    AxisScalars s;
+    double vscale;
+    double inj[DGB_MAX_DIM];
+};
+
+// Coordinates (all axes) of the first point of line `line` along `axis`.
+__device__ __forceinline__ long nd_line_base(const NDArgs &A, long line, int *coord)
+{
+    long outer = line / A.S, inner = line - outer * A.S;
+    long base = outer * A.LS + inner;
+    long rem = base;
+    for (int k = A.ndim - 1; k >= 0; k--) {
+        coord[k] = (int)(rem % A.L);
+        rem /= A.L;
+    }
+    return base;
+}
+
+__device__ void nd_load_params(const NDArgs &A, NDShared &Sh, const GridVecs &g)
+{
+    const int P = A.ndim, ax = A.axis;
+    AxisScalars &s = Sh.s;
+    double beta = A.beta;
+    if (A.table) {
+        const double *row = A.table + A.step * row_stride(P);
+        s.dt = row[0];
+        Sh.inj[0] = row[1]; // theta0, used below
+        s.nu = row[row_nu(P, ax)];
+        s.gamma = row[row_gamma(P, ax)];
+        s.h = row[row_h(P, ax)];
+        beta = row[row_beta(P)];
+        for (int j = 0; j < P; j++)
+            s.mig[j] = (j == ax) ? 0.0 : row[row_mig(P, ax, j)];
+    } else {
+        s.dt = A.dt;
+        Sh.inj[0] = A.theta0;
+        s.nu = A.nu;
+        s.gamma = A.gamma;
+        s.h = A.h;
+        for (int j = 0; j < P; j++)
+            s.mig[j] = (j == ax) ? 0.0 : A.mig[j];
+    }
+    double theta0 = Sh.inj[0];
+    s.inv_nu = 1.0 / s.nu;
+    double msum = 0;
+    for (int j = 0; j < P; j++)
+        if (j != ax)
+            msum = msum + s.mig[j];
+    s.msum = msum;
+    const int L = A.L;
+    s.B1s = 0.5 * (s.dt * g.dfac[0]);
+    s.B1e = -0.5 * (s.dt * g.dfac[L - 1]);
+    corner_bc(P, ax, s.mig, s.nu, s.gamma, s.h, g.x[0], g.x[L - 1], g.dx[0], g.dx[L - 2], s.dt,
+              s.bcs, s.bce);
+    // Vfunc_beta's factor in 1-D (dadi/integration_shared.c:8-10)
+    Sh.vscale = (P == 1) ? pow(beta + 1, 2) / (4 * beta) : 1.0;
+    double val = inject_value(P, s.dt, theta0, g.x[0], g.x[1], g.x[2]);
+    for (int k = 0; k < DGB_MAX_DIM; k++)
+        Sh.inj[k] = (A.inject_mask >> k & 1) ? val : 0.0;
+}
+
+__device__ void nd_grid_consts(const NDArgs &A, GridVecs &g)
+{
+    const int L = A.L;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        double x = A.xx[i];
+        g.x[i] = x;
+        g.xv[i] = x * (1. - x);
+        if (i < L - 1) {
+            double d = A.xx[i + 1] - x;
+            g.dx[i] = d;
+            g.ih[i] = 1.0 / (2 * d);
+            g.xInt[i] = 0.5 * (A.xx[i + 1] + x);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        if (i == 0)
+            g.dfac[i] = 2. / g.dx[0];
+        else if (i == L - 1)
+            g.dfac[i] = 2. / g.dx[L - 2];
+        else
+            g.dfac[i] = 2. / (g.dx[i] + g.dx[i - 1]);
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ void nd_carve(double *smem, int L, int nt, bool delj, double *&tile,
+                                         double *&gam, GridVecs &g, AxisVecs &v)
+{
+    double *p = smem;
+    tile = p;
+    p += (size_t)L * (nt + 1);
+    gam = p;
+    p += (size_t)L * nt;
+    g.x = p; p += L;
+    g.xv = p; p += L;
+    g.dfac = p; p += L;
+    g.xInt = p; p += L;
+    g.ih = p; p += L;
+    g.dx = p; p += L;
+    v.A1 = p; p += L;
+    v.A0 = p; p += L;
+    v.C1 = p; p += L;
+    v.C0 = p; p += L;
+    v.B0 = p; p += L;
+    if (delj) {
+        v.G = p; p += L;
+        v.Pv = p; p += L;
+        v.Qv = p; p += L;
+        v.VI = p; p += L;
+        v.DF = p; p += L;
+    }
+}
+
+// Load (dir=0) or store (dir=1) the CTA's tile of lines [l0, l0+n).
+__device__ __forceinline__ void nd_tile_io(const NDArgs &A, double *tile, int nt, long l0, int n,
+                                           bool store)
+{
+    const int L = A.L, tp = nt + 1;
+    if (A.S == 1) {
+        // contiguous axis: the n lines are n*L consecutive doubles
+        double *g0 = A.phi + l0 * L;
+        for (int idx = threadIdx.x; idx < n * L; idx += blockDim.x) {
+            int t = idx / L, p = idx - t * L;
+            if (store)
+                g0[idx] = tile[p * tp + t];
+            else
+                tile[p * tp + t] = g0[idx];
+        }
+    } else {
+        int t = threadIdx.x;
+        if (t < n) {
+            long line = l0 + t;
+            long outer = line / A.S, inner = line - outer * A.S;
+            double *g0 = A.phi + outer * A.LS + inner;
+            for (int p = 0; p < L; p++) {
+                if (store)
+                    g0[p * A.S] = tile[p * tp + t];
+                else
+                    tile[p * tp + t] = g0[p * A.S];
+            }
+        }
+    }
+}
+
+template <bool DELJ>
+__global__ void k_sweep_nd(NDArgs A)
+{
+    extern __shared__ __align__(16) double smem[];
+    __shared__ NDShared Sh;
+    const int nt = blockDim.x, L = A.L, P = A.ndim, ax = A.axis;
+    double *tile, *gam;
+    GridVecs g;
+    AxisVecs v;
+    nd_carve(smem, L, nt, DELJ, tile, gam, g, v);
+    nd_grid_consts(A, g);
+    if (threadIdx.x == 0)
+        nd_load_params(A, Sh, g);
+    __syncthreads();
+    for (int i = threadIdx.x; i < L; i += blockDim.x)
+        build_axis_entry(i, L, g, Sh.s, Sh.vscale, DELJ, v);
+    const long l0 = (long)blockIdx.x * nt;
+    const int n = (int)min((long)nt, A.nlines - l0);
+    nd_tile_io(A, tile, nt, l0, n, false);
+    __syncthreads();
+    // grid index of the corner coordinates (value exactly 0 / 1)
+    const int j0 = (g.x[0] == 0.0) ? 0 : -1;
+    const int j1 = (g.x[L - 1] == 1.0) ? L - 1 : -1;
+    const int t = threadIdx.x;
+    if (t < n) {
+        int coord[DGB_MAX_DIM];
+        nd_line_base(A, l0 + t, coord);
+        double W = 0;
+        double mo[DGB_MAX_DIM], oo[DGB_MAX_DIM];
+        int no = 0;
+        bool all0 = true, all1 = true;
+        int n1 = 0, k1 = -1;
+        for (int k = 0; k < P; k++) {
+            if (k == ax)
+                continue;
+            W = fma(Sh.s.mig[k], g.x[coord[k]], W);
+            mo[no] = Sh.s.mig[k];
+            oo[no] = g.x[coord[k]];
+            no++;
+            all0 = all0 && coord[k] == j0;
+            all1 = all1 && coord[k] == j1;
+            if (coord[k] == 1) {
+                n1++;
+                k1 = k;
+            } else if (coord[k] != 0) {
+                n1 = 99;
+            }
+        }
+        if (P == 1)
+            all0 = all1 = true; // 1-D applies both boundary terms unconditionally
+        const int tp = nt + 1;
+        // fused mutation injection (dadi/Integration.py:70-122)
+        if (A.inject_mask) {
+            if (n1 == 0 && Sh.inj[ax] != 0.0)
+                tile[1 * tp + t] += Sh.inj[ax];
+            if (n1 == 1 && Sh.inj[k1] != 0.0)
+                tile[0 * tp + t] += Sh.inj[k1];
+        }
+        double bs = all0 ? Sh.s.bcs : 0.0;
+        double be = all1 ? Sh.s.bce : 0.0;
+        if (DELJ)
+            solve_line_delj(tile + t, tp, gam + t, nt, L, mo, oo, no, bs, be, g, v);
+        else
+            solve_line(tile + t, tp, gam + t, nt, L, W, bs, be, v, Sh.s);
+    }
+    __syncthreads();
+    nd_tile_io(A, tile, nt, l0, n, true);
+}
+
+// Constant-coefficient sweep (reference arithmetic: b = bx + 1/dt,
+// r = (1/dt)*phi), coefficients read straight from the a/b/c arrays.
+__global__ void k_precalc_nd(NDArgs A)
+{
+    extern __shared__ __align__(16) double smem[];
+    const int nt = blockDim.x, L = A.L, P = A.ndim, ax = A.axis;
+    double *tile = smem, *gam = smem + (size_t)L * (nt + 1);
+    const int tp = nt + 1;
+    const long l0 = (long)blockIdx.x * nt;
+    const int n = (int)min((long)nt, A.nlines - l0);
+    const double dt = A.dts ? A.dts[A.step] : A.dt;
+    const double idt = 1 / dt;
+    nd_tile_io(A, tile, nt, l0, n, false);
+    __syncthreads();
+    const int t = threadIdx.x;
+    if (t < n) {
+        int coord[DGB_MAX_DIM];
+        long base = nd_line_base(A, l0 + t, coord);
+        if (A.inject_mask) {
+            int n1 = 0, k1 = -1;
+            for (int k = 0; k < P; k++) {
+                if (k == ax)
+                    continue;
+                if (coord[k] == 1) {
+                    n1++;
+                    k1 = k;
+                } else if (coord[k] != 0) {
+                    n1 = 99;
+                }
+            }
+            double val = inject_value(P, dt, A.theta0, A.xx[0], A.xx[1], A.xx[2]);
+            if (n1 == 0 && (A.inject_mask >> ax & 1))
+                tile[1 * tp + t] += val;
+            if (n1 == 1 && (A.inject_mask >> k1 & 1))
+                tile[0 * tp + t] += val;
+        }
+        double *ph = tile + t;
+        double *gm = gam + t;
+        const double *a = A.ca + base, *b = A.cb + base, *c = A.cc + base;
+        const long S = A.S;
+        double bet = b[0] + idt;
+        double inv = rcp_full(bet);
+        double u = (idt * ph[0]) * inv;
+        ph[0] = u;
+        for (int i = 1; i < L; i++) {
+            double gg = c[(i - 1) * S] * inv;
+            gm[i * nt] = gg;
+            double ai = a[i * S];
+            bet = fma(-ai, gg, b[i * S] + idt);
+            inv = rcp_full(bet);
+            u = fma(-ai, u, idt * ph[i * tp]) * inv;
+            ph[i * tp] = u;
+        }
+        for (int i = L - 2; i >= 0; i--) {
+            u = fma(-gm[(i + 1) * nt], u, ph[i * tp]);
+            ph[i * tp] = u;
+        }
+    }
+    __syncthreads();
+    nd_tile_io(A, tile, nt, l0, n, true);
+}
+
+__global__ void k_tridiag_batch(const double *a, const double *b, const double *c,
+                                const double *r, double *u, double *gam, int n, int batch)
+{
+    long s = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= batch)
+        return;
+    const double *as = a + s * n, *bs = b + s * n, *cs = c + s * n, *rs = r + s * n;
+    double *us = u + s * n, *gs = gam + s * n;
+    double bet = bs[0];
+    double inv = rcp_full(bet);
+    us[0] = rs[0] * inv;
+    for (int j = 1; j < n; j++) {
+        gs[j] = cs[j - 1] * inv;
+        bet = fma(-as[j], gs[j], bs[j]);
+        inv = rcp_full(bet);
+        us[j] = fma(-as[j], us[j - 1], rs[j]) * inv;
+    }
+    for (int j = n - 2; j >= 0; j--)
+        us[j] = fma(-gs[j + 1], us[j + 1], us[j]);
+}
+
+// ------------------------------------------------------------ host side
+
+static long ipow(int L, int p)
+{
+    long r = 1;
+    for (int i = 0; i < p; i++)
+        r *= L;
+    return r;
+}
+
+static int nd_threads(int L, long nlines)
+{
+    int nt = (L <= 48) ? 128 : 64;
+    if (nlines < nt)
+        nt = (int)std::max<long>(32, (nlines + 31) / 32 * 32);
+    return nt;
+}
+
+static void nd_fill(NDArgs &A, double *phi, int ndim, int L, int axis, const double *xx)
+{
+    A.phi = phi;
+    A.xx = xx;
+    A.ndim = ndim;
+    A.L = L;
+    A.axis = axis;
+    A.S = ipow(L, ndim - 1 - axis);
+    A.LS = A.S * L;
+    A.nlines = ipow(L, ndim - 1);
+}
+
+static int nd_launch_sweep(NDArgs &A, bool delj, cudaStream_t st)
+{
+    int nt = nd_threads(A.L, A.nlines);
+    size_t smem = nd_smem_doubles(A.L, nt, delj) * sizeof(double);
+    long nblocks = (A.nlines + nt - 1) / nt;
+    cudaError_t e;
+    if (delj) {
+        e = cudaFuncSetAttribute(k_sweep_nd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+        if (e != cudaSuccess)
+            return DGB_ERR_UNSUPPORTED;
+        k_sweep_nd<true><<<(unsigned)nblocks, nt, smem, st>>>(A);
+    } else {
+        e = cudaFuncSetAttribute(k_sweep_nd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+        if (e != cudaSuccess)
+            return DGB_ERR_UNSUPPORTED;
+        k_sweep_nd<false><<<(unsigned)nblocks, nt, smem, st>>>(A);
+    }
+    return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
+}
+
+static int nd_launch_precalc(NDArgs &A, cudaStream_t st)
+{
+    int nt = nd_threads(A.L, A.nlines);
+    size_t smem = ((size_t)A.L * (nt + 1) + (size_t)A.L * nt) * sizeof(double);
+    long nblocks = (A.nlines + nt - 1) / nt;
+    if (cudaFuncSetAttribute(k_precalc_nd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+        return DGB_ERR_UNSUPPORTED;
+    k_precalc_nd<<<(unsigned)nblocks, nt, smem, st>>>(A);
+    return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
+}
+
+static bool shape_ok(int ndim, int L) { return ndim >= 1 && ndim <= DGB_MAX_DIM && L >= 3; }
+
+} // namespace dgb
+
+using namespace dgb;
+
+// ------------------------------------------------------------------ C ABI
+
+extern "C" int dgb_abi_version(void) { return 1; }
+
+extern "C" const char *dgb_status_string(int status)
+{
+    switch (status) {
+    case DGB_OK:
+        return "ok";
+    case DGB_ERR_ARG:
+        return "invalid argument";
+    case DGB_ERR_CUDA:
+        return "CUDA error";
+    case DGB_ERR_UNSUPPORTED:
+        return "unsupported size or mode";
+    case DGB_ERR_WORKSPACE:
+        return "workspace missing or too small";
+    default:
+        return "unknown status";
+    }
+}
+
+extern "C" size_t dgb_workspace_bytes(int kind, int ndim, int L, long n)
+{
+    if (kind == 0)
+        return (ndim == 2) ? k2_table_ws_bytes(L) : 0;
+    if (kind == 1)
+        return k2_batch_ws_bytes(L, n);
+    if (kind == 2)
+        return (size_t)n * L * sizeof(double);
+    return 0;
+}
+
+extern "C" int dgb_tridiag_batch(const double *a, const double *b, const double *c,
+                                 const double *r, double *u, int n, int batch, void *ws,
+                                 size_t ws_bytes, void *stream)
+{
+    if (!a || !b || !c || !r || !u || n < 1 || batch < 0)
+        return DGB_ERR_ARG;
+    if (batch == 0)
+        return DGB_OK;
+    if (!ws || ws_bytes < (size_t)n * batch * sizeof(double))
+        return DGB_ERR_WORKSPACE;
+    int nt = 128;
+    k_tridiag_batch<<<(batch + nt - 1) / nt, nt, 0, (cudaStream_t)stream>>>(a, b, c, r, u,
+                                                                          (double *)ws, n, batch);
+    return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
+}
+
+extern "C" int dgb_implicit_sweep(double *phi, int ndim, int L, int axis, const double *xx,
+                                  double nu, const double *mig, double gamma, double h,
+                                  double beta, double dt, int use_delj_trick, void *ws,
+                                  size_t ws_bytes, void *stream)
+{
+    (void)ws;
+    (void)ws_bytes;
+    if (!phi || !xx || !shape_ok(ndim, L) || axis < 0 || axis >= ndim || (ndim > 1 && !mig))
+        return DGB_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    NDArgs A = {};
+    nd_fill(A, phi, ndim, L, axis, xx);
+    A.nu = nu;
+    A.gamma = gamma;
+    A.h = h;
+    A.beta = beta;
+    A.dt = dt;
+    for (int k = 0; k < ndim; k++)
+        A.mig[k] = (ndim > 1) ? mig[k] : 0.0;
+    return nd_launch_sweep(A, use_delj_trick != 0, st);
+}
+
+extern "C" int dgb_implicit_precalc_sweep(double *phi, int ndim, int L, int axis,
+                                          const double *a, const double *b, const double *c,
+                                          double dt, void *ws, size_t ws_bytes, void *stream)
+{
+    (void)ws;
+    (void)ws_bytes;
+    if (!phi || !a || !b || !c || !shape_ok(ndim, L) || axis < 0 || axis >= ndim)
+        return DGB_ERR_ARG;
+    NDArgs A = {};
+    nd_fill(A, phi, ndim, L, axis, nullptr);
+    A.ca = a;
+    A.cb = b;
+    A.cc = c;
+    A.dt = dt;
+    return nd_launch_precalc(A, (cudaStream_t)stream);
+}
+
+extern "C" int dgb_integrate_table(double *phi, int ndim, int L, const double *xx,
+                                   const double *table, int nsteps, int frozen_mask,
+                                   int nomut_mask, int use_delj_trick, void *ws,
+                                   size_t ws_bytes, void *stream)
+{
+    if (!phi || !xx || !table || !shape_ok(ndim, L) || nsteps < 0)
+        return DGB_ERR_ARG;
+    if (nsteps == 0)
+        return DGB_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (ndim == 2 && k2_smem_fits(L, false, use_delj_trick != 0, nullptr))
+        return k2_integrate_table(phi, L, xx, table, nsteps, frozen_mask, nomut_mask,
+                                  use_delj_trick, ws, ws_bytes, st);
+    const int active = ((1 << ndim) - 1) & ~frozen_mask & ~nomut_mask;
+    NDArgs A = {};
+    nd_fill(A, phi, ndim, L, 0, xx);
+    int rc = DGB_OK;
+    A.table = table;
+    for (long s = 0; s < nsteps; s++) {
+        bool first = true;
+        for (int ax = 0; ax < ndim; ax++) {
+            if (frozen_mask >> ax & 1)
+                continue;
+            A.axis = ax;
+            A.S = ipow(L, ndim - 1 - ax);
+            A.LS = A.S * L;
+            A.step = s;
+            A.inject_mask = first ? active : 0;
+            first = false;
+            rc = nd_launch_sweep(A, use_delj_trick != 0, st);
+            if (rc)
+                return rc;
+        }
+    }
+    return DGB_OK;
+}
+
+extern "C" int dgb_integrate_precalc(double *phi, int ndim, int L, const double *xx,
+                                     const double *abc, const double *dts, int nsteps,
+                                     double theta0, int frozen_mask, int nomut_mask, void *ws,
+                                     size_t ws_bytes, void *stream)
+{
+    (void)ws;
+    (void)ws_bytes;
+    if (!phi || !xx || !abc || !dts || !shape_ok(ndim, L) || nsteps < 0)
+        return DGB_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int active = ((1 << ndim) - 1) & ~frozen_mask & ~nomut_mask;
+    const long n = ipow(L, ndim);
+    NDArgs A = {};
+    nd_fill(A, phi, ndim, L, 0, xx);
+    A.dts = dts;
+    A.theta0 = theta0;
+    for (long s = 0; s < nsteps; s++) {
+        bool first = true;
+        for (int ax = 0; ax < ndim; ax++) {
+            if (frozen_mask >> ax & 1)
+                continue;
+            A.axis = ax;
+            A.S = ipow(L, ndim - 1 - ax);
+            A.LS = A.S * L;
+            A.step = s;
+            A.ca = abc + (3 * ax + 0) * n;
+            A.cb = abc + (3 * ax + 1) * n;
+            A.cc = abc + (3 * ax + 2) * n;
+            A.inject_mask = first ? active : 0;
+            first = false;
+            int rc = nd_launch_precalc(A, st);
+            if (rc)
+                return rc;
+        }
+    }
+    return DGB_OK;
+}

@@ -1,0 +1,48 @@
+"""The demographic models of the benchmark workloads, on the GPU integrator.
+
+split_mig and IM follow dadi/Demographics2D.py:133-167 and 268-309; growth3
+is three populations split from one (dadi/PhiManip.py:236-250) that each grow
+exponentially, nu_i(t) = nu0_i exp(log(nuF_i/nu0_i) t/T), with symmetric
+migration and per-population selection.
+"""
+import numpy as np
+
+from . import integration, numerics, phimanip, spectrum
+
+
+def split_mig(params, ns, pts):
+    nu1, nu2, T, m = params
+    xx = numerics.default_grid(pts)
+    phi = phimanip.phi_1D_to_2D(xx, phimanip.phi_1D(xx))
+    phi = integration.two_pops(phi, xx, T, nu1, nu2, m12=m, m21=m)
+    return spectrum.from_phi(phi, ns, (xx, xx))
+
+
+split_mig.__param_names__ = ['nu1', 'nu2', 'T', 'm']
+
+
+def IM(params, ns, pts):
+    s, nu1, nu2, T, m12, m21 = params
+    xx = numerics.default_grid(pts)
+    phi = phimanip.phi_1D_to_2D(xx, phimanip.phi_1D(xx))
+    nu1_func = lambda t: s * (nu1 / s) ** (t / T)
+    nu2_func = lambda t: (1 - s) * (nu2 / (1 - s)) ** (t / T)
+    phi = integration.two_pops(phi, xx, T, nu1_func, nu2_func, m12=m12, m21=m21)
+    return spectrum.from_phi(phi, ns, (xx, xx))
+
+
+IM.__param_names__ = ['s', 'nu1', 'nu2', 'T', 'm12', 'm21']
+
+
+def growth3(params, ns, pts):
+    """params = ((nu0_1..3), (nuF_1..3), (m12, m13, m23), (gamma1..3), T)."""
+    (nu0, nuF, (m12, m13, m23), g, T) = params
+    xx = numerics.default_grid(pts)
+    phi = phimanip.phi_1D_to_2D(xx, phimanip.phi_1D(xx))
+    phi = phimanip.phi_2D_to_3D_split_2(xx, phi)
+    nus = [(lambda a, b: (lambda t: a * np.exp(np.log(b / a) * t / T)))(a, b)
+           for a, b in zip(nu0, nuF)]
+    phi = integration.three_pops(phi, xx, T, nus[0], nus[1], nus[2],
+                                 m12=m12, m13=m13, m21=m12, m23=m23, m31=m13, m32=m23,
+                                 gamma1=g[0], gamma2=g[1], gamma3=g[2])
+    return spectrum.from_phi(phi, ns, (xx, xx, xx))

@@ -1,0 +1,172 @@
+/*
+ * dadi_gb300 -- C ABI of the GB300 (sm_103a) diffusion integrator.
+ *
+ * Every entry point takes plain pointers and sizes, returns an int status
+ * (DGB_OK == 0, negative on error, see dgb_status_string) and never throws.
+ * Array arguments are DEVICE pointers unless a comment says "host".  Arrays
+ * are C-ordered float64 with every axis of length L (dadi's square grids,
+ * dadi/integration_c.pyx:74-161).  `stream` is a cudaStream_t (NULL = legacy
+ * default stream); all work is enqueued on it and no call synchronises unless
+ * it says so.  `ws`/`ws_bytes` is caller-owned device scratch; query the size
+ * with dgb_workspace_bytes.  Calls are re-entrant: no global mutable state.
+ *
+ * Parameter tables.  A time loop (dadi/Integration.py:178-727) is described
+ * by one row per step, evaluated on the host exactly as the reference does
+ * (parameters at the *next* time, dt from the *current* ones):
+ *   row[0] = this_dt, row[1] = theta0, row[2+k] = nu_k, row[2+P+k] = gamma_k,
+ *   row[2+2P+k] = h_k, row[2+3P] = beta (1-D only, else 1),
+ *   row[3+3P+...] = m_kj for k = 0..P-1, j != k in increasing j.
+ * so a row holds DGB_ROW_STRIDE(P) doubles.
+ */
+#ifndef DADI_GB300_H
+#define DADI_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DGB_OK 0
+#define DGB_ERR_ARG (-1)         /* invalid argument (ValueError on the Python side) */
+#define DGB_ERR_CUDA (-2)        /* a CUDA call failed */
+#define DGB_ERR_UNSUPPORTED (-3) /* size or mode outside what the kernels handle */
+#define DGB_ERR_WORKSPACE (-4)   /* workspace missing or too small */
+
+#define DGB_MAX_DIM 4
+#define DGB_ROW_STRIDE(P) (3 + 3 * (P) + (P) * ((P)-1))
+
+/* Parametric time dependence of one parameter, evaluated on the device.
+ * Forms: CONST a; EXPGROW a*(b/a)**(t/c) (dadi/Demographics2D.py:302-303);
+ * EXPLOG a*exp(log(b/a)*t/c); LINEAR a + b*t. */
+#define DGB_PF_CONST 0
+#define DGB_PF_EXPGROW 1
+#define DGB_PF_EXPLOG 2
+#define DGB_PF_LINEAR 3
+typedef struct {
+    int kind;
+    int pad_;
+    double a, b, c;
+} dgb_pform;
+
+/* One 2-population integration for the batched engine: the arguments of
+ * Integration.two_pops (dadi/Integration.py:260-263) in parametric form. */
+typedef struct {
+    double T, initial_t;
+    dgb_pform nu[2], m12, m21, gamma[2], h[2], theta0;
+    int frozen_mask, nomut_mask;
+} dgb_inst2d;
+
+/* Per-instance status bits written by the batched engine. */
+#define DGB_ST_BADPARAM 1  /* a negative size/migration/theta0 or zero size */
+#define DGB_ST_STEPCAP 2   /* exceeded the per-integration step cap */
+#define DGB_ST_NONFINITE 4 /* dt or phi became non-finite */
+#define DGB_ST_ZERODT 8    /* timestep is zero (dadi/Integration.py:173-175) */
+
+/* Timestep settings read at call time (dadi/Integration.py:25,39,42-44). */
+typedef struct {
+    double timescale_factor;     /* default 1e-3 */
+    double old_timescale_factor; /* default 0.1 */
+    int use_old_timestep;        /* default 0 */
+    int use_delj_trick;          /* default 0 */
+    int gam_placement;           /* batched engine: 0 auto, 1 shared memory, 2 workspace */
+    int pad_;
+} dgb_settings;
+
+int dgb_abi_version(void);
+const char *dgb_status_string(int status);
+
+/* Scratch bytes needed by a call.  kind: 0 = dgb_integrate_table /
+ * dgb_integrate_precalc / the single sweeps, 1 = dgb_batch2d_integrate (with
+ * n = number of work items), 2 = dgb_tridiag_batch. */
+size_t dgb_workspace_bytes(int kind, int ndim, int L, long n);
+
+/* Batched Numerical-Recipes tridiagonal solve of `batch` independent systems
+ * of size n, system s stored at [s*n, (s+1)*n).  Replaces
+ * tridiag_cython.tridiag (dadi/tridiag_cython.pyx:14-18, dadi/tridiag.c:14-40). */
+int dgb_tridiag_batch(const double *a, const double *b, const double *c,
+                      const double *r, double *u, int n, int batch,
+                      void *ws, size_t ws_bytes, void *stream);
+
+/* One fully implicit sweep of phi along `axis`, in place.  mig (host, ndim
+ * doubles) holds the migration rates into the swept population from each
+ * other population (mig[axis] ignored).  Replaces integration_c.implicit_1Dx,
+ * implicit_2Dx/2Dy, implicit_3Dx/3Dy/3Dz and implicit_4Dx/4Dy/4Dz/4Da
+ * (dadi/integration_c.pyx:68-161; dadi/integration1D.c:7-66,
+ * integration2D.c:19-160, integration3D.c:13-239, integration4D.c:13-321). */
+int dgb_implicit_sweep(double *phi, int ndim, int L, int axis, const double *xx,
+                       double nu, const double *mig, double gamma, double h,
+                       double beta, double dt, int use_delj_trick,
+                       void *ws, size_t ws_bytes, void *stream);
+
+/* One constant-coefficient sweep: b excludes 1/dt; b+1/dt and r = phi/dt per
+ * element.  Replaces integration_c.implicit_precalc_2Dx/2Dy/3Dx/3Dy/3Dz
+ * (dadi/integration_c.pyx:86-131; dadi/integration2D.c:162-217,
+ * integration3D.c:241-345). */
+int dgb_implicit_precalc_sweep(double *phi, int ndim, int L, int axis,
+                               const double *a, const double *b, const double *c,
+                               double dt, void *ws, size_t ws_bytes, void *stream);
+
+/* A whole time loop of `nsteps` steps described by a parameter table (device,
+ * nsteps rows of DGB_ROW_STRIDE(ndim) doubles).  Each step injects mutations
+ * (skipped for populations in frozen_mask | nomut_mask) and sweeps every axis
+ * not in frozen_mask.  2-D grids up to the shared-memory limit run as one
+ * CTA with phi resident in shared memory for the whole loop; other shapes
+ * run one fused sweep kernel per axis per step.  Replaces the loops of
+ * Integration.one_pop/two_pops/three_pops/four_pops (dadi/Integration.py:
+ * 224-257, 340-386, 514-553, 635-726) and dadi.cuda.Integration.
+ * _two_pops_temporal_params / _three_pops_temporal_params /
+ * _four_pops_temporal_params (dadi/cuda/Integration.py:163-291, 376-545,
+ * 547-750). */
+int dgb_integrate_table(double *phi, int ndim, int L, const double *xx,
+                        const double *table, int nsteps, int frozen_mask,
+                        int nomut_mask, int use_delj_trick,
+                        void *ws, size_t ws_bytes, void *stream);
+
+/* A whole constant-coefficient time loop: abc holds 3*ndim arrays of L^ndim
+ * doubles (a_0, b_0, c_0, a_1, ...; b without 1/dt, as built by
+ * dadi/Integration.py:1057-1095, 1145-1222); dts (device) the nsteps step
+ * lengths; theta0 the mutation scale.  Replaces the precalc loops of
+ * _two_pops_const_params / _three_pops_const_params (dadi/Integration.py:
+ * 1108-1117, 1231-1241) and dadi.cuda.Integration._two_pops_const_params /
+ * _three_pops_const_params (dadi/cuda/Integration.py:89-161, 293-374). */
+int dgb_integrate_precalc(double *phi, int ndim, int L, const double *xx,
+                          const double *abc, const double *dts, int nsteps,
+                          double theta0, int frozen_mask, int nomut_mask,
+                          void *ws, size_t ws_bytes, void *stream);
+
+/* Batched 2-population engine: ninst integrations x ngrids grids, each
+ * (instance, grid) pair one work item of a persistent launch that evaluates
+ * the parametric schedule on the device and keeps phi in shared memory.
+ *   insts    device, ninst dgb_inst2d
+ *   Ls       host, ngrids grid sizes
+ *   xx_all   device, concatenated grids (sum of Ls doubles)
+ *   phi0_all device, concatenated initial densities (sum of L^2), shared by
+ *            every instance
+ *   phi_out  device, for grid g the block of ninst*L_g^2 doubles starting
+ *            after the blocks of grids < g (instance-major inside a block)
+ *   order    device, nwork = ninst*ngrids work ids (inst*ngrids + g), in the
+ *            order they should be started (longest first balances best)
+ *   status   device, ninst ints, OR-ed DGB_ST_* bits (caller zeroes them)
+ *   max_steps per-integration step cap (DGB_ST_STEPCAP when hit)
+ * This replaces many calls of Integration.two_pops with one launch; its
+ * parallel form is the reference's multi-process Cache2D generation
+ * (dadi/DFE/Cache2D_mod.py:117-167). */
+int dgb_batch2d_integrate(const dgb_inst2d *insts, int ninst, const int *Ls,
+                          int ngrids, const double *xx_all,
+                          const double *phi0_all, double *phi_out,
+                          const int *order, int *status, long max_steps,
+                          const dgb_settings *settings,
+                          void *ws, size_t ws_bytes, void *stream);
+
+/* Host helper: number of time steps each batched instance takes (the
+ * schedule of dadi/Integration.py:355-386 evaluated in C on the host), used
+ * to order work longest-first.  insts is a HOST array here. */
+int dgb_batch2d_count_steps(const dgb_inst2d *insts, int ninst,
+                            const dgb_settings *settings, long max_steps,
+                            long *steps_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,236 @@
+"""Generate the golden vectors in tests/golden/ by running the reference dadi.
+
+Run once in a container that holds the reference tree (it cannot run on a GPU
+host, which has no reference):
+
+    python tests/golden/make_golden.py [--ref /root/reference] [--build /tmp/dadi_ref]
+
+The reference is copied to the build directory, its pyproject.toml moved aside
+(its licence field trips the installed setuptools), its Cython extensions built
+in place, and the off-path imports demes / ruamel / nlopt replaced by stub
+modules before `import dadi`.  Every fixture is produced by dadi's own public
+functions; the inputs live in cases.py or are stored next to the outputs.
+"""
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+import time
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import cases  # noqa: E402
+
+
+def load_dadi(ref, build):
+    if not os.path.exists(os.path.join(build, "dadi", "integration_c.c")) or not any(
+            f.startswith("integration_c") and f.endswith(".so")
+            for f in os.listdir(os.path.join(build, "dadi"))):
+        if os.path.exists(build):
+            shutil.rmtree(build)
+        shutil.copytree(ref, build)
+        subprocess.run(["chmod", "-R", "u+w", build], check=True)
+        os.rename(os.path.join(build, "pyproject.toml"),
+                  os.path.join(build, "pyproject.toml.bak"))
+        subprocess.run([sys.executable, "setup.py", "build_ext", "--inplace"], cwd=build,
+                       check=True, stdout=subprocess.DEVNULL)
+
+    class _Stub(types.ModuleType):
+        def __getattr__(self, name):
+            if name.startswith("__"):
+                raise AttributeError(name)
+            return 0
+    for n in ["demes", "ruamel", "ruamel.yaml", "nlopt"]:
+        sys.modules.setdefault(n, _Stub(n))
+    sys.path.insert(0, build)
+    import dadi
+    return dadi
+
+
+def args_of(case):
+    return [cases.resolve(a) for a in case["args"]], {
+        k: cases.resolve(v) for k, v in case.get("kw", {}).items()}
+
+
+def gen_integrations(dadi, out):
+    for group, fn, nd in [("two", dadi.Integration.two_pops, 2),
+                          ("three", dadi.Integration.three_pops, 3),
+                          ("four", dadi.Integration.four_pops, 4),
+                          ("one", dadi.Integration.one_pop, 1)]:
+        lst = {"two": cases.TWO_POPS, "three": cases.THREE_POPS,
+               "four": cases.FOUR_POPS, "one": cases.ONE_POP}[group]
+        for case in lst:
+            xx = cases.grid(case["grid"], case["pts"])
+            phi0 = cases.initial_phi(case["seed"], (case["pts"],) * nd)
+            a, kw = args_of(case)
+            res = fn(phi0.copy(), xx, *a, **kw)
+            out["int_" + case["name"]] = res
+            out["int_" + case["name"] + "_phi0"] = phi0
+
+
+def gen_sweeps(dadi, out):
+    ic = dadi.integration_c
+    p = cases.SWEEP_PARAMS
+    rng = np.random.default_rng(77)
+    for name, nd, axis, pts, g in cases.SWEEPS:
+        xx = cases.grid(g, pts)
+        phi0 = rng.uniform(size=(pts,) * nd)
+        for delj in (0, 1):
+            phi = phi0.copy()
+            mig = [p["mig"][j] for j in range(nd) if j != axis]
+            if nd == 1:
+                ic.implicit_1Dx(phi, xx, p["nu"], p["gamma"], p["h"], p["beta"], p["dt"], delj)
+            else:
+                f = getattr(ic, "implicit_" + name)
+                f(phi, *([xx] * nd), p["nu"], *mig, p["gamma"], p["h"], p["dt"], delj)
+            out["sweep_%s_delj%d" % (name, delj)] = phi
+        out["sweep_%s_phi0" % name] = phi0
+    # constant-coefficient sweeps on random coefficient arrays
+    for nd in (2, 3):
+        pts = 9
+        phi0 = rng.uniform(size=(pts,) * nd)
+        for axis in range(nd):
+            a = -rng.uniform(size=phi0.shape)
+            c = -rng.uniform(size=phi0.shape)
+            b = rng.uniform(2, 3, size=phi0.shape)
+            phi = phi0.copy()
+            f = getattr(ic, "implicit_precalc_%dD%s" % (nd, "xyz"[axis]))
+            f(phi, a, b, c, 0.01)
+            key = "precalc_%dD%d" % (nd, axis)
+            out[key] = phi
+            out[key + "_abc"] = np.stack([a, b, c])
+            out[key + "_phi0"] = phi0
+
+
+def gen_host(dadi, out):
+    N = dadi.Numerics
+    PM = dadi.PhiManip
+    S = dadi.Spectrum
+    for pts in (5, 10, 40, 80, 100, 120):
+        out["grid_%d" % pts] = N.default_grid(pts)
+    xx = N.default_grid(30)
+    out["phi1d_snm"] = PM.phi_1D(xx)
+    out["phi1d_g2"] = PM.phi_1D(xx, nu=1.5, theta0=2.0, gamma=2.0)
+    out["phi1d_gm5"] = PM.phi_1D(xx, gamma=-5.0, beta=1.4)
+    out["phi1d_h03"] = PM.phi_1D(xx, gamma=-3.0, h=0.3)
+    phi2 = PM.phi_1D_to_2D(xx, PM.phi_1D(xx))
+    out["phi2d_split"] = phi2
+    xs = N.default_grid(12)
+    phi3 = PM.phi_2D_to_3D_split_2(xs, PM.phi_1D_to_2D(xs, PM.phi_1D(xs)))
+    out["phi3d_split2"] = phi3
+    out["phi4d_from3d"] = PM.phi_3D_to_4D(phi3, 0.3, 0.2, xs, xs, xs, xs)
+    rng = np.random.default_rng(5)
+    for nd, pts, ns in [(1, 25, (12,)), (2, 21, (8, 11)), (3, 11, (5, 6, 4)),
+                        (4, 7, (3, 4, 2, 3))]:
+        xg = N.default_grid(pts)
+        phi = rng.uniform(size=(pts,) * nd)
+        fs = S.from_phi(phi, ns, (xg,) * nd)
+        out["fromphi_%dd" % nd] = np.asarray(fs.data)
+        out["fromphi_%dd_phi" % nd] = phi
+        out["fromphi_%dd_ns" % nd] = np.array(ns)
+    # extrapolation and likelihoods
+    ys = [rng.uniform(1, 2, size=(5, 5)) for _ in range(3)]
+    xsl = [0.01, 0.008, 0.006]
+    out["extrap_in"] = np.stack(ys)
+    out["extrap_q"] = N.quadratic_extrap(ys, xsl)
+    out["extrap_l"] = N.linear_extrap(ys[:2], xsl[:2])
+    model = dadi.Spectrum(rng.uniform(0.1, 5, size=(6, 7)))
+    data = dadi.Spectrum(rng.poisson(3 * np.asarray(model)).astype(float))
+    out["ll_model"] = np.asarray(model.data)
+    out["ll_data"] = np.asarray(data.data)
+    out["ll"] = np.array(dadi.Inference.ll(model, data))
+    out["ll_multinom"] = np.array(dadi.Inference.ll_multinom(model, data))
+    a, b, c, r = rng.uniform(size=(4, 100))
+    b = b + 2
+    out["tridiag_abcr"] = np.stack([a, b, c, r])
+    out["tridiag_u"] = dadi.tridiag_cython.tridiag(a, b, c, r)
+
+
+def growth3(dadi):
+    def model(params, ns, pts):
+        (nu0, nuF, (m12, m13, m23), g, T) = params
+        xx = dadi.Numerics.default_grid(pts)
+        phi = dadi.PhiManip.phi_1D(xx)
+        phi = dadi.PhiManip.phi_1D_to_2D(xx, phi)
+        phi = dadi.PhiManip.phi_2D_to_3D_split_2(xx, phi)
+        nus = [(lambda a, b: (lambda t: a * np.exp(np.log(b / a) * t / T)))(a, b)
+               for a, b in zip(nu0, nuF)]
+        phi = dadi.Integration.three_pops(phi, xx, T, nus[0], nus[1], nus[2],
+                                          m12=m12, m13=m13, m21=m12, m23=m23,
+                                          m31=m13, m32=m23,
+                                          gamma1=g[0], gamma2=g[1], gamma3=g[2])
+        return dadi.Spectrum.from_phi(phi, ns, (xx, xx, xx))
+    return model
+
+
+def gen_models(dadi, out, big):
+    D2 = dadi.Demographics2D
+    sm = cases.SPLIT_MIG
+    f = dadi.Numerics.make_extrap_func(D2.split_mig)
+    out["splitmig_fs"] = np.asarray(f(sm["params"], sm["ns"], sm["pts_l"]).data)
+    for pts in sm["pts_l"]:
+        out["splitmig_fs_%d" % pts] = np.asarray(D2.split_mig(sm["params"], sm["ns"], pts).data)
+    fim = dadi.Numerics.make_extrap_func(D2.IM)
+    draws = cases.im_draws()
+    out["im_draws_head"] = draws[:64]
+    out["im_small_fs"] = np.asarray(fim(draws[0], (10, 10), [20, 25, 30]).data)
+    # IM spectra of a few seed-0 draws at the batched workload's grids
+    sel = [0, 1, 2, 3, 5]
+    for i in sel:
+        t = time.time()
+        out["im_fs_%d" % i] = np.asarray(fim(draws[i], (40, 40), [80, 90, 100]).data)
+        print("IM draw %d: %.1fs" % (i, time.time() - t), flush=True)
+    for pts in (80, 90, 100):
+        out["im0_fs_%d" % pts] = np.asarray(D2.IM(draws[0], (40, 40), pts).data)
+    if big:
+        g = cases.GROWTH3
+        t = time.time()
+        f3 = dadi.Numerics.make_extrap_func(growth3(dadi))
+        out["growth3_fs"] = np.asarray(f3(g["params"], g["ns"], g["pts_l"]).data)
+        print("growth3: %.1fs" % (time.time() - t), flush=True)
+    # observed data for the batched workload's likelihood: Poisson(5e4 * model(set 0))
+    m0 = fim(draws[0], (40, 40), [80, 90, 100])
+    obs = np.random.default_rng(0).poisson(5e4 * np.asarray(m0.data)).astype(float)
+    out["im_obs"] = obs
+    data = dadi.Spectrum(obs)
+    out["im_ll"] = np.array([dadi.Inference.ll(5e4 * fim(draws[i], (40, 40), [80, 90, 100]),
+                                               data) for i in sel])
+
+
+def gen_grad(dadi, out):
+    fim = dadi.Numerics.make_extrap_func(dadi.Demographics2D.IM)
+    draws = cases.im_draws()
+    p0 = draws[0]
+    data = dadi.Spectrum(np.random.default_rng(1).poisson(
+        1e4 * np.asarray(fim(p0, (10, 10), [20, 25, 30]).data)).astype(float))
+    func = lambda p: dadi.Inference.ll(1e4 * fim(p, (10, 10), [20, 25, 30]), data)
+    out["grad_p0"] = p0
+    out["grad_data"] = np.asarray(data.data)
+    out["grad_godambe"] = np.asarray(dadi.Godambe.get_grad(func, p0, 1e-4)).ravel()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--build", default="/tmp/dadi_ref")
+    ap.add_argument("--no-big", action="store_true", help="skip the 3-D model (~1 min)")
+    a = ap.parse_args()
+    dadi = load_dadi(a.ref, a.build)
+    for name, gen in [("integrate", gen_integrations), ("sweeps", gen_sweeps),
+                      ("host", gen_host), ("grad", gen_grad)]:
+        out = {}
+        gen(dadi, out)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print("wrote", name, len(out), flush=True)
+    out = {}
+    gen_models(dadi, out, not a.no_big)
+    np.savez_compressed(os.path.join(HERE, "models.npz"), **out)
+    print("wrote models", len(out))
+
+
+if __name__ == "__main__":
+    main()

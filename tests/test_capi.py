@@ -1,0 +1,62 @@
+"""The C ABI library builds, loads and exports every entry point the header
+declares; host-only entry points run without a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import cases
+from dadi_gb300 import _lib, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "dadi_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(dgb_[a-z0-9_]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.lib()
+
+
+def test_exports_every_declared_symbol(lib):
+    declared = header_functions()
+    assert declared, "no declarations parsed"
+    assert sorted(_lib.EXPORTS) == declared
+    for name in declared:
+        assert hasattr(lib, name), name
+
+
+def test_status_strings(lib):
+    assert lib.dgb_abi_version() == 1
+    assert lib.dgb_status_string(0) == b"ok"
+    assert b"workspace" in lib.dgb_status_string(_lib.DGB_ERR_WORKSPACE)
+
+
+def test_struct_layout():
+    assert ctypes.sizeof(_lib.PForm) == 32
+    assert ctypes.sizeof(_lib.Settings) == 32
+    assert ctypes.sizeof(_lib.Inst2D) == 16 + 9 * 32 + 8
+
+
+def test_count_steps_matches_python_schedule(lib):
+    from dadi_gb300 import batch
+    draws = cases.im_draws(16)
+    insts = batch.im_instances(draws)
+    steps = batch.count_steps(insts)
+    for p, n in zip(draws, steps):
+        s, nu1, nu2, T, m12, m21 = p
+        t, k = 0.0, 0
+        a = lambda t: s * (nu1 / s) ** (t / T)
+        b = lambda t: (1 - s) * (nu2 / (1 - s)) ** (t / T)
+        while t < T:
+            dt = min(1e-3 / max(0.25 / a(t), m12), 1e-3 / max(0.25 / b(t), m21))
+            t = t + min(dt, T - t)
+            k += 1
+        assert abs(k - n) <= 1

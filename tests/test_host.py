@@ -1,0 +1,118 @@
+"""Host-side pieces of the package against the reference's own outputs
+(golden vectors from dadi 2.4.3) and the oracle: grid, initial conditions,
+splits, from_phi, extrapolation, likelihoods, the per-step parameter table and
+the constant-coefficient builder.  No GPU needed."""
+import numpy as np
+import pytest
+
+import cases
+from dadi_gb300 import inference, integration, numerics, phimanip, spectrum
+from oracle import integration as oint
+from util import max_rel
+
+
+def test_grid_and_phi(golden):
+    h = golden["host"]
+    for pts in (5, 10, 40, 80, 100, 120):
+        assert np.array_equal(numerics.default_grid(pts), h["grid_%d" % pts])
+    xx = numerics.default_grid(30)
+    assert np.array_equal(phimanip.phi_1D(xx), h["phi1d_snm"])
+    assert np.array_equal(phimanip.phi_1D(xx, nu=1.5, theta0=2.0, gamma=2.0), h["phi1d_g2"])
+    assert np.array_equal(phimanip.phi_1D(xx, gamma=-5.0, beta=1.4), h["phi1d_gm5"])
+    assert max_rel(phimanip.phi_1D(xx, gamma=-3.0, h=0.3), h["phi1d_h03"]) < 1e-12
+    assert np.array_equal(phimanip.phi_1D_to_2D(xx, phimanip.phi_1D(xx)), h["phi2d_split"])
+    xs = numerics.default_grid(12)
+    p3 = phimanip.phi_2D_to_3D_split_2(xs, phimanip.phi_1D_to_2D(xs, phimanip.phi_1D(xs)))
+    assert np.array_equal(p3, h["phi3d_split2"])
+    assert np.array_equal(phimanip.phi_3D_to_4D(p3, 0.3, 0.2, xs, xs, xs, xs),
+                          h["phi4d_from3d"])
+
+
+@pytest.mark.parametrize("nd,pts", [(1, 25), (2, 21), (3, 11), (4, 7)])
+def test_from_phi(golden, nd, pts):
+    h = golden["host"]
+    xx = numerics.default_grid(pts)
+    fs = spectrum.from_phi(h["fromphi_%dd_phi" % nd], tuple(h["fromphi_%dd_ns" % nd]),
+                           (xx,) * nd)
+    assert np.array_equal(np.asarray(fs.data), h["fromphi_%dd" % nd])
+    assert fs.mask.flat[0] and fs.mask.flat[-1] and fs.extrap_x == xx[1]
+
+
+def test_extrap_and_ll(golden):
+    h = golden["host"]
+    ys = list(h["extrap_in"])
+    assert np.array_equal(numerics.quadratic_extrap(ys, [0.01, 0.008, 0.006]), h["extrap_q"])
+    assert np.array_equal(numerics.linear_extrap(ys[:2], [0.01, 0.008]), h["extrap_l"])
+    model = spectrum.Spectrum(h["ll_model"])
+    data = spectrum.Spectrum(h["ll_data"])
+    assert inference.ll(model, data) == pytest.approx(float(h["ll"]), rel=1e-14)
+    assert inference.ll_multinom(model, data) == pytest.approx(float(h["ll_multinom"]), rel=1e-14)
+
+
+def test_extrap_fail_mag():
+    """Entries extrapolated more than fail_mag decades away fall back to the
+    smallest-x input (dadi/Numerics.py:449-464)."""
+    a = np.array([1.0, 1e-5])
+    b = np.array([1.0, 1e-20])
+    c = np.array([1.0, 1e-30])
+    ex = numerics.extrapolate([a, b, c], [0.3, 0.2, 0.1])
+    assert ex[1] == c[1]
+    assert ex[0] == pytest.approx(1.0)
+
+
+@pytest.mark.parametrize("case", cases.TWO_POPS + cases.THREE_POPS[:3],
+                         ids=lambda c: c["name"])
+def test_table_matches_oracle_schedule(case):
+    """The host-evaluated schedule (step count, dt sequence, final time) is the
+    reference loop's: rebuilding the oracle's integration from the table's dts
+    gives the same step count."""
+    P = 2 if case["name"].startswith("2d") else 3
+    xx = cases.grid(case["grid"], case["pts"])
+    args = [cases.resolve(v) for v in case["args"]]
+    kw = {k: cases.resolve(v) for k, v in case.get("kw", {}).items()}
+    T = args[0]
+    initial_t = kw.get("initial_t", args[12 if P == 2 else 18] if len(args) > (12 if P == 2 else 18) else 0)
+    f = integration.ensure_1arg_func
+    if P == 2:
+        T, nu1, nu2, m12, m21, g1, g2, h1, h2, th = args[:10]
+        table, hist = integration.build_table(2, xx, T, initial_t, [f(nu1), f(nu2)],
+                                              [[None, f(m12)], [f(m21), None]],
+                                              [f(g1), f(g2)], [f(h1), f(h2)], f(th))
+    else:
+        (T, n1, n2, n3, m12, m13, m21, m23, m31, m32, g1, g2, g3, h1, h2, h3, th) = args[:17]
+        mig = [[None, f(m12), f(m13)], [f(m21), None, f(m23)], [f(m31), f(m32), None]]
+        table, hist = integration.build_table(3, xx, T, initial_t, [f(n1), f(n2), f(n3)], mig,
+                                              [f(g1), f(g2), f(g3)], [f(h1), f(h2), f(h3)],
+                                              f(th))
+    t = initial_t
+    for row in table:
+        t = t + row[0]
+    assert t == pytest.approx(T, rel=1e-12)
+    assert len(hist) == len(table) + 1
+    assert table.shape[1] == integration.row_stride(P)
+
+
+def test_table_validation():
+    xx = numerics.default_grid(10)
+    f = integration.ensure_1arg_func
+    with pytest.raises(ValueError):
+        integration.build_table(2, xx, 0.1, 0, [f(1.0), f(lambda t: 1.0 if t < 0.05 else -1.0)],
+                                [[None, f(0)], [f(0), None]], [f(0), f(0)], [f(.5), f(.5)], f(1))
+    with pytest.raises(ValueError):
+        integration.build_table(2, xx, 0.1, 0, [f(1.0), f(1.0)],
+                                [[None, f(-1.0)], [f(0), None]], [f(0), f(0)], [f(.5), f(.5)],
+                                f(1))
+    with pytest.raises(ValueError):
+        integration.two_pops(np.zeros((10, 10)), xx, 0.1, 1, 1, m12=1, frozen1=True)
+    with pytest.raises(ValueError):
+        integration.two_pops(np.zeros((10, 10)), xx, 0.1, initial_t=0.2)
+
+
+@pytest.mark.parametrize("P,axis", [(2, 0), (2, 1), (3, 0), (3, 2)])
+def test_const_coefficients_match_oracle(P, axis):
+    xx = cases.grid("lin", 9)
+    ms = [0.3, 1.7][:P - 1]
+    a1 = integration.const_coefficients(xx, P, axis, 0.7, ms, -1.2, 0.3)
+    a2 = oint.precalc_coefficients(xx, P, axis, 0.7, ms, -1.2, 0.3)
+    for u, v in zip(a1, a2):
+        assert np.array_equal(u, v)

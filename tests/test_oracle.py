@@ -1,0 +1,139 @@
+"""The oracle (CPU restatement) against the reference's own outputs: golden
+vectors produced by running dadi 2.4.3 (tests/golden/make_golden.py), and the
+reference C sweeps compiled from their sources when that build exists."""
+import numpy as np
+import pytest
+
+import cases
+from oracle import clib, integration as oint, numerics as onum
+from util import ALL_CASES, case_inputs
+
+
+@pytest.mark.parametrize("group,case", ALL_CASES, ids=[c["name"] for _, c in ALL_CASES])
+def test_integration_bitwise(golden, group, case):
+    fn = {"one": oint.one_pop, "two": oint.two_pops, "three": oint.three_pops,
+          "four": oint.four_pops}[group]
+    xx, phi0, args, kw = case_inputs(group, case)
+    out = fn(phi0.copy(), xx, *args, **kw)
+    assert np.array_equal(out, golden["integrate"]["int_" + case["name"]])
+
+
+@pytest.mark.parametrize("name,nd,axis,pts,gk", cases.SWEEPS)
+@pytest.mark.parametrize("delj", [0, 1])
+def test_sweep_bitwise(golden, name, nd, axis, pts, gk, delj):
+    g = golden["sweeps"]
+    p = cases.SWEEP_PARAMS
+    phi = g["sweep_%s_phi0" % name].copy()
+    clib.sweep(phi, cases.grid(gk, pts), axis, p["nu"], p["mig"][:nd], p["gamma"], p["h"],
+               p["dt"], beta=p["beta"], use_delj_trick=delj)
+    assert np.array_equal(phi, g["sweep_%s_delj%d" % (name, delj)])
+
+
+@pytest.mark.parametrize("nd,axis", [(2, 0), (2, 1), (3, 0), (3, 1), (3, 2)])
+def test_precalc_sweep_bitwise(golden, nd, axis):
+    g = golden["sweeps"]
+    k = "precalc_%dD%d" % (nd, axis)
+    phi = g[k + "_phi0"].copy()
+    a, b, c = g[k + "_abc"]
+    clib.sweep_precalc(phi, axis, a, b, c, 0.01)
+    assert np.array_equal(phi, g[k])
+
+
+def test_tridiag(golden):
+    h = golden["host"]
+    a, b, c, r = h["tridiag_abcr"]
+    assert np.array_equal(clib.tridiag(a, b, c, r), h["tridiag_u"])
+
+
+def test_host_pieces(golden):
+    h = golden["host"]
+    for pts in (5, 10, 40, 80, 100, 120):
+        assert np.array_equal(onum.default_grid(pts), h["grid_%d" % pts])
+    xx = onum.default_grid(30)
+    assert np.array_equal(onum.phi_1D(xx), h["phi1d_snm"])
+    assert np.array_equal(onum.phi_1D(xx, nu=1.5, theta0=2.0, gamma=2.0), h["phi1d_g2"])
+    assert np.array_equal(onum.phi_1D(xx, gamma=-5.0, beta=1.4), h["phi1d_gm5"])
+    assert np.array_equal(onum.phi_1D_to_2D(xx, onum.phi_1D(xx)), h["phi2d_split"])
+    xs = onum.default_grid(12)
+    p3 = onum.phi_2D_to_3D_admix(onum.phi_1D_to_2D(xs, onum.phi_1D(xs)), 0, xs, xs, xs)
+    assert np.array_equal(p3, h["phi3d_split2"])
+    assert np.array_equal(onum.phi_3D_to_4D(p3, 0.3, 0.2, xs, xs, xs, xs), h["phi4d_from3d"])
+    for nd, pts in [(1, 25), (2, 21), (3, 11), (4, 7)]:
+        fs = onum.from_phi(h["fromphi_%dd_phi" % nd], tuple(h["fromphi_%dd_ns" % nd]),
+                           onum.default_grid(pts))
+        assert np.array_equal(fs, h["fromphi_%dd" % nd])
+    ys = list(h["extrap_in"])
+    assert np.array_equal(onum.quadratic_extrap(ys, [0.01, 0.008, 0.006]), h["extrap_q"])
+    assert np.array_equal(onum.linear_extrap(ys[:2], [0.01, 0.008]), h["extrap_l"])
+    m, d = h["ll_model"], h["ll_data"]
+    mask = onum.corner_mask(m.shape)
+    assert onum.ll(m, d, mask) == pytest.approx(float(h["ll"]), rel=1e-14)
+    assert onum.ll_multinom(m, d, mask) == pytest.approx(float(h["ll_multinom"]), rel=1e-14)
+
+
+def test_models_small(golden):
+    """Full model pipelines (grid, initial condition, integration, from_phi,
+    extrapolation) against dadi's own make_extrap_func output."""
+    g = golden["models"]
+    sm = cases.SPLIT_MIG
+    fs = onum.extrap_model(onum.split_mig, sm["params"], sm["ns"], sm["pts_l"])
+    assert np.array_equal(fs, g["splitmig_fs"])
+    d0 = cases.im_draws()[0]
+    assert np.array_equal(cases.im_draws()[:64], g["im_draws_head"])
+    fs = onum.extrap_model(onum.IM, d0, (10, 10), [20, 25, 30])
+    assert np.array_equal(fs, g["im_small_fs"])
+
+
+def test_against_compiled_reference():
+    """The C restatement equals the reference C sweeps compiled from their own
+    sources (only where the reference tree was available to build them)."""
+    import ctypes
+    ref = clib.ref_lib()
+    if ref is None:
+        pytest.skip("reference C not built here (no reference tree)")
+    dp = ctypes.POINTER(ctypes.c_double)
+    rng = np.random.default_rng(3)
+    L = 17
+    xx = onum.default_grid(L)
+    for delj in (0, 1):
+        phi = rng.uniform(size=(L, L))
+        a = phi.copy()
+        ref.implicit_2Dx.argtypes = [dp, dp, dp] + [ctypes.c_double] * 5 + [ctypes.c_int] * 5
+        ref.implicit_2Dx(a.ctypes.data_as(dp), xx.ctypes.data_as(dp), xx.ctypes.data_as(dp),
+                         0.7, 1.3, -2.0, 0.3, 0.01, L, L, delj, 0, L)
+        b = phi.copy()
+        clib.sweep(b, xx, 0, 0.7, [0, 1.3], -2.0, 0.3, 0.01, use_delj_trick=delj)
+        assert np.array_equal(a, b)
+        ref.implicit_3Dz.argtypes = [dp, dp, dp, dp] + [ctypes.c_double] * 6 + [ctypes.c_int] * 6
+        phi3 = rng.uniform(size=(9, 9, 9))
+        x9 = onum.default_grid(9)
+        a = phi3.copy()
+        ref.implicit_3Dz(a.ctypes.data_as(dp), x9.ctypes.data_as(dp), x9.ctypes.data_as(dp),
+                         x9.ctypes.data_as(dp), 1.1, 0.4, 2.2, 1.5, 0.8, 0.02, 9, 9, 9, delj, 0, 9)
+        b = phi3.copy()
+        clib.sweep(b, x9, 2, 1.1, [0.4, 2.2, 0], 1.5, 0.8, 0.02, use_delj_trick=delj)
+        assert np.array_equal(a, b)
+
+
+def test_reference_noise_floor_tiny_entries(golden):
+    """Forming the right-hand side as (1/dt)*phi instead of phi/dt -- the form
+    the reference's own constant-parameter sweeps use -- moves the tiny
+    entries of a seed-0 IM spectrum by more than 1e-9 relative, while entries
+    above 1e-12 of the maximum move by far less.  This is why spectrum parity
+    is relative above that level and absolute below it (util.fs_parity)."""
+    from util import fs_parity
+    d = cases.im_draws()[5]
+    ref = golden["models"]["im_fs_5"]
+    clib.rhs_variant = True
+    try:
+        fs = onum.extrap_model(onum.IM, d, (40, 40), [80, 90, 100])
+    finally:
+        clib.rhs_variant = False
+    rel_big, abs_small, n_small = fs_parity(fs, ref)
+    m = onum.corner_mask(ref.shape)
+    with np.errstate(all="ignore"):
+        rel_all = np.max((np.abs(fs - ref) / np.abs(ref))[~m])
+    assert n_small > 0
+    assert rel_all > 1e-9          # the reference's own floor on tiny entries
+    assert rel_big < 1e-10          # entries that matter move far less
+    assert abs_small < 1e-21
