@@ -24,8 +24,8 @@ ST_BADPARAM, ST_STEPCAP, ST_NONFINITE, ST_ZERODT = 1, 2, 4, 8
 #: Every entry point the header declares (checked by the test suite).
 EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
            "dgb_tridiag_batch", "dgb_implicit_sweep", "dgb_implicit_precalc_sweep",
-           "dgb_integrate_table", "dgb_integrate_precalc", "dgb_batch2d_integrate",
-           "dgb_batch2d_count_steps"]
+           "dgb_integrate_table", "dgb_integrate_precalc", "dgb_sched2d",
+           "dgb_batch2d_integrate", "dgb_batch2d_count_steps"]
 
 
 class PForm(ctypes.Structure):
@@ -70,8 +70,10 @@ def _declare(L):
         "dgb_implicit_precalc_sweep": (i, [_vp, i, i, i, _vp, _vp, _vp, d, _vp, sz, _vp]),
         "dgb_integrate_table": (i, [_vp, i, i, _vp, _vp, i, i, i, i, _vp, sz, _vp]),
         "dgb_integrate_precalc": (i, [_vp, i, i, _vp, _vp, _vp, i, d, i, i, _vp, sz, _vp]),
-        "dgb_batch2d_integrate": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp,
-                                      _vp, _vp, lg, ctypes.POINTER(Settings), _vp, sz, _vp]),
+        "dgb_sched2d": (i, [_vp, i, i, _vp, ctypes.POINTER(Settings), lg, i, _vp, _vp, _vp, _vp,
+                            _vp]),
+        "dgb_batch2d_integrate": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp,
+                                      _vp, _vp, _vp, ctypes.POINTER(Settings), _vp, sz, _vp]),
         "dgb_batch2d_count_steps": (i, [ctypes.POINTER(Inst2D), i, ctypes.POINTER(Settings), lg,
                                         ctypes.POINTER(ctypes.c_long)]),
     }

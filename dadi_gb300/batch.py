@@ -106,39 +106,75 @@ class Batch2D:
         phi0 = [phimanip.phi_1D_to_2D(xx, phimanip.phi_1D(xx)) for xx in self.xxs]
         self.d_xx = _lib.to_device(torch, np.concatenate(self.xxs))
         self.d_phi0 = _lib.to_device(torch, np.concatenate([p.ravel() for p in phi0]))
+        self.d_dx0 = _lib.to_device(torch, np.array([xx[1] - xx[0] for xx in self.xxs]))
         self.Ls = (ctypes.c_int * len(self.pts_l))(*self.pts_l)
         self.x_l = [xx[1] for xx in self.xxs]
         self.mask = np.zeros((ns[0] + 1, ns[1] + 1), dtype=bool)
         self.mask.flat[0] = self.mask.flat[-1] = True
 
-    def integrate(self, rec, order=None):
+    def schedule(self, d_rec, n):
+        """Device schedules of n dgb_inst2d records already on the device:
+        (table, row_off, row_cnt, status)."""
+        torch = self.torch
+        lib = _lib.lib()
+        st = settings_from_globals(self.gam_placement)
+        ng = len(self.pts_l)
+        nsched = n * ng if st.use_old_timestep else n
+        sh = _lib.stream_handle(torch)
+        cnt = torch.zeros(nsched, dtype=torch.int32, device="cuda")
+        _lib.check(lib.dgb_sched2d(_lib.dptr(d_rec), n, ng, _lib.dptr(self.d_dx0), ctypes.byref(st),
+                                   self.max_steps, 0, _lib.dptr(cnt), None, None, None, sh),
+                   "dgb_sched2d(count)")
+        ends = torch.cumsum(cnt.to(torch.int64), 0)
+        total = int(ends[-1].item())
+        off = (ends - cnt.to(torch.int64)).contiguous()
+        table = torch.empty(max(total, 1) * 11, dtype=torch.float64, device="cuda")
+        status = torch.zeros(n, dtype=torch.int32, device="cuda")
+        _lib.check(lib.dgb_sched2d(_lib.dptr(d_rec), n, ng, _lib.dptr(self.d_dx0), ctypes.byref(st),
+                                   self.max_steps, 1, _lib.dptr(cnt), _lib.dptr(off),
+                                   _lib.dptr(table), _lib.dptr(status), sh),
+                   "dgb_sched2d(fill)")
+        return table, off, cnt, status
+
+    def integrate(self, rec, order=None, timer=None):
         """Run the integrations of dgb_inst2d records `rec` (host structured
-        array).  Returns (list of per-grid phi tensors (n, L, L), status)."""
+        array).  Returns (list of per-grid phi tensors (n, L, L), status).
+        timer: optional pair of CUDA events recorded around the integration
+        kernel alone."""
         torch = self.torch
         n = len(rec)
         ng = len(self.pts_l)
         st = settings_from_globals(self.gam_placement)
+        rec = np.ascontiguousarray(rec)
+        d_rec = torch.from_numpy(rec.view(np.uint8)).to("cuda")
+        table, off, cnt, status = self.schedule(d_rec, n)
+        Lsq = torch.tensor([L * L for L in self.pts_l], dtype=torch.int64, device="cuda")
         if order is None:
-            steps = count_steps(rec, st, self.max_steps)
-            cost = (steps[:, None] * np.array(self.pts_l)[None, :] ** 2).ravel()
-            order = np.argsort(-cost, kind="stable").astype(np.int32)
-        d_rec = torch.from_numpy(np.ascontiguousarray(rec).view(np.uint8)).to("cuda")
-        d_order = torch.from_numpy(np.ascontiguousarray(order, dtype=np.int32)).to("cuda")
+            steps = cnt.to(torch.int64).view(n, -1)
+            cost = (steps * Lsq[None, :]).reshape(-1)
+            d_order = torch.argsort(-cost, stable=True).to(torch.int32)
+        else:
+            d_order = torch.from_numpy(np.ascontiguousarray(order, dtype=np.int32)).to("cuda")
+        masks = (rec["frozen"].astype(np.int32) & 0xff) | ((rec["nomut"].astype(np.int32) & 0xff) << 8)
+        d_masks = torch.from_numpy(np.ascontiguousarray(masks)).to("cuda")
         total = sum(n * L * L for L in self.pts_l)
         d_out = torch.empty(total, dtype=torch.float64, device="cuda")
-        d_status = torch.zeros(n, dtype=torch.int32, device="cuda")
         nws = _lib.lib().dgb_workspace_bytes(1, 2, max(self.pts_l), n * ng)
         ws, nws = _lib.workspace(torch, nws)
+        if timer is not None:
+            timer[0].record()
         rc = _lib.lib().dgb_batch2d_integrate(
-            _lib.dptr(d_rec), n, self.Ls, ng, _lib.dptr(self.d_xx), _lib.dptr(self.d_phi0),
-            _lib.dptr(d_out), _lib.dptr(d_order), _lib.dptr(d_status), self.max_steps,
+            _lib.dptr(d_masks), n, self.Ls, ng, _lib.dptr(self.d_xx), _lib.dptr(self.d_phi0),
+            _lib.dptr(d_out), _lib.dptr(table), _lib.dptr(off), _lib.dptr(cnt), _lib.dptr(d_order),
             ctypes.byref(st), _lib.dptr(ws), nws, _lib.stream_handle(torch))
+        if timer is not None:
+            timer[1].record()
         _lib.check(rc, "dgb_batch2d_integrate")
-        phis, off = [], 0
+        phis, o = [], 0
         for L in self.pts_l:
-            phis.append(d_out[off:off + n * L * L].view(n, L, L))
-            off += n * L * L
-        return phis, d_status
+            phis.append(d_out[o:o + n * L * L].view(n, L, L))
+            o += n * L * L
+        return phis, status
 
     def spectra(self, phis):
         """Per-grid raw spectra (n, n1+1, n2+1) on the device."""

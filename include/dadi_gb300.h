@@ -135,33 +135,44 @@ int dgb_integrate_precalc(double *phi, int ndim, int L, const double *xx,
                           double theta0, int frozen_mask, int nomut_mask,
                           void *ws, size_t ws_bytes, void *stream);
 
-/* Batched 2-population engine: ninst integrations x ngrids grids, each
- * (instance, grid) pair one work item of a persistent launch that evaluates
- * the parametric schedule on the device and keeps phi in shared memory.
- *   insts    device, ninst dgb_inst2d
+/* Batched 2-population engine, step 1: the per-step parameter rows of many
+ * parametric two_pops integrations (the loop of dadi/Integration.py:346-386:
+ * dt from the current parameters by _compute_dt, :147-176, parameters at the
+ * next time, the reference's validation), one device thread per schedule.
+ * Run it twice: fill == 0 writes row_cnt[s]; after the caller's exclusive
+ * scan of row_cnt into row_off, fill == 1 writes the rows (DGB_ROW_STRIDE(2)
+ * doubles each) at table + row_off[s]*11 and ORs DGB_ST_* bits into
+ * status[instance] (caller zeroes it).  There is one schedule per instance,
+ * or per (instance, grid) when settings->use_old_timestep makes dt depend on
+ * the grid; dx0s (device) holds each grid's first spacing.
+ *   insts  device, ninst dgb_inst2d */
+int dgb_sched2d(const dgb_inst2d *insts, int ninst, int ngrids, const double *dx0s,
+                const dgb_settings *settings, long max_steps, int fill, int *row_cnt,
+                const long *row_off, double *table, int *status, void *stream);
+
+/* Batched 2-population engine, step 2: ninst integrations x ngrids grids as
+ * one persistent launch; each (instance, grid) pair is a work item that keeps
+ * phi in shared memory for its whole loop and reads its schedule's rows.
+ *   masks    device, ninst ints: frozen_mask | nomut_mask << 8 (null: none)
  *   Ls       host, ngrids grid sizes
  *   xx_all   device, concatenated grids (sum of Ls doubles)
  *   phi0_all device, concatenated initial densities (sum of L^2), shared by
  *            every instance
  *   phi_out  device, for grid g the block of ninst*L_g^2 doubles starting
  *            after the blocks of grids < g (instance-major inside a block)
- *   order    device, nwork = ninst*ngrids work ids (inst*ngrids + g), in the
- *            order they should be started (longest first balances best)
- *   status   device, ninst ints, OR-ed DGB_ST_* bits (caller zeroes them)
- *   max_steps per-integration step cap (DGB_ST_STEPCAP when hit)
- * This replaces many calls of Integration.two_pops with one launch; its
- * parallel form is the reference's multi-process Cache2D generation
- * (dadi/DFE/Cache2D_mod.py:117-167). */
-int dgb_batch2d_integrate(const dgb_inst2d *insts, int ninst, const int *Ls,
-                          int ngrids, const double *xx_all,
-                          const double *phi0_all, double *phi_out,
-                          const int *order, int *status, long max_steps,
-                          const dgb_settings *settings,
+ *   table, row_off, row_cnt  the rows of step 1
+ *   order    device, ninst*ngrids work ids (inst*ngrids + g) in start order
+ *            (longest first balances best)
+ * Many calls of Integration.two_pops become one launch; the reference runs
+ * such batches as host processes (dadi/DFE/Cache2D_mod.py:117-167). */
+int dgb_batch2d_integrate(const int *masks, int ninst, const int *Ls, int ngrids,
+                          const double *xx_all, const double *phi0_all, double *phi_out,
+                          const double *table, const long *row_off, const int *row_cnt,
+                          const int *order, const dgb_settings *settings,
                           void *ws, size_t ws_bytes, void *stream);
 
-/* Host helper: number of time steps each batched instance takes (the
- * schedule of dadi/Integration.py:355-386 evaluated in C on the host), used
- * to order work longest-first.  insts is a HOST array here. */
+/* Host helper: the number of steps of each schedule, evaluated in C on the
+ * host (insts is a HOST array here); the same walk as dgb_sched2d. */
 int dgb_batch2d_count_steps(const dgb_inst2d *insts, int ninst,
                             const dgb_settings *settings, long max_steps,
                             long *steps_out);
