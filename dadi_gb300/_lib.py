@@ -25,7 +25,8 @@ ST_BADPARAM, ST_STEPCAP, ST_NONFINITE, ST_ZERODT = 1, 2, 4, 8
 EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
            "dgb_tridiag_batch", "dgb_implicit_sweep", "dgb_implicit_precalc_sweep",
            "dgb_integrate_table", "dgb_integrate_precalc", "dgb_sched2d",
-           "dgb_batch2d_integrate", "dgb_batch2d_count_steps"]
+           "dgb_batch2d_integrate", "dgb_batch2d_count_steps", "dgb_probe_fp64_fma",
+           "dgb_probe_rcp"]
 
 
 class PForm(ctypes.Structure):
@@ -76,6 +77,8 @@ def _declare(L):
                                       _vp, _vp, _vp, ctypes.POINTER(Settings), _vp, sz, _vp]),
         "dgb_batch2d_count_steps": (i, [ctypes.POINTER(Inst2D), i, ctypes.POINTER(Settings), lg,
                                         ctypes.POINTER(ctypes.c_long)]),
+        "dgb_probe_fp64_fma": (i, [_vp, i, i, i, i, _vp]),
+        "dgb_probe_rcp": (i, [_vp, _vp, i, _vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -144,3 +147,27 @@ def settings_struct(timescale_factor=1e-3, old_timescale_factor=0.1, use_old_tim
                     use_delj_trick=False, gam_placement=0):
     return Settings(float(timescale_factor), float(old_timescale_factor),
                     int(bool(use_old_timestep)), int(bool(use_delj_trick)), int(gam_placement), 0)
+
+
+def fp64_fma_peak_tflops(torch, iters=4096, active_lanes=32):
+    """Measured FP64 FMA rate of this GPU in TFLOP/s (2 flops per FMA):
+    4 warps per SM on every SM, 8 independent chains per thread, counting
+    only the FMAs of the active lanes."""
+    nsm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    blocks, threads = nsm, 128
+    out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
+    sh = stream_handle(torch)
+    check(lib().dgb_probe_fp64_fma(dptr(out), blocks, threads, 16, active_lanes, sh),
+          "dgb_probe_fp64_fma")
+    best = 0.0
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        check(lib().dgb_probe_fp64_fma(dptr(out), blocks, threads, iters, active_lanes, sh),
+              "dgb_probe_fp64_fma")
+        e1.record()
+        torch.cuda.synchronize()
+        fmas = blocks * (threads // 32) * active_lanes * iters * 8
+        best = max(best, 2.0 * fmas / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best

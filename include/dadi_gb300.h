@@ -177,6 +177,18 @@ int dgb_batch2d_count_steps(const dgb_inst2d *insts, int ninst,
                             const dgb_settings *settings, long max_steps,
                             long *steps_out);
 
+/* Measurement helpers with no counterpart in the reference.
+ * dgb_probe_fp64_fma: blocks x threads threads, of which the first
+ * active_lanes lanes of every warp run 8 independent chains of `iters` FP64
+ * FMAs and store one double each to out[blocks*threads] (device).  Timing it
+ * gives the FP64 pipe's FMA rate (the roofline of the sweeps) and shows
+ * whether idle lanes cost issue slots.
+ * dgb_probe_rcp: out[i] = the kernels' refined reciprocal of x[i] (device),
+ * so tests can check it against correctly rounded division. */
+int dgb_probe_fp64_fma(double *out, int blocks, int threads, int iters, int active_lanes,
+                       void *stream);
+int dgb_probe_rcp(const double *x, double *out, int n, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
