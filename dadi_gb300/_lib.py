@@ -17,6 +17,8 @@ DGB_ERR_ARG = -1
 DGB_ERR_CUDA = -2
 DGB_ERR_UNSUPPORTED = -3
 DGB_ERR_WORKSPACE = -4
+DGB_ERR_TOO_LARGE = -5
+NOALLOC_MAX_L = 128
 
 PF_CONST, PF_EXPGROW, PF_EXPLOG, PF_LINEAR = 0, 1, 2, 3
 ST_BADPARAM, ST_STEPCAP, ST_NONFINITE, ST_ZERODT = 1, 2, 4, 8
@@ -26,7 +28,7 @@ EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
            "dgb_tridiag_batch", "dgb_implicit_sweep", "dgb_implicit_precalc_sweep",
            "dgb_integrate_table", "dgb_integrate_precalc", "dgb_sched2d",
            "dgb_batch2d_integrate", "dgb_batch2d_count_steps", "dgb_probe_fp64_fma",
-           "dgb_probe_rcp"]
+           "dgb_probe_rcp", "dgb_integrate2d_noalloc"]
 
 
 class PForm(ctypes.Structure):
@@ -79,6 +81,7 @@ def _declare(L):
                                         ctypes.POINTER(ctypes.c_long)]),
         "dgb_probe_fp64_fma": (i, [_vp, i, i, i, i, _vp]),
         "dgb_probe_rcp": (i, [_vp, _vp, i, _vp]),
+        "dgb_integrate2d_noalloc": (i, [_vp, i, _vp, _vp, i, i, i, i, _vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -21,6 +21,7 @@
 // Reference: the time loop of Integration.two_pops (dadi/Integration.py:
 // 340-386) with implicit_2Dx / implicit_2Dy (dadi/integration2D.c:19-160).
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "dgb_common.cuh"
@@ -526,6 +527,34 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     return k2_launch(A, nblocks, smem, st);
 }
 
+// ------------------------------------------- allocation-free entry point
+
+// Thomas scratch of dgb_integrate2d_noalloc: one L x L array for L up to
+// DGB_NOALLOC_MAX_L (128 KB), resident on every GPU that loads the library.
+static __device__ __align__(256) double g_noalloc_gam[DGB_NOALLOC_MAX_L * DGB_NOALLOC_MAX_L];
+
+// Device address of g_noalloc_gam per device, looked up once per device with
+// that device current (host code must not use the symbol itself).
+constexpr int NOALLOC_MAXDEV = 64;
+static std::once_flag g_noalloc_once[NOALLOC_MAXDEV];
+static double *g_noalloc_ptr[NOALLOC_MAXDEV];
+static int g_noalloc_rc[NOALLOC_MAXDEV];
+
+static int noalloc_scratch(double **ptr)
+{
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAXDEV)
+        return DGB_ERR_CUDA;
+    std::call_once(g_noalloc_once[dev], [dev]() {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_gam);
+        g_noalloc_ptr[dev] = (double *)p;
+        g_noalloc_rc[dev] = (e == cudaSuccess && p) ? DGB_OK : DGB_ERR_CUDA;
+    });
+    *ptr = g_noalloc_ptr[dev];
+    return g_noalloc_rc[dev];
+}
+
 } // namespace dgb
 
 // ------------------------------------------------------------------ C ABI
@@ -570,4 +599,38 @@ extern "C" int dgb_batch2d_count_steps(const dgb_inst2d *insts, int ninst,
     for (int n = 0; n < ninst; n++)
         steps_out[n] = dgb::sched2d_walk(insts[n], *settings, 1e-3, max_steps, nullptr, nullptr);
     return DGB_OK;
+}
+
+extern "C" int dgb_integrate2d_noalloc(double *phi, int L, const double *xx, const double *table,
+                                       int nsteps, int frozen_mask, int nomut_mask,
+                                       int use_delj_trick, void *stream)
+{
+    if (!phi || !xx || !table || nsteps < 0 || L < 3)
+        return DGB_ERR_ARG;
+    if (L > DGB_NOALLOC_MAX_L)
+        return DGB_ERR_TOO_LARGE;
+    if (nsteps == 0)
+        return DGB_OK;
+    double *scratch = nullptr;
+    int rc = dgb::noalloc_scratch(&scratch);
+    if (rc)
+        return rc;
+    size_t bytes = 0;
+    if (!dgb::k2_smem_fits(L, false, use_delj_trick != 0, &bytes))
+        return DGB_ERR_UNSUPPORTED;
+    dgb::K2Args A = {};
+    A.ngrids = 1;
+    A.L[0] = L;
+    A.xx_all = xx;
+    A.phi_out = phi;
+    A.table = table;
+    A.fixed_cnt = nsteps;
+    A.frozen_mask = frozen_mask;
+    A.nomut_mask = nomut_mask;
+    A.nwork = 1;
+    A.Lmax = L;
+    A.use_delj = use_delj_trick;
+    A.gam_smem = 0;
+    A.gam_glob = scratch;
+    return dgb::k2_launch(A, 1, bytes, (cudaStream_t)stream);
 }

@@ -431,6 +431,9 @@ extern "C" const char *dgb_status_string(int status)
         return "unsupported size or mode";
     case DGB_ERR_WORKSPACE:
         return "workspace missing or too small";
+    case DGB_ERR_TOO_LARGE:
+        return "grid larger than the allocation-free entry point's static scratch "
+               "(L > DGB_NOALLOC_MAX_L)";
     default:
         return "unknown status";
     }

@@ -32,6 +32,7 @@ extern "C" {
 #define DGB_ERR_CUDA (-2)        /* a CUDA call failed */
 #define DGB_ERR_UNSUPPORTED (-3) /* size or mode outside what the kernels handle */
 #define DGB_ERR_WORKSPACE (-4)   /* workspace missing or too small */
+#define DGB_ERR_TOO_LARGE (-5)   /* grid larger than dgb_integrate2d_noalloc's static scratch */
 
 #define DGB_MAX_DIM 4
 #define DGB_ROW_STRIDE(P) (3 + 3 * (P) + (P) * ((P)-1))
@@ -176,6 +177,26 @@ int dgb_batch2d_integrate(const int *masks, int ninst, const int *Ls, int ngrids
 int dgb_batch2d_count_steps(const dgb_inst2d *insts, int ninst,
                             const dgb_settings *settings, long max_steps,
                             long *steps_out);
+
+/* Allocation-free 2-D integration; it has no counterpart in the reference.
+ * The same computation as dgb_integrate_table for ndim == 2 (one integration
+ * through a parameter table, phi updated in place), for callers that cannot
+ * allocate device memory or pass a workspace -- e.g. code that runs where
+ * cudaMalloc is not allowed or a caching allocator must not be entered, or
+ * a host that embeds the library without a device allocator of its own.
+ * Its Thomas scratch is a file-scope device array of DGB_NOALLOC_MAX_L^2
+ * doubles (128 KB) that every GPU which loads the library holds until the
+ * process exits; grids with L > DGB_NOALLOC_MAX_L return DGB_ERR_TOO_LARGE.
+ * The first call on each device looks up the array's address
+ * (cudaGetSymbolAddress) with that device current, so make that first call
+ * before any stream capture.  Every call shares the one array, which keeps
+ * the previous call's contents (nothing in it needs to start at zero): calls
+ * that overlap on the GPU -- on different streams or from different host
+ * threads -- race on it, so serialise them.  The call allocates nothing. */
+#define DGB_NOALLOC_MAX_L 128
+int dgb_integrate2d_noalloc(double *phi, int L, const double *xx, const double *table,
+                            int nsteps, int frozen_mask, int nomut_mask, int use_delj_trick,
+                            void *stream);
 
 /* Measurement helpers with no counterpart in the reference.
  * dgb_probe_fp64_fma: blocks x threads threads, of which the first
