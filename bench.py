@@ -69,8 +69,9 @@ class ClockSampler:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index=0):
+    def __init__(self, index=0, period_ms=500):
         self.index = index
+        self.period_ms = max(int(period_ms), 100)
         self.proc = None
         self.lines = []
 
@@ -78,7 +79,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -251,13 +252,20 @@ def run_ours(a, world, rank, local):
         return fs, ll, status
 
     # warm-up
+    warm_ms = []
     for _ in range(a.warmup):
+        w0 = torch.cuda.Event(enable_timing=True)
+        w1 = torch.cuda.Event(enable_timing=True)
+        w0.record()
         step_device()
-    torch.cuda.synchronize()
+        w1.record()
+        torch.cuda.synchronize()
+        warm_ms.append(w0.elapsed_time(w1))
 
     # timed region: per-kernel events around the integration for the roofline
-    clocks = ClockSampler(local)
-    clocks.start()
+    clocks = ClockSampler(local, a.clock_ms)
+    if a.clock_ms > 0:
+        clocks.start()
     kern_ms = []
     barrier(world)
     torch.cuda.synchronize()
@@ -372,6 +380,7 @@ def run_ours(a, world, rank, local):
                          "algorithmic_tflops counts %d reference flops per point-sweep"
                          % (FP64_INSTR_PER_PS, FLOPS_PER_PS)},
         "kernel_ms_per_step": kmean * 1e3,
+        "warmup_ms": warm_ms,
         "clocks": clk,
         "gpu_launches": 3 * a.steps,  # per step: 2 schedule passes + 1 integration
         "failed_instances": bad,
@@ -416,6 +425,8 @@ def main():
     ap.add_argument("--gam", type=int, default=0, help="0 auto, 1 shared, 2 workspace")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--clock-ms", type=int, default=500,
+                    help="nvidia-smi sampling period during the timed region (0: off)")
     ap.add_argument("--profile-items", type=int, default=0,
                     help="run only a small batch (this many seed-0 instances with 200-800 "
                          "steps, twice) for profiler captures, then exit")

@@ -221,6 +221,35 @@ __device__ __forceinline__ void build_axis_entry(int i, int L, const GridVecs &g
 
 // ------------------------------------------------------------ line solvers
 
+// Back substitution u_i = u'_i - gam_{i+1} u_{i+1} for i = L-2..0, where
+// u holds u_{L-1}.  The gam and u' of 16 rows are loaded before their
+// dependent FMA chain runs, so scratch that lives in global memory (L2) does
+// not stall the chain on every row.
+template <typename TP, typename TG>
+__device__ __forceinline__ void back_substitute(TP *__restrict__ ph, int sp,
+                                                TG *__restrict__ gm, int gs, int L, double u)
+{
+    constexpr int B = 16;
+    int i = L - 2;
+    for (; i >= B - 1; i -= B) {
+        double gv[B], pv[B];
+#pragma unroll
+        for (int k = 0; k < B; k++) {
+            gv[k] = gm[(i - k + 1) * gs];
+            pv[k] = ph[(i - k) * sp];
+        }
+#pragma unroll
+        for (int k = 0; k < B; k++) {
+            u = fma(-gv[k], u, pv[k]);
+            ph[(i - k) * sp] = u;
+        }
+    }
+    for (; i >= 0; i--) {
+        u = fma(-(double)gm[(i + 1) * gs], u, ph[i * sp]);
+        ph[i * sp] = u;
+    }
+}
+
 // Thomas solve of one line, delta_j = 0.5.  Element p of the line is
 // ph[p*sp]; gam scratch element p is gm[p*gs].  W is the line's migration
 // weight, bs/be the corner boundary terms for this line (0 if none).
@@ -254,11 +283,7 @@ __device__ __forceinline__ void solve_line(TP *__restrict__ ph, int sp, TG *__re
         u = fma(-a, u, ph[i * sp]) * inv;
         ph[i * sp] = u;
     }
-#pragma unroll 4
-    for (i = L - 2; i >= 0; i--) {
-        u = fma(-(double)gm[(i + 1) * gs], u, ph[i * sp]);
-        ph[i * sp] = u;
-    }
+    back_substitute(ph, sp, gm, gs, L, u);
 }
 
 // Chang-Cooper delta_j (dadi/integration_shared.c:52-70) for one interval.
@@ -323,10 +348,7 @@ __device__ __forceinline__ void solve_line_delj(TP *__restrict__ ph, int sp, TG 
             gm[(i + 1) * gs] = g;
         }
     }
-    for (int i = L - 2; i >= 0; i--) {
-        u = fma(-(double)gm[(i + 1) * gs], u, ph[i * sp]);
-        ph[i * sp] = u;
-    }
+    back_substitute(ph, sp, gm, gs, L, u);
 }
 
 } // namespace dgb

@@ -396,14 +396,32 @@ static int k2_launch(K2Args &A, int nblocks, size_t smem, cudaStream_t st)
     return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
 }
 
+// Resident CTAs per SM for a dynamic shared-memory size.  The kernel's
+// dynamic-smem limit is raised to the opt-in maximum first: the occupancy
+// query honours the current limit, so without this its answer would depend on
+// the previous launch.
 static int k2_occupancy(bool delj, size_t smem)
 {
-    int nb = 0;
-    cudaError_t e = delj ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                               &nb, k_integrate2d<true>, K2_THREADS, smem)
-                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                               &nb, k_integrate2d<false>, K2_THREADS, smem);
-    return (e == cudaSuccess && nb > 0) ? nb : 1;
+    int dev = 0, optin = 0, nb = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaError_t e;
+    if (delj) {
+        cudaFuncSetAttribute(k_integrate2d<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             optin);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate2d<true>, K2_THREADS,
+                                                          smem);
+    } else {
+        cudaFuncSetAttribute(k_integrate2d<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             optin);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate2d<false>, K2_THREADS,
+                                                          smem);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return nb > 0 ? nb : 1;
 }
 
 static int k2_num_sms()
@@ -499,7 +517,11 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     int occ_g = k2_occupancy(A.use_delj, bytes_g + sizeof(K2Shared));
     size_t slice = (size_t)Lmax * Lmax * sizeof(double);
     int max_g_blocks = (int)std::min<size_t>((ws_bytes - 256) / slice, (size_t)nsm * occ_g);
-    bool use_s = fit_s && (occ_s * nsm >= max_g_blocks || max_g_blocks < nsm);
+    // gam in shared memory whenever it fits: measured on the 4096-instance IM
+    // batch at pts 80/90/100 it beats two CTAs per SM with gam in L2 (17.8 s
+    // vs 18.9 s), the FP64 pipe being saturated by one warp per SMSP
+    bool use_s = fit_s;
+    (void)occ_s;
     if (settings->gam_placement == 1) {
         if (!fit_s)
             return DGB_ERR_UNSUPPORTED;
