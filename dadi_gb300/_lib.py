@@ -28,7 +28,8 @@ EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
            "dgb_tridiag_batch", "dgb_implicit_sweep", "dgb_implicit_precalc_sweep",
            "dgb_integrate_table", "dgb_integrate_precalc", "dgb_sched2d",
            "dgb_batch2d_integrate", "dgb_batch2d_count_steps", "dgb_probe_fp64_fma",
-           "dgb_probe_rcp", "dgb_integrate2d_noalloc"]
+           "dgb_probe_rcp", "dgb_integrate2d_noalloc", "dgb_sched2d_deriv",
+           "dgb_batch2d_integrate_ckpt", "dgb_adjoint2d_scratch_bytes", "dgb_adjoint2d"]
 
 
 class PForm(ctypes.Structure):
@@ -82,6 +83,15 @@ def _declare(L):
         "dgb_probe_fp64_fma": (i, [_vp, i, i, i, i, _vp]),
         "dgb_probe_rcp": (i, [_vp, _vp, i, _vp]),
         "dgb_integrate2d_noalloc": (i, [_vp, i, _vp, _vp, i, i, i, i, _vp]),
+        "dgb_sched2d_deriv": (i, [_vp, _vp, i, i, _vp, ctypes.POINTER(Settings), _vp, _vp, _vp,
+                                  _vp]),
+        "dgb_batch2d_integrate_ckpt": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp,
+                                           _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(Settings),
+                                           _vp, _vp, i, _vp, sz, _vp]),
+        "dgb_adjoint2d_scratch_bytes": (sz, [i, i, i]),
+        "dgb_adjoint2d": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp, _vp,
+                              _vp, _vp, i, _vp, _vp, _vp, ctypes.POINTER(Settings), _vp, sz,
+                              _vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -69,6 +69,29 @@ def im_instances(params, initial_t=0.0, theta0=1.0):
     return rec
 
 
+#: dgb_seed2d: dT[6], dt0[6], dform[9 forms][a, b, c][6]
+SEED_DTYPE = np.dtype([("dT", "f8", 6), ("dt0", "f8", 6), ("dform", "f8", (9, 3, 6))])
+IM_PARAMS = ("s", "nu1", "nu2", "T", "m12", "m21")
+
+
+def im_seeds(n):
+    """Derivative seeds of im_instances' coefficients with respect to
+    (s, nu1, nu2, T, m12, m21): nu1(t) = s (nu1/s)**(t/T) has a = s, b = nu1,
+    c = T; nu2(t) = (1-s) (nu2/(1-s))**(t/T) has a = 1-s, b = nu2, c = T."""
+    sd = np.zeros(n, dtype=SEED_DTYPE)
+    S, N1, N2, T, M12, M21 = range(6)
+    sd["dT"][:, T] = 1
+    sd["dform"][:, 0, 0, S] = 1
+    sd["dform"][:, 0, 1, N1] = 1
+    sd["dform"][:, 0, 2, T] = 1
+    sd["dform"][:, 1, 0, S] = -1
+    sd["dform"][:, 1, 1, N2] = 1
+    sd["dform"][:, 1, 2, T] = 1
+    sd["dform"][:, 2, 0, M12] = 1
+    sd["dform"][:, 3, 0, M21] = 1
+    return sd
+
+
 def settings_from_globals(gam_placement=0):
     tsf, otsf, old, delj = integration.current_settings()
     return _lib.settings_struct(tsf, otsf, old, delj, gam_placement)
@@ -176,6 +199,98 @@ class Batch2D:
             o += n * L * L
         return phis, status
 
+    def loglik_and_grad(self, params, data, scale=1.0, ckpt_every=None, seeds=None, rec=None):
+        """Poisson log-likelihood of scale * (extrapolated IM spectrum) against
+        data for each parameter row, and its gradient with respect to
+        (s, nu1, nu2, T, m12, m21) by the discrete adjoint.  Returns CUDA
+        tensors (ll (n,), grad (n, 6), status (n,))."""
+        ll, ctx = self.forward_for_adjoint(params, data, scale, ckpt_every, seeds, rec)
+        grad = self.adjoint(ctx, self.torch.ones_like(ll))
+        return ll.detach(), grad, ctx["status"]
+
+    def forward_for_adjoint(self, params, data, scale=1.0, ckpt_every=None, seeds=None,
+                            rec=None):
+        """Forward pass that keeps what the adjoint needs: schedules,
+        derivative rows, checkpoints and the differentiable tail (from_phi,
+        extrapolation, likelihood) as a torch graph."""
+        torch = self.torch
+        lib = _lib.lib()
+        if rec is None:
+            rec = im_instances(params)
+        rec = np.ascontiguousarray(rec)
+        n = len(rec)
+        ng = len(self.pts_l)
+        st = settings_from_globals(self.gam_placement)
+        if st.use_delj_trick:
+            raise NotImplementedError("the adjoint does not support the delj trick")
+        sh = _lib.stream_handle(torch)
+        d_rec = torch.from_numpy(rec.view(np.uint8)).to("cuda")
+        table, off, cnt, status = self.schedule(d_rec, n)
+        seeds = im_seeds(n) if seeds is None else np.ascontiguousarray(seeds)
+        d_seed = torch.from_numpy(seeds.view(np.uint8)).to("cuda")
+        drows = torch.empty(max(int(table.numel() // 11), 1) * 60, dtype=torch.float64,
+                            device="cuda")
+        _lib.check(lib.dgb_sched2d_deriv(_lib.dptr(d_rec), _lib.dptr(d_seed), n, ng,
+                                         _lib.dptr(self.d_dx0), ctypes.byref(st), _lib.dptr(cnt),
+                                         _lib.dptr(off), _lib.dptr(drows), sh), "dgb_sched2d_deriv")
+        steps = cnt.to(torch.int64).view(n, -1)
+        Lsq = torch.tensor([L * L for L in self.pts_l], dtype=torch.int64, device="cuda")
+        cost = (steps * Lsq[None, :]).reshape(-1)
+        d_order = torch.argsort(-cost, stable=True).to(torch.int32)
+        smax = int(steps.max().item())
+        C = int(ckpt_every) if ckpt_every else max(8, min(256, int(np.ceil(np.sqrt(max(smax, 1))))))
+        per_item = ((steps + C - 1) // C).expand(n, ng) * Lsq[None, :]
+        ends = torch.cumsum(per_item.reshape(-1), 0)
+        ck_off = (ends - per_item.reshape(-1)).contiguous()
+        ckpt = torch.empty(max(int(ends[-1].item()), 1), dtype=torch.float64, device="cuda")
+        masks = (rec["frozen"].astype(np.int32) & 0xff) | ((rec["nomut"].astype(np.int32) & 0xff) << 8)
+        d_masks = torch.from_numpy(np.ascontiguousarray(masks)).to("cuda")
+        total = sum(n * L * L for L in self.pts_l)
+        d_out = torch.empty(total, dtype=torch.float64, device="cuda")
+        nws = lib.dgb_workspace_bytes(1, 2, max(self.pts_l), n * ng)
+        ws, nws = _lib.workspace(torch, nws)
+        _lib.check(lib.dgb_batch2d_integrate_ckpt(
+            _lib.dptr(d_masks), n, self.Ls, ng, _lib.dptr(self.d_xx), _lib.dptr(self.d_phi0),
+            _lib.dptr(d_out), _lib.dptr(table), _lib.dptr(off), _lib.dptr(cnt), _lib.dptr(d_order),
+            ctypes.byref(st), _lib.dptr(ckpt), _lib.dptr(ck_off), C, _lib.dptr(ws), nws, sh),
+            "dgb_batch2d_integrate_ckpt")
+        phis, o = [], 0
+        for L in self.pts_l:
+            phis.append(d_out[o:o + n * L * L].view(n, L, L).detach().requires_grad_(True))
+            o += n * L * L
+        d = data if torch.is_tensor(data) else _lib.to_device(torch, data)
+        with torch.enable_grad():
+            fs = self.extrapolate(self.spectra(phis))
+            ll = self.loglik(fs, d, scale)
+        ctx = dict(phis=phis, ll=ll, table=table, off=off, cnt=cnt, drows=drows, ckpt=ckpt,
+                   ck_off=ck_off, C=C, masks=d_masks, order=d_order, status=status, n=n, st=st)
+        return ll, ctx
+
+    def adjoint(self, ctx, grad_ll):
+        """d(sum_i grad_ll[i] * ll_i)/d(params) by the discrete adjoint: (n, 6)."""
+        torch = self.torch
+        lib = _lib.lib()
+        phis = ctx["phis"]
+        lams = torch.autograd.grad(ctx["ll"], phis, grad_outputs=grad_ll, allow_unused=True)
+        lam = torch.cat([(l if l is not None else torch.zeros_like(p)).reshape(-1)
+                         for l, p in zip(lams, phis)]).contiguous()
+        n = ctx["n"]
+        ng = len(self.pts_l)
+        grad = torch.zeros(n, 6, dtype=torch.float64, device="cuda")
+        C = ctx["C"]
+        Lmax = max(self.pts_l)
+        per_cta = lib.dgb_adjoint2d_scratch_bytes(Lmax, C, 1)
+        nblocks = min(n * ng, torch.cuda.get_device_properties(0).multi_processor_count * 2)
+        ws, nws = _lib.workspace(torch, 256 + per_cta * nblocks)
+        st = ctx["st"]
+        _lib.check(lib.dgb_adjoint2d(
+            _lib.dptr(ctx["masks"]), n, self.Ls, ng, _lib.dptr(self.d_xx), _lib.dptr(ctx["table"]),
+            _lib.dptr(ctx["drows"]), _lib.dptr(ctx["off"]), _lib.dptr(ctx["cnt"]),
+            _lib.dptr(ctx["ckpt"]), _lib.dptr(ctx["ck_off"]), C, _lib.dptr(lam), _lib.dptr(grad),
+            _lib.dptr(ctx["order"]), ctypes.byref(st), _lib.dptr(ws), nws,
+            _lib.stream_handle(torch)), "dgb_adjoint2d")
+        return grad
+
     def spectra(self, phis):
         """Per-grid raw spectra (n, n1+1, n2+1) on the device."""
         return [spectrum.from_phi_2D_batch(self.torch, p, self.ns[0], self.ns[1], xx)
@@ -215,3 +330,33 @@ class Batch2D:
         fs = self.extrapolate(self.spectra(phis))
         ll = self.loglik(fs, data, scale) if data is not None else None
         return fs, ll, status
+
+
+class IMLogLik:
+    """torch.autograd.Function wrapper: ll = IMLogLik.apply(engine, params,
+    data, scale) with params a (n, 6) float64 tensor of IM parameters
+    (s, nu1, nu2, T, m12, m21); ll.backward() runs the discrete adjoint."""
+
+    @staticmethod
+    def _function():
+        import torch
+
+        class _Fn(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, params, engine, data, scale):
+                p = params.detach().cpu().numpy()
+                ll, actx = engine.forward_for_adjoint(p, data, scale)
+                ctx.engine = engine
+                ctx.actx = actx
+                ctx.dev = params.device
+                return ll.detach()
+
+            @staticmethod
+            def backward(ctx, grad_ll):
+                g = ctx.engine.adjoint(ctx.actx, grad_ll.contiguous())
+                return g.to(ctx.dev), None, None, None
+        return _Fn
+
+    @classmethod
+    def apply(cls, engine, params, data, scale=1.0):
+        return cls._function().apply(params, engine, data, scale)

@@ -1,0 +1,675 @@
+// Discrete adjoint of the batched 2-population integrator.
+//
+// Forward (k_integrate2d with checkpoints): phi_{k+1} = Y_k^{-1} X_k^{-1}
+// (phi_k + inj_k), with X_k, Y_k the dt-scaled tridiagonal operators
+// A' = I + dt D of the x and y sweeps (dadi/integration2D.c:19-160) and inj_k
+// the mutation mass of dadi/Integration.py:76-87.  Given lambda_n = dJ/dphi_n,
+// each step backwards solves the transposed systems
+//     mu = Y_k^{-T} lambda_{k+1},   nu = X_k^{-T} mu,   lambda_k = nu
+// and contracts  dJ/dq = -mu^T (dY/dq) phi_{k+1} - nu^T (dX/dq) chi_k
+// (chi_k = X_k^{-1} psi_k, psi_k = phi_k + inj_k) for every per-step scalar
+// q of the parameter row: dt (through A' - I = dt D and the injection), nu,
+// m, gamma, h of each axis, and theta0 (through the injection).  For dt the
+// contraction is -(mu.r - mu.phi)/dt with r the sweep's right-hand side; for
+// the others it is a sum over intervals of (f_i mu_i - f_{i+1} mu_{i+1})
+// times the interval's coefficient derivatives (the a/b/c layout of
+// compute_abc_nobc, dadi/integration_shared.c:72-93), plus the corner
+// boundary terms.  The chain rule to the model parameters uses derivative
+// rows dq_k/dtheta produced by a forward-mode (dual number) walk of the same
+// schedule (k_sched2d_dual), which carries the schedule's own dependence on
+// theta: dt from the parameters at the current time (_compute_dt,
+// dadi/Integration.py:147-176), the final partial step T - t, and t/T inside
+// the parametric sizes.
+//
+// Memory: phi is checkpointed every C steps by the forward pass; each segment
+// of C steps is recomputed from its checkpoint into a per-CTA buffer, then
+// walked backwards.  All per-item arrays live in global memory (per-CTA
+// slices), so any grid size runs.
+#include <algorithm>
+
+#include "dgb_common.cuh"
+#include "dgb_internal.h"
+
+namespace dgb {
+
+constexpr int AD_THREADS = 128;
+constexpr int AD_MAXG = DGB_B2_MAXG;
+constexpr int NPAR = DGB_AD_NPAR; // parameters differentiated
+constexpr int NQ = 10;            // per-step scalars of a 2-D parameter row
+enum { Q_DT, Q_NU0, Q_NU1, Q_M01, Q_M10, Q_G0, Q_G1, Q_H0, Q_H1, Q_TH };
+
+// ------------------------------------------------------- dual numbers
+
+struct Dual {
+    double v;
+    double d[NPAR];
+};
+
+__device__ __forceinline__ Dual dconst(double v)
+{
+    Dual r;
+    r.v = v;
+#pragma unroll
+    for (int p = 0; p < NPAR; p++)
+        r.d[p] = 0;
+    return r;
+}
+
+__device__ __forceinline__ Dual dseed(double v, const double *d)
+{
+    Dual r;
+    r.v = v;
+#pragma unroll
+    for (int p = 0; p < NPAR; p++)
+        r.d[p] = d[p];
+    return r;
+}
+
+// d of a parametric form value f(t) with coefficient seeds (a, b, c) and t.
+__device__ Dual pform_dual(const dgb_pform &f, const double *da, const double *db,
+                           const double *dc, const Dual &t)
+{
+    Dual r;
+    r.v = pform_eval(f, t.v);
+    const double a = f.a, b = f.b, c = f.c;
+    switch (f.kind) {
+    case DGB_PF_EXPGROW: {
+        // a (b/a)^(t/c)
+        double q = b / a, y = t.v / c, p = pow(q, y), lq = log(q);
+#pragma unroll
+        for (int k = 0; k < NPAR; k++) {
+            double dq = (db[k] - q * da[k]) / a;
+            double dy = (t.d[k] - y * dc[k]) / c;
+            r.d[k] = da[k] * p + a * p * (y * dq / q + lq * dy);
+        }
+        break;
+    }
+    case DGB_PF_EXPLOG: {
+        // a exp(log(b/a) t / c)
+        double L0 = log(b / a), z = L0 * t.v / c, e = exp(z);
+#pragma unroll
+        for (int k = 0; k < NPAR; k++) {
+            double dL = db[k] / b - da[k] / a;
+            double dz = (dL * t.v + L0 * t.d[k]) / c - z * dc[k] / c;
+            r.d[k] = da[k] * e + a * e * dz;
+        }
+        break;
+    }
+    case DGB_PF_LINEAR:
+#pragma unroll
+        for (int k = 0; k < NPAR; k++)
+            r.d[k] = da[k] + db[k] * t.v + b * t.d[k];
+        break;
+    default:
+#pragma unroll
+        for (int k = 0; k < NPAR; k++)
+            r.d[k] = da[k];
+    }
+    return r;
+}
+
+// Derivative of compute_dt (dadi/Integration.py:147-176) along the branch the
+// value takes; the value itself is compute_dt's.
+__device__ Dual compute_dt_dual(const Dual &nu, const Dual &msum, const Dual &gamma,
+                                const Dual &h, const dgb_settings &s, double dx0)
+{
+    Dual r;
+    r.v = compute_dt(nu.v, msum.v, gamma.v, h.v, s, dx0);
+#pragma unroll
+    for (int k = 0; k < NPAR; k++)
+        r.d[k] = 0;
+    if (s.use_old_timestep)
+        return r;
+    double v1 = 0.25 / nu.v;
+    double t1 = fabs(h.v + (1 - 2 * h.v) * 0.5) * 0.5 * (1 - 0.5);
+    double u2 = h.v + (1 - 2 * h.v) * 0.25;
+    double t2 = fabs(u2) * 0.25 * (1 - 0.25);
+    bool use_t2 = t2 > t1;
+    double tm = use_t2 ? t2 : t1;
+    double v3 = fabs(gamma.v) * 2 * tm;
+    int branch = 0;
+    double mx = v1;
+    if (msum.v > mx) {
+        mx = msum.v;
+        branch = 1;
+    }
+    if (v3 > mx) {
+        mx = v3;
+        branch = 2;
+    }
+    if (!(mx > 0))
+        return r;
+    double sg = gamma.v >= 0 ? 1.0 : -1.0, su = u2 >= 0 ? 1.0 : -1.0;
+#pragma unroll
+    for (int k = 0; k < NPAR; k++) {
+        double dmx;
+        if (branch == 0)
+            dmx = -0.25 * nu.d[k] / (nu.v * nu.v);
+        else if (branch == 1)
+            dmx = msum.d[k];
+        else {
+            double dtm = use_t2 ? su * 0.5 * h.d[k] * 0.25 * (1 - 0.25) : 0.0;
+            dmx = sg * gamma.d[k] * 2 * tm + fabs(gamma.v) * 2 * dtm;
+        }
+        r.d[k] = -s.timescale_factor * dmx / (mx * mx);
+    }
+    return r;
+}
+
+// The schedule walk of sched2d (dgb_integrate2d.cu) with derivatives, for
+// exactly nrows steps; writes NQ x NPAR derivative doubles per step.
+__device__ void sched2d_walk_dual(const dgb_inst2d &I, const dgb_seed2d &S,
+                                  const dgb_settings &st, double dx0, int nrows, double *drows)
+{
+    const dgb_pform *F[9] = {&I.nu[0], &I.nu[1], &I.m12, &I.m21, &I.gamma[0],
+                             &I.gamma[1], &I.h[0], &I.h[1], &I.theta0};
+    Dual cur = dseed(I.initial_t, S.dt0);
+    Dual T = dseed(I.T, S.dT);
+    Dual P[9];
+    for (int f = 0; f < 8; f++)
+        P[f] = pform_dual(*F[f], S.dform[f][0], S.dform[f][1], S.dform[f][2], cur);
+    for (int n = 0; n < nrows; n++) {
+        Dual d0 = compute_dt_dual(P[0], P[2], P[4], P[6], st, dx0);
+        Dual d1 = compute_dt_dual(P[1], P[3], P[5], P[7], st, dx0);
+        Dual dtm = (d1.v < d0.v) ? d1 : d0;
+        Dual rem;
+        rem.v = T.v - cur.v;
+#pragma unroll
+        for (int k = 0; k < NPAR; k++)
+            rem.d[k] = T.d[k] - cur.d[k];
+        Dual dt = (rem.v < dtm.v) ? rem : dtm;
+        Dual next;
+        next.v = cur.v + dt.v;
+#pragma unroll
+        for (int k = 0; k < NPAR; k++)
+            next.d[k] = cur.d[k] + dt.d[k];
+        for (int f = 0; f < 9; f++)
+            P[f] = pform_dual(*F[f], S.dform[f][0], S.dform[f][1], S.dform[f][2], next);
+        double *o = drows + (size_t)n * NQ * NPAR;
+        const Dual *q[NQ] = {&dt, &P[0], &P[1], &P[2], &P[3], &P[4], &P[5], &P[6], &P[7], &P[8]};
+        for (int j = 0; j < NQ; j++)
+#pragma unroll
+            for (int k = 0; k < NPAR; k++)
+                o[j * NPAR + k] = q[j]->d[k];
+        cur = next;
+    }
+}
+
+__global__ void k_sched2d_dual(const dgb_inst2d *insts, const dgb_seed2d *seeds, int nsched,
+                               int ngrids, int per_grid, const double *dx0s, dgb_settings st,
+                               const int *row_cnt, const long *row_off, double *drows)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsched)
+        return;
+    int inst = per_grid ? s / ngrids : s;
+    double dx0 = dx0s[per_grid ? s % ngrids : 0];
+    sched2d_walk_dual(insts[inst], seeds[inst], st, dx0, row_cnt[s],
+                      drows + row_off[s] * NQ * NPAR);
+}
+
+// ------------------------------------------------------- adjoint kernel
+
+struct ADArgs {
+    int ngrids;
+    int L[AD_MAXG];
+    long xx_off[AD_MAXG];
+    long out_off[AD_MAXG];
+    const double *xx_all;
+    const double *table;  // value rows (11 per step)
+    const double *drows;  // derivative rows (NQ*NPAR per step), same row offsets
+    const long *row_off;
+    const int *row_cnt;
+    int sched_per_grid;
+    const int *masks;
+    const double *ckpt;
+    const long *ckpt_off;
+    int ckpt_every;
+    double *lam;          // dJ/dphi_final in the phi_out layout (overwritten)
+    double *grad;         // ninst x NPAR, accumulated (caller zeroes)
+    const int *order;
+    int nwork;
+    int *counter;
+    double *scratch;      // per CTA: (ckpt_every + 3) * Lmax^2 doubles
+    int Lmax;
+};
+
+struct ADVecs {
+    AxisVecs f[2]; // forward coefficient vectors
+    AxisVecs t[2]; // transposed (sub/super swapped)
+};
+
+struct ADShared {
+    AxisScalars ax[2];
+    double inj, dinj_dt, dinj_th;
+    double D[NQ * NPAR];
+    int item;
+};
+
+__device__ __forceinline__ void ad_axis_scalars(AxisScalars &s, int a, const double *row,
+                                                const GridVecs &g, int L)
+{
+    double dt = row[0];
+    s.dt = dt;
+    s.nu = row[row_nu(2, a)];
+    s.inv_nu = 1.0 / s.nu;
+    s.gamma = row[row_gamma(2, a)];
+    s.h = row[row_h(2, a)];
+    double m = row[row_mig(2, a, 1 - a)];
+    s.msum = m;
+    s.mig[a] = 0;
+    s.mig[1 - a] = m;
+    s.B1s = 0.5 * (dt * g.dfac[0]);
+    s.B1e = -0.5 * (dt * g.dfac[L - 1]);
+    corner_bc(2, a, s.mig, s.nu, s.gamma, s.h, g.x[0], g.x[L - 1], g.dx[0], g.dx[L - 2], dt,
+              s.bcs, s.bce);
+}
+
+// Per-step setup shared by the recomputation and the backward step: axis
+// scalars, injection value and (with transposed) the derivative row.
+__device__ void ad_step_setup(ADShared &S, ADVecs &V, const GridVecs &g, int L, const double *row,
+                              const double *drow, bool transposed)
+{
+    const int tid = threadIdx.x;
+    if (tid < 2)
+        ad_axis_scalars(S.ax[tid], tid, row, g, L);
+    else if (tid == 2) {
+        S.inj = inject_value(2, row[0], row[1], g.x[0], g.x[1], g.x[2]);
+        S.dinj_dt = inject_value(2, 1.0, row[1], g.x[0], g.x[1], g.x[2]);
+        S.dinj_th = inject_value(2, row[0], 1.0, g.x[0], g.x[1], g.x[2]);
+    }
+    if (transposed)
+        for (int j = tid; j < NQ * NPAR; j += blockDim.x)
+            S.D[j] = drow[j];
+    __syncthreads();
+    for (int t = tid; t < 2 * L; t += blockDim.x) {
+        int a = t >= L, i = t - a * L;
+        build_axis_entry(i, L, g, S.ax[a], 1.0, false, V.f[a]);
+    }
+    __syncthreads();
+    if (transposed) {
+        for (int t = tid; t < 2 * L; t += blockDim.x) {
+            int a = t >= L, i = t - a * L;
+            V.t[a].A1[i] = (i > 0) ? V.f[a].C1[i - 1] : 0.0;
+            V.t[a].A0[i] = (i > 0) ? V.f[a].C0[i - 1] : 0.0;
+            V.t[a].C1[i] = (i < L - 1) ? V.f[a].A1[i + 1] : 0.0;
+            V.t[a].C0[i] = (i < L - 1) ? V.f[a].A0[i + 1] : 0.0;
+            V.t[a].B0[i] = V.f[a].B0[i];
+        }
+        __syncthreads();
+    }
+}
+
+// Solve all lines of axis a of the L x L row-major array u (in place), with
+// the forward or transposed vectors.
+__device__ void ad_sweep(double *u, double *gam, int L, int a, const AxisVecs &v,
+                         const AxisScalars &s, const GridVecs &g, int j0, int j1)
+{
+    const int sp = (a == 0) ? L : 1, sl = (a == 0) ? 1 : L;
+    for (int line = threadIdx.x; line < L; line += blockDim.x) {
+        double W = s.mig[1 - a] * g.x[line];
+        double bs = (line == j0) ? s.bcs : 0.0;
+        double be = (line == j1) ? s.bce : 0.0;
+        solve_line(u + (size_t)line * sl, sp, gam + line, L, L, W, bs, be, v, s);
+    }
+}
+
+// Sensitivities of -mu^T (dA'/dq) phi for the lines of axis a handled by this
+// thread, added into G[Q_DT], G[nu], G[m], G[gamma], G[h] of that axis.
+__device__ void ad_contract(const double *mu, const double *phi, const double *rhs,
+                            const double *inj_pts, double inj, int L, int a,
+                            const AxisScalars &s, const GridVecs &g, int j0, int j1, double *G)
+{
+    const int sp = (a == 0) ? L : 1, sl = (a == 0) ? 1 : L;
+    const int qn = a ? Q_NU1 : Q_NU0, qm = a ? Q_M10 : Q_M01, qg = a ? Q_G1 : Q_G0,
+              qh = a ? Q_H1 : Q_H0;
+    const double dt = s.dt, inu = s.inv_nu, gam = s.gamma, hh = s.h;
+    for (int line = threadIdx.x; line < L; line += blockDim.x) {
+        const double *m = mu + (size_t)line * sl, *p = phi + (size_t)line * sl,
+                     *r = rhs + (size_t)line * sl;
+        const double o = g.x[line];
+        double smr = 0, smp = 0, snu = 0, sm = 0, sg = 0, sh = 0;
+        double mi = m[0], pi = p[0];
+        for (int i = 0; i < L; i++) {
+            double ri = r[i * sp];
+            if (inj_pts) {
+                // psi = phi + injection at (1,0) / (0,1), which lie on lines 0 / 1
+                int row = (a == 0) ? i : line, col = (a == 0) ? line : i;
+                if ((row == 1 && col == 0) && inj_pts[0] != 0.0)
+                    ri += inj;
+                if ((row == 0 && col == 1) && inj_pts[1] != 0.0)
+                    ri += inj;
+            }
+            smr = fma(mi, ri, smr);
+            smp = fma(mi, pi, smp);
+            if (i < L - 1) {
+                double mn = m[(i + 1) * sp], pn = p[(i + 1) * sp];
+                double xi = g.xInt[i];
+                double Pi = inu * g.xv[i] * g.ih[i];
+                double Qi = inu * g.xv[i + 1] * g.ih[i];
+                double Di = g.dfac[i] * mi - g.dfac[i + 1] * mn;
+                double hp = 0.5 * (pi + pn);
+                double xx1 = xi * (1. - xi);
+                snu = fma(Di, (Qi * pn - Pi * pi) * inu, snu);
+                sm = fma(Di * (o - xi), hp, sm);
+                sg = fma(Di * (2 * (hh + (1. - 2 * hh) * xi) * xx1), hp, sg);
+                sh = fma(Di * (gam * 2 * (1. - 2 * xi) * xx1), hp, sh);
+                mi = mn;
+                pi = pn;
+            }
+        }
+        double bnu = 0, bm = 0, bg = 0, bh = 0;
+        if (line == j0 && s.bcs != 0.0) {
+            double x0 = g.x[0], f = dt * 2. / g.dx[0], w = m[0] * p[0];
+            bnu += w * f * (-0.5 * inu * inu);
+            bm += w * f * x0;
+            bg -= w * f * (2 * (hh + (1. - 2 * hh) * x0) * x0 * (1. - x0));
+            bh -= w * f * (gam * 2 * (1. - 2 * x0) * x0 * (1. - x0));
+        }
+        if (line == j1 && s.bce != 0.0) {
+            double xl = g.x[L - 1], f = dt * 2. / g.dx[L - 2];
+            double w = m[(L - 1) * sp] * p[(L - 1) * sp];
+            bnu += w * f * (-0.5 * inu * inu);
+            bm += w * f * (1. - xl);
+            bg += w * f * (2 * (hh + (1. - 2 * hh) * xl) * xl * (1. - xl));
+            bh += w * f * (gam * 2 * (1. - 2 * xl) * xl * (1. - xl));
+        }
+        G[Q_DT] -= (smr - smp) / dt;
+        G[qn] -= dt * snu + bnu;
+        G[qm] -= dt * sm + bm;
+        G[qg] -= dt * sg + bg;
+        G[qh] -= dt * sh + bh;
+    }
+}
+
+__device__ __forceinline__ void ad_carve(double *smem, int L, GridVecs &g, ADVecs &V)
+{
+    double *p = smem;
+    g.x = p; p += L;
+    g.xv = p; p += L;
+    g.dfac = p; p += L;
+    g.xInt = p; p += L;
+    g.ih = p; p += L;
+    g.dx = p; p += L;
+    for (int a = 0; a < 2; a++) {
+        V.f[a].A1 = p; p += L;
+        V.f[a].A0 = p; p += L;
+        V.f[a].C1 = p; p += L;
+        V.f[a].C0 = p; p += L;
+        V.f[a].B0 = p; p += L;
+        V.t[a].A1 = p; p += L;
+        V.t[a].A0 = p; p += L;
+        V.t[a].C1 = p; p += L;
+        V.t[a].C0 = p; p += L;
+        V.t[a].B0 = p; p += L;
+    }
+}
+
+__global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
+{
+    extern __shared__ __align__(16) double smem[];
+    __shared__ ADShared S;
+    __shared__ double red[AD_THREADS / 32][NPAR];
+    const int tid = threadIdx.x;
+    GridVecs g;
+    ADVecs V;
+    ad_carve(smem, A.Lmax, g, V);
+    const size_t L2max = (size_t)A.Lmax * A.Lmax;
+    double *seg = A.scratch + (size_t)blockIdx.x * (A.ckpt_every + 3) * L2max;
+    double *W1 = seg + (size_t)(A.ckpt_every + 1) * L2max;
+    double *gam = W1 + L2max;
+
+    for (;;) {
+        if (tid == 0)
+            S.item = atomicAdd(A.counter, 1);
+        __syncthreads();
+        const int w = S.item;
+        if (w >= A.nwork)
+            break;
+        const int wid = A.order[w];
+        const int inst = wid / A.ngrids;
+        const int gi = wid - inst * A.ngrids;
+        const int L = A.L[gi];
+        const size_t LL = (size_t)L * L;
+        const double *xx = A.xx_all + A.xx_off[gi];
+        double *lam = A.lam + A.out_off[gi] + (size_t)inst * LL;
+        const int sidx = A.sched_per_grid ? wid : inst;
+        const double *rows = A.table + A.row_off[sidx] * 11;
+        const double *drows = A.drows + A.row_off[sidx] * NQ * NPAR;
+        const int n = A.row_cnt[sidx];
+        const double *ck = A.ckpt + A.ckpt_off[wid];
+        const int frozen = A.masks ? (A.masks[inst] & 0xff) : 0;
+        const int nomut = A.masks ? (A.masks[inst] >> 8 & 0xff) : 0;
+        const bool injx = !(frozen & 1) && !(nomut & 1), injy = !(frozen & 2) && !(nomut & 2);
+        const int C = A.ckpt_every;
+
+        for (int i = tid; i < L; i += blockDim.x) {
+            double x = xx[i];
+            g.x[i] = x;
+            g.xv[i] = x * (1. - x);
+            if (i < L - 1) {
+                double d = xx[i + 1] - x;
+                g.dx[i] = d;
+                g.ih[i] = 1.0 / (2 * d);
+                g.xInt[i] = 0.5 * (xx[i + 1] + x);
+            }
+        }
+        __syncthreads();
+        for (int i = tid; i < L; i += blockDim.x) {
+            if (i == 0)
+                g.dfac[i] = 2. / g.dx[0];
+            else if (i == L - 1)
+                g.dfac[i] = 2. / g.dx[L - 2];
+            else
+                g.dfac[i] = 2. / (g.dx[i] + g.dx[i - 1]);
+        }
+        __syncthreads();
+        const int j0 = (g.x[0] == 0.0) ? 0 : -1;
+        const int j1 = (g.x[L - 1] == 1.0) ? L - 1 : -1;
+        double acc[NPAR];
+#pragma unroll
+        for (int p = 0; p < NPAR; p++)
+            acc[p] = 0;
+        const double inj_on[2] = {injx ? 1.0 : 0.0, injy ? 1.0 : 0.0};
+
+        const int nseg = (n + C - 1) / C;
+        for (int sgi = nseg - 1; sgi >= 0; sgi--) {
+            const int k0 = sgi * C, k1 = min(k0 + C, n);
+            for (size_t idx = tid; idx < LL; idx += blockDim.x)
+                seg[idx] = ck[(size_t)sgi * LL + idx];
+            __syncthreads();
+            // recompute phi_{k0+1} .. phi_{k1} into seg slots 1 .. k1-k0
+            for (int k = k0; k < k1 - 1; k++) {
+                ad_step_setup(S, V, g, L, rows + (size_t)k * 11, nullptr, false);
+                double *src = seg + (size_t)(k - k0) * LL, *dst = src + LL;
+                for (size_t idx = tid; idx < LL; idx += blockDim.x)
+                    dst[idx] = src[idx];
+                __syncthreads();
+                if (tid == 0) {
+                    if (injx)
+                        dst[1 * L + 0] += S.inj;
+                    if (injy)
+                        dst[0 * L + 1] += S.inj;
+                }
+                __syncthreads();
+                for (int a = 0; a < 2; a++) {
+                    if (frozen & (1 << a))
+                        continue;
+                    ad_sweep(dst, gam, L, a, V.f[a], S.ax[a], g, j0, j1);
+                    __syncthreads();
+                }
+            }
+            // backward through the segment
+            for (int k = k1 - 1; k >= k0; k--) {
+                ad_step_setup(S, V, g, L, rows + (size_t)k * 11,
+                              drows + (size_t)k * NQ * NPAR, true);
+                const double *phik = seg + (size_t)(k - k0) * LL;
+                // phi_{k+1}: the next slot, or for the segment's last step the
+                // checkpoint of the next segment / the final density, both
+                // recomputed here into W1 after chi is no longer needed.
+                // chi_k = X^{-1}(phi_k + inj) into W1
+                for (size_t idx = tid; idx < LL; idx += blockDim.x)
+                    W1[idx] = phik[idx];
+                __syncthreads();
+                if (tid == 0) {
+                    if (injx)
+                        W1[1 * L + 0] += S.inj;
+                    if (injy)
+                        W1[0 * L + 1] += S.inj;
+                }
+                __syncthreads();
+                if (!(frozen & 1)) {
+                    ad_sweep(W1, gam, L, 0, V.f[0], S.ax[0], g, j0, j1);
+                    __syncthreads();
+                }
+                double G[NQ];
+#pragma unroll
+                for (int q = 0; q < NQ; q++)
+                    G[q] = 0;
+                // phi_{k+1} = Y^{-1} chi: slot k-k0+1 holds it unless k is the
+                // segment's last step; then recompute it in the spare slot.
+                double *phin = seg + (size_t)(k - k0 + 1) * LL;
+                if (k == k1 - 1) {
+                    for (size_t idx = tid; idx < LL; idx += blockDim.x)
+                        phin[idx] = W1[idx];
+                    __syncthreads();
+                    if (!(frozen & 2)) {
+                        ad_sweep(phin, gam, L, 1, V.f[1], S.ax[1], g, j0, j1);
+                        __syncthreads();
+                    }
+                }
+                // y: mu = Y^{-T} lambda, contract with phi_{k+1}, rhs chi
+                if (!(frozen & 2)) {
+                    ad_sweep(lam, gam, L, 1, V.t[1], S.ax[1], g, j0, j1);
+                    __syncthreads();
+                    ad_contract(lam, phin, W1, nullptr, 0.0, L, 1, S.ax[1], g, j0, j1, G);
+                    __syncthreads();
+                }
+                // x: nu = X^{-T} mu, contract with chi, rhs psi
+                if (!(frozen & 1)) {
+                    ad_sweep(lam, gam, L, 0, V.t[0], S.ax[0], g, j0, j1);
+                    __syncthreads();
+                    ad_contract(lam, W1, phik, inj_on, S.inj, L, 0, S.ax[0], g, j0, j1, G);
+                }
+                // injection: d psi(1,0), psi(0,1) / d(dt, theta0)
+                if (tid == 0) {
+                    double lin = (injx ? lam[1 * L + 0] : 0.0) + (injy ? lam[0 * L + 1] : 0.0);
+                    G[Q_DT] += lin * S.dinj_dt;
+                    G[Q_TH] += lin * S.dinj_th;
+                }
+#pragma unroll
+                for (int p = 0; p < NPAR; p++) {
+                    double sacc = acc[p];
+#pragma unroll
+                    for (int q = 0; q < NQ; q++)
+                        sacc = fma(G[q], S.D[q * NPAR + p], sacc);
+                    acc[p] = sacc;
+                }
+                __syncthreads();
+            }
+        }
+        // block reduction of acc into grad[inst]
+#pragma unroll
+        for (int p = 0; p < NPAR; p++) {
+            double v = acc[p];
+            for (int off = 16; off > 0; off >>= 1)
+                v += __shfl_down_sync(0xffffffffu, v, off);
+            if ((tid & 31) == 0)
+                red[tid >> 5][p] = v;
+        }
+        __syncthreads();
+        if (tid < NPAR) {
+            double v = 0;
+            for (int wv = 0; wv < (int)(blockDim.x >> 5); wv++)
+                v += red[wv][tid];
+            atomicAdd(A.grad + (size_t)inst * NPAR + tid, v);
+        }
+        __syncthreads();
+    }
+}
+
+} // namespace dgb
+
+// ------------------------------------------------------------------ C ABI
+
+extern "C" int dgb_sched2d_deriv(const dgb_inst2d *insts, const dgb_seed2d *seeds, int ninst,
+                                 int ngrids, const double *dx0s, const dgb_settings *settings,
+                                 const int *row_cnt, const long *row_off, double *drows,
+                                 void *stream)
+{
+    if (!insts || !seeds || ninst < 1 || ngrids < 1 || !dx0s || !settings || !row_cnt ||
+        !row_off || !drows)
+        return DGB_ERR_ARG;
+    int per_grid = settings->use_old_timestep ? 1 : 0;
+    int nsched = per_grid ? ninst * ngrids : ninst;
+    dgb::k_sched2d_dual<<<(nsched + 31) / 32, 32, 0, (cudaStream_t)stream>>>(
+        insts, seeds, nsched, ngrids, per_grid, dx0s, *settings, row_cnt, row_off, drows);
+    return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
+}
+
+extern "C" size_t dgb_adjoint2d_scratch_bytes(int Lmax, int ckpt_every, int nblocks)
+{
+    return (size_t)nblocks * (ckpt_every + 3) * Lmax * Lmax * sizeof(double);
+}
+
+extern "C" int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngrids,
+                             const double *xx_all, const double *table, const double *drows,
+                             const long *row_off, const int *row_cnt, const double *ckpt,
+                             const long *ckpt_off, int ckpt_every, double *lam, double *grad,
+                             const int *order, const dgb_settings *settings, void *ws,
+                             size_t ws_bytes, void *stream)
+{
+    using namespace dgb;
+    if (!Ls || !xx_all || !table || !drows || !row_off || !row_cnt || !ckpt || !ckpt_off ||
+        ckpt_every < 1 || !lam || !grad || !order || !settings || ngrids < 1 ||
+        ngrids > AD_MAXG || ninst < 1)
+        return DGB_ERR_ARG;
+    if (settings->use_delj_trick)
+        return DGB_ERR_UNSUPPORTED;
+    ADArgs A = {};
+    A.ngrids = ngrids;
+    long xo = 0, oo = 0;
+    int Lmax = 0;
+    for (int gi = 0; gi < ngrids; gi++) {
+        if (Ls[gi] < 3)
+            return DGB_ERR_ARG;
+        A.L[gi] = Ls[gi];
+        A.xx_off[gi] = xo;
+        A.out_off[gi] = oo;
+        xo += Ls[gi];
+        oo += (long)ninst * Ls[gi] * Ls[gi];
+        Lmax = std::max(Lmax, Ls[gi]);
+    }
+    A.xx_all = xx_all;
+    A.table = table;
+    A.drows = drows;
+    A.row_off = row_off;
+    A.row_cnt = row_cnt;
+    A.sched_per_grid = settings->use_old_timestep ? 1 : 0;
+    A.masks = masks;
+    A.ckpt = ckpt;
+    A.ckpt_off = ckpt_off;
+    A.ckpt_every = ckpt_every;
+    A.lam = lam;
+    A.grad = grad;
+    A.order = order;
+    A.nwork = ninst * ngrids;
+    A.Lmax = Lmax;
+    if (!ws || ws_bytes < 256)
+        return DGB_ERR_WORKSPACE;
+    A.counter = (int *)ws;
+    size_t per_cta = (size_t)(ckpt_every + 3) * Lmax * Lmax * sizeof(double);
+    long nblocks = (long)((ws_bytes - 256) / per_cta);
+    if (nblocks < 1)
+        return DGB_ERR_WORKSPACE;
+    nblocks = std::min<long>(nblocks, A.nwork);
+    A.scratch = (double *)((char *)ws + 256);
+    size_t smem = (size_t)26 * Lmax * sizeof(double);
+    if (cudaFuncSetAttribute(k_adjoint2d, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+        return DGB_ERR_CUDA;
+    if (cudaMemsetAsync(A.counter, 0, sizeof(int), (cudaStream_t)stream) != cudaSuccess)
+        return DGB_ERR_CUDA;
+    k_adjoint2d<<<(unsigned)nblocks, AD_THREADS, smem, (cudaStream_t)stream>>>(A);
+    return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
+}

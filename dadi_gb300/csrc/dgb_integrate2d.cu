@@ -56,6 +56,9 @@ struct K2Args {
     int gam_smem;          // 1: gam in shared memory
     double *gam_glob;      // per-CTA slices of Lmax*Lmax doubles
     int use_delj;
+    double *ckpt;          // optional: phi before every ckpt_every-th step
+    const long *ckpt_off;  // first checkpoint double of each work id
+    int ckpt_every;
 };
 
 __host__ __device__ inline int odd_pitch(int L) { return (L % 2) ? L : L + 1; }
@@ -206,6 +209,14 @@ __global__ void __launch_bounds__(K2_THREADS) k_integrate2d(K2Args A)
 
         for (int step = 0; step < nsteps; step++) {
             const double *row = rows + (size_t)step * K2_ROW;
+            if (A.ckpt && step % A.ckpt_every == 0) {
+                // checkpoint for the adjoint: phi before this step, row-major
+                double *c = A.ckpt + A.ckpt_off[wid] + (size_t)(step / A.ckpt_every) * L * L;
+                for (int idx = tid; idx < L * L; idx += blockDim.x) {
+                    int r = idx / L, q = idx - r * L;
+                    c[idx] = phi[r * pitch + q];
+                }
+            }
             // ---- step scalars: lane a of warp 0 handles axis a, lane 2 the injection
             if (warp == 0) {
                 if (lane < 2)
@@ -472,7 +483,8 @@ size_t k2_batch_ws_bytes(int Lmax, long nwork)
 int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const double *xx_all,
              const double *phi0_all, double *phi_out, const double *table, const long *row_off,
              const int *row_cnt, int sched_per_grid, const int *order,
-             const dgb_settings *settings, void *ws, size_t ws_bytes, cudaStream_t st)
+             const dgb_settings *settings, void *ws, size_t ws_bytes, cudaStream_t st,
+             double *ckpt = nullptr, const long *ckpt_off = nullptr, int ckpt_every = 0)
 {
     if (ngrids < 1 || ngrids > K2_MAXG || ninst < 1)
         return DGB_ERR_ARG;
@@ -504,6 +516,9 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     A.nwork = ninst * ngrids;
     A.Lmax = Lmax;
     A.use_delj = settings->use_delj_trick;
+    A.ckpt = ckpt;
+    A.ckpt_off = ckpt_off;
+    A.ckpt_every = ckpt_every > 0 ? ckpt_every : 1;
     if (!ws || ws_bytes < 256)
         return DGB_ERR_WORKSPACE;
     A.counter = (int *)ws;
@@ -655,4 +670,20 @@ extern "C" int dgb_integrate2d_noalloc(double *phi, int L, const double *xx, con
     A.gam_smem = 0;
     A.gam_glob = scratch;
     return dgb::k2_launch(A, 1, bytes, (cudaStream_t)stream);
+}
+
+extern "C" int dgb_batch2d_integrate_ckpt(const int *masks, int ninst, const int *Ls, int ngrids,
+                                          const double *xx_all, const double *phi0_all,
+                                          double *phi_out, const double *table,
+                                          const long *row_off, const int *row_cnt,
+                                          const int *order, const dgb_settings *settings,
+                                          double *ckpt, const long *ckpt_off, int ckpt_every,
+                                          void *ws, size_t ws_bytes, void *stream)
+{
+    if (!Ls || !xx_all || !phi0_all || !phi_out || !table || !row_off || !row_cnt || !order ||
+        !settings || !ckpt || !ckpt_off || ckpt_every < 1)
+        return DGB_ERR_ARG;
+    return dgb::k2_batch(ninst, masks, Ls, ngrids, xx_all, phi0_all, phi_out, table, row_off,
+                         row_cnt, settings->use_old_timestep ? 1 : 0, order, settings, ws,
+                         ws_bytes, (cudaStream_t)stream, ckpt, ckpt_off, ckpt_every);
 }

@@ -172,6 +172,53 @@ int dgb_batch2d_integrate(const int *masks, int ninst, const int *Ls, int ngrids
                           const int *order, const dgb_settings *settings,
                           void *ws, size_t ws_bytes, void *stream);
 
+/* Adjoint (reverse-mode) gradients of the batched 2-population engine with
+ * respect to DGB_AD_NPAR model parameters theta.  dgb_seed2d holds, per
+ * instance, d(T)/dtheta, d(initial_t)/dtheta and d(coefficient)/dtheta for
+ * the a, b, c coefficients of the nine parametric forms of dgb_inst2d in the
+ * order nu[0], nu[1], m12, m21, gamma[0], gamma[1], h[0], h[1], theta0. */
+#define DGB_AD_NPAR 6
+typedef struct {
+    double dT[DGB_AD_NPAR];
+    double dt0[DGB_AD_NPAR];
+    double dform[9][3][DGB_AD_NPAR];
+} dgb_seed2d;
+
+/* Forward-mode pass over the same schedules as dgb_sched2d(fill=1): writes,
+ * for each step, d(q)/dtheta (DGB_AD_NPAR doubles) for q = dt, nu1, nu2, m12,
+ * m21, gamma1, gamma2, h1, h2, theta0 (60 doubles per step) at
+ * drows + row_off[s]*60, following the value walk branch for branch
+ * (dadi/Integration.py:147-176, 355-366).  insts/seeds device arrays. */
+int dgb_sched2d_deriv(const dgb_inst2d *insts, const dgb_seed2d *seeds, int ninst, int ngrids,
+                      const double *dx0s, const dgb_settings *settings, const int *row_cnt,
+                      const long *row_off, double *drows, void *stream);
+
+/* dgb_batch2d_integrate that also stores, for every work item, phi before
+ * every ckpt_every-th step (row-major L*L doubles each) at
+ * ckpt + ckpt_off[work id] -- the checkpoints the adjoint restarts from. */
+int dgb_batch2d_integrate_ckpt(const int *masks, int ninst, const int *Ls, int ngrids,
+                               const double *xx_all, const double *phi0_all, double *phi_out,
+                               const double *table, const long *row_off, const int *row_cnt,
+                               const int *order, const dgb_settings *settings, double *ckpt,
+                               const long *ckpt_off, int ckpt_every, void *ws, size_t ws_bytes,
+                               void *stream);
+
+/* Discrete adjoint of those integrations.  lam (device, phi_out layout) holds
+ * dJ/dphi_final on entry and is overwritten; grad (device, ninst x
+ * DGB_AD_NPAR, zeroed by the caller) receives dJ/dtheta summed over the grids.
+ * Each work item recomputes its checkpoint segments forward and walks them
+ * backwards through the transposed tridiagonal solves.  Scratch per CTA:
+ * dgb_adjoint2d_scratch_bytes; ws = 256 bytes of counter + that scratch for
+ * as many CTAs as it holds.  The delj trick is not supported here
+ * (DGB_ERR_UNSUPPORTED).  The reference has no adjoint; its gradients come
+ * from finite differences (dadi/Godambe.py:131-185). */
+size_t dgb_adjoint2d_scratch_bytes(int Lmax, int ckpt_every, int nblocks);
+int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngrids, const double *xx_all,
+                  const double *table, const double *drows, const long *row_off,
+                  const int *row_cnt, const double *ckpt, const long *ckpt_off, int ckpt_every,
+                  double *lam, double *grad, const int *order, const dgb_settings *settings,
+                  void *ws, size_t ws_bytes, void *stream);
+
 /* Host helper: the number of steps of each schedule, evaluated in C on the
  * host (insts is a HOST array here); the same walk as dgb_sched2d. */
 int dgb_batch2d_count_steps(const dgb_inst2d *insts, int ninst,

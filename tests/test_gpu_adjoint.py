@@ -1,0 +1,113 @@
+"""Discrete-adjoint gradients of the Poisson log-likelihood of extrapolated 2-D
+IM spectra, against finite differences of the same GPU forward and against
+dadi's own Godambe.get_grad on the CPU reference (golden vector).
+
+Central differences with eps = 1e-4 (relative; the step Godambe.get_grad
+uses, dadi/Godambe.py:131-185) carry an O(eps^2) truncation error that, for
+the extrapolated likelihood, reaches ~1e-5 of the gradient's max norm in the
+T component; halving eps divides it by 4.  So the adjoint is held to 1e-6
+(max-norm relative) against the Richardson combination (4 D(eps/2) - D(eps))/3
+of two central differences, and against Godambe.get_grad with that same
+truncation estimate removed.
+"""
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+GRAD_TOL = 1e-6
+PTS = (20, 25, 30)
+NS = (10, 10)
+
+
+def _engine(pts=PTS):
+    from dadi_gb300 import batch
+    return batch.Batch2D(pts, NS)
+
+
+def _ll(eng, params, data, scale):
+    fs, ll, st = eng.run(np.atleast_2d(params), data=data, scale=scale)
+    return ll.cpu().numpy()
+
+
+def _central_fd(eng, p, data, scale, eps):
+    g = np.zeros(6)
+    for k in range(6):
+        h = eps * p[k]
+        pp, pm = p.copy(), p.copy()
+        pp[k] += h
+        pm[k] -= h
+        g[k] = (_ll(eng, pp, data, scale)[0] - _ll(eng, pm, data, scale)[0]) / (2 * h)
+    return g
+
+
+def _fd_pair(eng, p, data, scale, eps=1e-4):
+    d1 = _central_fd(eng, p, data, scale, eps)
+    d2 = _central_fd(eng, p, data, scale, eps / 2)
+    return d1, (4 * d2 - d1) / 3
+
+
+def _close(g, ref):
+    return float(np.max(np.abs(g - ref)) / np.max(np.abs(ref)))
+
+
+def test_adjoint_matches_finite_differences_and_godambe(cuda_lib, golden):
+    g = golden["grad"]
+    p0 = g["grad_p0"]
+    data = g["grad_data"]
+    eng = _engine()
+    ll, grad, st = eng.loglik_and_grad(p0[None, :], data, scale=1e4)
+    assert int(st.abs().sum()) == 0
+    adj = grad.cpu().numpy()[0]
+    fd, rich = _fd_pair(eng, p0, data, 1e4)
+    assert _close(adj, rich) < GRAD_TOL, (adj, rich)
+    # the reference's eps=1e-4 gradient equals ours at the same eps ...
+    assert _close(fd, g["grad_godambe"]) < 1e-7
+    # ... and, with the truncation error estimated from the eps pair removed,
+    # the adjoint
+    godambe_corrected = g["grad_godambe"] + (rich - fd)
+    assert _close(adj, godambe_corrected) < GRAD_TOL, (adj, godambe_corrected)
+
+
+def test_adjoint_single_grid_matches_fd(cuda_lib, golden):
+    g = golden["grad"]
+    eng = _engine((30,))
+    ll, grad, st = eng.loglik_and_grad(g["grad_p0"][None, :], g["grad_data"], scale=1e4)
+    fd, rich = _fd_pair(eng, g["grad_p0"], g["grad_data"], 1e4)
+    assert _close(grad.cpu().numpy()[0], rich) < GRAD_TOL
+    assert _close(grad.cpu().numpy()[0], fd) < GRAD_TOL
+
+
+def test_adjoint_batch_matches_alone(cuda_lib, golden):
+    """Several parameter sets in one adjoint launch give each set's own
+    gradient (within 1e-10: the loss seeds pass through cuBLAS matrix
+    products whose summation order depends on the batch size), and the
+    gradient agrees with finite differences for sets with different step
+    counts."""
+    from dadi_gb300 import batch
+    draws = cases.im_draws(4096)
+    steps = batch.count_steps(batch.im_instances(draws))
+    sel = [i for i in range(64) if 30 <= steps[i] <= 1500][:4]
+    data = golden["grad"]["grad_data"]
+    eng = _engine()
+    ll, grad, st = eng.loglik_and_grad(draws[sel], data, scale=1e4)
+    grad = grad.cpu().numpy()
+    for k, i in enumerate(sel):
+        _, g1, _ = eng.loglik_and_grad(draws[i][None, :], data, scale=1e4)
+        assert _close(grad[k], g1.cpu().numpy()[0]) < 1e-10
+    fd, rich = _fd_pair(eng, draws[sel[0]], data, 1e4)
+    assert _close(grad[0], rich) < GRAD_TOL, (grad[0], rich)
+
+
+def test_autograd_function(cuda_lib, golden):
+    import torch
+    from dadi_gb300 import batch
+    g = golden["grad"]
+    eng = _engine()
+    p = torch.tensor(g["grad_p0"][None, :], dtype=torch.float64, requires_grad=True)
+    ll = batch.IMLogLik.apply(eng, p, g["grad_data"], 1e4)
+    ll.sum().backward()
+    _, direct, _ = eng.loglik_and_grad(g["grad_p0"][None, :], g["grad_data"], scale=1e4)
+    assert _close(p.grad.numpy()[0], direct.cpu().numpy()[0]) < 1e-12
