@@ -29,7 +29,8 @@ EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
            "dgb_integrate_table", "dgb_integrate_precalc", "dgb_sched2d",
            "dgb_batch2d_integrate", "dgb_batch2d_count_steps", "dgb_probe_fp64_fma",
            "dgb_probe_rcp", "dgb_integrate2d_noalloc", "dgb_sched2d_deriv",
-           "dgb_batch2d_integrate_ckpt", "dgb_adjoint2d_scratch_bytes", "dgb_adjoint2d"]
+           "dgb_batch2d_integrate_ckpt", "dgb_adjoint2d_scratch_bytes", "dgb_adjoint2d",
+           "dgb_items2d_integrate", "dgb_sched2d_host"]
 
 
 class PForm(ctypes.Structure):
@@ -89,6 +90,9 @@ def _declare(L):
                                            _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(Settings),
                                            _vp, _vp, i, _vp, sz, _vp]),
         "dgb_adjoint2d_scratch_bytes": (sz, [i, i, i]),
+        "dgb_items2d_integrate": (i, [_vp, i, i, _vp, _vp, _vp, _vp, _vp, _vp,
+                                      ctypes.POINTER(Settings), _vp, sz, _vp]),
+        "dgb_sched2d_host": (i, [_vp, i, ctypes.POINTER(Settings), lg, d, _vp, _vp, _vp, _vp]),
         "dgb_adjoint2d": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp, _vp,
                               _vp, _vp, i, _vp, _vp, _vp, ctypes.POINTER(Settings), _vp, sz,
                               _vp]),

@@ -665,8 +665,7 @@ extern "C" int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngr
     nblocks = std::min<long>(nblocks, A.nwork);
     A.scratch = (double *)((char *)ws + 256);
     size_t smem = (size_t)26 * Lmax * sizeof(double);
-    if (cudaFuncSetAttribute(k_adjoint2d, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess)
+    if (raise_smem_limit(k_adjoint2d))
         return DGB_ERR_CUDA;
     if (cudaMemsetAsync(A.counter, 0, sizeof(int), (cudaStream_t)stream) != cudaSuccess)
         return DGB_ERR_CUDA;

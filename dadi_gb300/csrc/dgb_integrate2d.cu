@@ -59,6 +59,7 @@ struct K2Args {
     double *ckpt;          // optional: phi before every ckpt_every-th step
     const long *ckpt_off;  // first checkpoint double of each work id
     int ckpt_every;
+    const dgb_item2d *items; // optional explicit work items (grid, slot, schedule each)
 };
 
 __host__ __device__ inline int odd_pitch(int L) { return (L % 2) ? L : L + 1; }
@@ -164,17 +165,34 @@ __global__ void __launch_bounds__(K2_THREADS) k_integrate2d(K2Args A)
         if (w >= A.nwork)
             break;
         const int wid = A.order ? A.order[w] : w;
-        const int inst = wid / A.ngrids;
-        const int gi = wid - inst * A.ngrids;
-        const int L = A.L[gi];
-        const double *xx = A.xx_all + A.xx_off[gi];
-        double *out = A.phi_out + A.out_off[gi] + (size_t)inst * L * L;
-        const double *src = A.phi0_all ? A.phi0_all + A.phi0_off[gi] : out;
-        const int sidx = A.sched_per_grid ? wid : inst;
+        int inst, L, sidx, frozen, nomut;
+        const double *xx, *src;
+        double *out;
+        if (A.items) {
+            // explicit item: its own grid, output slot (holding the initial
+            // density) and schedule
+            const dgb_item2d &it = A.items[wid];
+            inst = wid;
+            L = it.L;
+            xx = A.xx_all + it.xx_off;
+            out = A.phi_out + it.out_off;
+            src = out;
+            sidx = (int)it.sched;
+            frozen = it.masks & 0xff;
+            nomut = it.masks >> 8 & 0xff;
+        } else {
+            inst = wid / A.ngrids;
+            const int gi = wid - inst * A.ngrids;
+            L = A.L[gi];
+            xx = A.xx_all + A.xx_off[gi];
+            out = A.phi_out + A.out_off[gi] + (size_t)inst * L * L;
+            src = A.phi0_all ? A.phi0_all + A.phi0_off[gi] : out;
+            sidx = A.sched_per_grid ? wid : inst;
+            frozen = A.masks ? (A.masks[inst] & 0xff) : A.frozen_mask;
+            nomut = A.masks ? (A.masks[inst] >> 8 & 0xff) : A.nomut_mask;
+        }
         const double *rows = A.row_off ? A.table + A.row_off[sidx] * K2_ROW : A.table;
         const int nsteps = A.row_off ? A.row_cnt[sidx] : A.fixed_cnt;
-        const int frozen = A.masks ? (A.masks[inst] & 0xff) : A.frozen_mask;
-        const int nomut = A.masks ? (A.masks[inst] >> 8 & 0xff) : A.nomut_mask;
 
         // grid constants and initial density
         for (int i = tid; i < L; i += blockDim.x) {
@@ -390,17 +408,12 @@ int k2_smem_fits(int Lmax, bool gam_smem, bool delj, size_t *bytes)
 
 static int k2_launch(K2Args &A, int nblocks, size_t smem, cudaStream_t st)
 {
-    cudaError_t e;
     if (A.use_delj) {
-        e = cudaFuncSetAttribute(k_integrate2d<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem);
-        if (e != cudaSuccess)
+        if (raise_smem_limit(k_integrate2d<true>))
             return DGB_ERR_CUDA;
         k_integrate2d<true><<<nblocks, K2_THREADS, smem, st>>>(A);
     } else {
-        e = cudaFuncSetAttribute(k_integrate2d<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem);
-        if (e != cudaSuccess)
+        if (raise_smem_limit(k_integrate2d<false>))
             return DGB_ERR_CUDA;
         k_integrate2d<false><<<nblocks, K2_THREADS, smem, st>>>(A);
     }
@@ -413,18 +426,14 @@ static int k2_launch(K2Args &A, int nblocks, size_t smem, cudaStream_t st)
 // the previous launch.
 static int k2_occupancy(bool delj, size_t smem)
 {
-    int dev = 0, optin = 0, nb = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    int nb = 0;
     cudaError_t e;
     if (delj) {
-        cudaFuncSetAttribute(k_integrate2d<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             optin);
+        raise_smem_limit(k_integrate2d<true>);
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate2d<true>, K2_THREADS,
                                                           smem);
     } else {
-        cudaFuncSetAttribute(k_integrate2d<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             optin);
+        raise_smem_limit(k_integrate2d<false>);
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate2d<false>, K2_THREADS,
                                                           smem);
     }
@@ -686,4 +695,76 @@ extern "C" int dgb_batch2d_integrate_ckpt(const int *masks, int ninst, const int
     return dgb::k2_batch(ninst, masks, Ls, ngrids, xx_all, phi0_all, phi_out, table, row_off,
                          row_cnt, settings->use_old_timestep ? 1 : 0, order, settings, ws,
                          ws_bytes, (cudaStream_t)stream, ckpt, ckpt_off, ckpt_every);
+}
+
+extern "C" int dgb_items2d_integrate(const dgb_item2d *items, int nitems, int Lmax,
+                                     const double *xx_all, double *phi_out, const double *table,
+                                     const long *row_off, const int *row_cnt, const int *order,
+                                     const dgb_settings *settings, void *ws, size_t ws_bytes,
+                                     void *stream)
+{
+    using namespace dgb;
+    if (!items || nitems < 1 || Lmax < 3 || !xx_all || !phi_out || !table || !row_off ||
+        !row_cnt || !settings)
+        return DGB_ERR_ARG;
+    K2Args A = {};
+    A.ngrids = 1;
+    A.L[0] = Lmax;
+    A.xx_all = xx_all;
+    A.phi_out = phi_out;
+    A.table = table;
+    A.row_off = row_off;
+    A.row_cnt = row_cnt;
+    A.order = order;
+    A.nwork = nitems;
+    A.Lmax = Lmax;
+    A.use_delj = settings->use_delj_trick;
+    A.items = items;
+    if (!ws || ws_bytes < 256)
+        return DGB_ERR_WORKSPACE;
+    A.counter = (int *)ws;
+    size_t bytes_s = 0, bytes_g = 0;
+    bool fit_s = k2_smem_fits(Lmax, true, A.use_delj, &bytes_s);
+    if (!k2_smem_fits(Lmax, false, A.use_delj, &bytes_g))
+        return DGB_ERR_UNSUPPORTED;
+    int nsm = k2_num_sms();
+    int nblocks;
+    size_t smem;
+    if (fit_s) {
+        A.gam_smem = 1;
+        nblocks = nsm * k2_occupancy(A.use_delj, bytes_s + sizeof(K2Shared));
+        smem = bytes_s;
+    } else {
+        A.gam_smem = 0;
+        size_t slice = (size_t)Lmax * Lmax * sizeof(double);
+        nblocks = (int)std::min<size_t>((ws_bytes - 256) / slice,
+                                        (size_t)nsm * k2_occupancy(A.use_delj, bytes_g + 256));
+        A.gam_glob = (double *)((char *)ws + 256);
+        smem = bytes_g;
+    }
+    if (nblocks < 1)
+        return DGB_ERR_WORKSPACE;
+    nblocks = std::min(nblocks, nitems);
+    if (cudaMemsetAsync(A.counter, 0, sizeof(int), (cudaStream_t)stream) != cudaSuccess)
+        return DGB_ERR_CUDA;
+    return k2_launch(A, nblocks, smem, (cudaStream_t)stream);
+}
+
+extern "C" int dgb_sched2d_host(const dgb_inst2d *insts, int ninst,
+                                const dgb_settings *settings, long max_steps, double dx0,
+                                int *row_cnt, const long *row_off, double *table, int *status)
+{
+    if (!insts || ninst < 0 || !settings || max_steps < 1 || (!table && !row_cnt) ||
+        (table && (!row_off || !status)))
+        return DGB_ERR_ARG;
+    for (int n = 0; n < ninst; n++) {
+        int err = 0;
+        long c = dgb::sched2d_walk(insts[n], *settings, dx0, max_steps,
+                                   table ? table + row_off[n] * dgb::K2_ROW : nullptr, &err);
+        if (!table)
+            row_cnt[n] = (int)c;
+        else
+            status[n] |= err;
+    }
+    return DGB_OK;
 }

@@ -380,17 +380,14 @@ static int nd_launch_sweep(NDArgs &A, bool delj, cudaStream_t st)
     size_t smem = nd_smem_doubles(A.L, nt, delj) * sizeof(double);
     long nblocks = (A.nlines + nt - 1) / nt;
     cudaError_t e;
+    (void)e;
     if (delj) {
-        e = cudaFuncSetAttribute(k_sweep_nd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem);
-        if (e != cudaSuccess)
-            return DGB_ERR_UNSUPPORTED;
+        if (raise_smem_limit(k_sweep_nd<true>))
+            return DGB_ERR_CUDA;
         k_sweep_nd<true><<<(unsigned)nblocks, nt, smem, st>>>(A);
     } else {
-        e = cudaFuncSetAttribute(k_sweep_nd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem);
-        if (e != cudaSuccess)
-            return DGB_ERR_UNSUPPORTED;
+        if (raise_smem_limit(k_sweep_nd<false>))
+            return DGB_ERR_CUDA;
         k_sweep_nd<false><<<(unsigned)nblocks, nt, smem, st>>>(A);
     }
     return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
@@ -401,9 +398,8 @@ static int nd_launch_precalc(NDArgs &A, cudaStream_t st)
     int nt = nd_threads(A.L, A.nlines);
     size_t smem = ((size_t)A.L * (nt + 1) + (size_t)A.L * nt) * sizeof(double);
     long nblocks = (A.nlines + nt - 1) / nt;
-    if (cudaFuncSetAttribute(k_precalc_nd, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess)
-        return DGB_ERR_UNSUPPORTED;
+    if (raise_smem_limit(k_precalc_nd))
+        return DGB_ERR_CUDA;
     k_precalc_nd<<<(unsigned)nblocks, nt, smem, st>>>(A);
     return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
 }

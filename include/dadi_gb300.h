@@ -219,6 +219,37 @@ int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngrids, const 
                   double *lam, double *grad, const int *order, const dgb_settings *settings,
                   void *ws, size_t ws_bytes, void *stream);
 
+/* One work item of dgb_items2d_integrate: a 2-D integration on grid
+ * xx_all[xx_off .. xx_off+L) whose density sits at phi_out + out_off (initial
+ * density on entry, result on exit), driven by schedule `sched` (index into
+ * row_off / row_cnt), with masks = frozen_mask | nomut_mask << 8. */
+typedef struct {
+    int L;
+    int masks;
+    long xx_off;
+    long out_off;
+    long sched;
+} dgb_item2d;
+
+/* The batched 2-D integration over an explicit list of work items, so one
+ * persistent launch mixes grids of different sizes and integrations of
+ * different requests (the serving engine's continuous batches).  Lmax bounds
+ * every item's L; order (device, optional) gives the start order; ws as for
+ * dgb_batch2d_integrate with Lmax. */
+int dgb_items2d_integrate(const dgb_item2d *items, int nitems, int Lmax, const double *xx_all,
+                          double *phi_out, const double *table, const long *row_off,
+                          const int *row_cnt, const int *order, const dgb_settings *settings,
+                          void *ws, size_t ws_bytes, void *stream);
+
+/* dgb_sched2d evaluated in C on the host (all arrays HOST): table == NULL
+ * counts rows into row_cnt; otherwise writes the rows at table +
+ * row_off[i]*11 and ORs status bits into status[i].  One schedule per
+ * instance on a grid with first spacing dx0.  For callers that must not wait
+ * on the device (the serving loop forms batches while kernels run). */
+int dgb_sched2d_host(const dgb_inst2d *insts, int ninst, const dgb_settings *settings,
+                     long max_steps, double dx0, int *row_cnt, const long *row_off,
+                     double *table, int *status);
+
 /* Host helper: the number of steps of each schedule, evaluated in C on the
  * host (insts is a HOST array here); the same walk as dgb_sched2d. */
 int dgb_batch2d_count_steps(const dgb_inst2d *insts, int ninst,
