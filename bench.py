@@ -10,12 +10,15 @@ engine over the whole 4096-instance batch.  Synthetic data stands in for an
 observed spectrum (none is used by the reference's benchmark).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--serve R] [--adjoint]
 
 `value` times the engine with the parameters already on the device; `e2e`
 times the public API call (host parameter and data arrays in, host spectra and
 likelihoods out).  --impl reference times the CPU integrator restatement
 (the reference's algorithm: Python time loop over C sweeps) on all host
 cores over a bounded sample and scales it to the workload by point-sweeps.
+`serving` reports p50/p99 latency and spectra/s of a served mixed request
+stream; `adjoint` (with --adjoint) the time of 256 likelihood gradients.
 """
 import argparse
 import json
@@ -26,6 +29,10 @@ import threading
 import time
 
 import numpy as np
+
+# the serving leg keeps ~26 streams busy at once: give each its own hardware
+# queue (must be set before CUDA starts)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -231,7 +238,6 @@ def run_ours(a, world, rank, local):
     torch.cuda.set_device(local)
     from dadi_gb300 import batch, build
     build.build()
-    from oracle import numerics as onum  # noqa: F401  (checker only: cpu_baseline leg)
     draws = im_draws(NINST, rank)
     rec = batch.im_instances(draws)
     steps = batch.count_steps(rec)   # host walk of the same schedules: point-sweep count
@@ -245,10 +251,10 @@ def run_ours(a, world, rank, local):
     def step_device():
         # one pass of the engine over the batch with the parameters prepared
         # on the device side of the API: device schedules, the integration,
-        # from_phi, extrapolation and the likelihood all run on the GPU
+        # and the epilogue (from_phi, extrapolation, likelihood) all run on
+        # the GPU, in 5 launches
         phis, status = eng.integrate(rec)
-        fs = eng.extrapolate(eng.spectra(phis))
-        ll = eng.loglik(fs, d_obs, 5e4)
+        fs, ll = eng.spectra_ll(phis, d_obs, 5e4)
         return fs, ll, status
 
     # warm-up
@@ -279,8 +285,7 @@ def run_ours(a, world, rank, local):
         k1 = torch.cuda.Event(enable_timing=True)
         t_start.record()
         phis, status = eng.integrate(rec, timer=(k0, k1))
-        fs = eng.extrapolate(eng.spectra(phis))
-        ll = eng.loglik(fs, d_obs, 5e4)
+        fs, ll = eng.spectra_ll(phis, d_obs, 5e4)
         t_end.record()
         torch.cuda.synchronize()
         total_ms += t_start.elapsed_time(t_end)
@@ -335,6 +340,9 @@ def run_ours(a, world, rank, local):
                          "scaled to the 4096-instance workload by point-sweeps"
                          % (n, sps, cores, wall)}
 
+    serve = run_serving(a, obs) if (rank == 0 and a.serve > 0) else None
+    adjoint = run_adjoint(a, obs) if (rank == 0 and a.adjoint) else None
+
     if rank != 0:
         return 0
     from dadi_gb300 import _lib as glib
@@ -382,14 +390,79 @@ def run_ours(a, world, rank, local):
         "kernel_ms_per_step": kmean * 1e3,
         "warmup_ms": warm_ms,
         "clocks": clk,
-        "gpu_launches": 3 * a.steps,  # per step: 2 schedule passes + 1 integration
+        "gpu_launches": 5 * a.steps,  # per step: 2 schedule passes, the integration, 2 epilogue
         "failed_instances": bad,
         "plain": plain,
         "batched_over_plain": (value / plain["value"]) if plain else None,
         "cpu_baseline": cpu,
+        "serving": serve,
+        "adjoint": adjoint,
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def run_serving(a, obs):
+    """The serving workload: a seeded Poisson request stream (mean `rate`
+    requests/s; 70% 2-D IM at pts base 40..100 with pts_l base, +10, +20 and
+    ns (20,20) or (40,40); 20% DFE cache entries, IM with selection on the
+    50-point gamma grid over [-2000, -1e-4]; 8% 3-D growth model at pts
+    60..90; 2% four populations at pts 30..40; 10% of the IM requests with
+    ns (40,40) also want gradients) served with continuous batching.  Latency
+    is completion minus arrival, on the host clock."""
+    from dadi_gb300 import serving
+    srv = serving.Server(hbm_budget=a.serve_budget << 30)
+    srv.prepare(range(40, 121), [(20, 20), (40, 40)])
+    # warm-up stream: library handles, worker engines
+    srv.run(serving.config5_stream(max(8, a.serve // 20), seed=1, rate=a.serve_rate,
+                                   obs=obs))
+    reqs = serving.config5_stream(a.serve, seed=0, rate=a.serve_rate, obs=obs)
+    out = srv.run(reqs)
+    summ = serving.latency_summary(out)
+    by = {}
+    for kind in ("im", "im_sel", "growth3", "four"):
+        lat = [r.latency for r in out if r.kind == kind and not r.want_grad and r.error is None]
+        if lat:
+            by[kind] = {"n": len(lat), "p50_s": float(np.percentile(lat, 50)),
+                        "p99_s": float(np.percentile(lat, 99))}
+    lat = [r.latency for r in out if r.want_grad and r.error is None]
+    if lat:
+        by["im_grad"] = {"n": len(lat), "p50_s": float(np.percentile(lat, 50)),
+                         "p99_s": float(np.percentile(lat, 99))}
+    summ.update({"arrival_rate_per_s": a.serve_rate, "arrival_span_s": float(out[-1].arrival),
+                 "hbm_budget_gib": a.serve_budget, "by_class": by,
+                 "failed_status": sum(1 for r in out if r.status)})
+    return summ
+
+
+def run_adjoint(a, obs):
+    """Gradients of the Poisson log-likelihood for the first 256 seed-0 IM
+    parameter sets at pts [100,110,120], ns (40,40): forward with
+    checkpoints, from_phi/extrapolation/likelihood backward through torch,
+    and the discrete adjoint; CUDA-event timed."""
+    import torch
+    from dadi_gb300 import batch
+    draws = im_draws(256, 0)
+    eng = batch.Batch2D((100, 110, 120), NS)
+    d_obs = torch.from_numpy(obs).cuda()
+    eng.loglik_and_grad(draws[:4], d_obs, scale=5e4)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e2 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    ll, ctx = eng.forward_for_adjoint(draws, d_obs, scale=5e4)
+    e1.record()
+    grad = eng.adjoint(ctx, torch.ones_like(ll))
+    e2.record()
+    torch.cuda.synchronize()
+    fwd = e0.elapsed_time(e1) / 1e3
+    adj = e1.elapsed_time(e2) / 1e3
+    return {"sets": 256, "pts_l": [100, 110, 120], "ns": list(NS),
+            "checkpoint_every": ctx["C"], "forward_s": fwd, "adjoint_s": adj,
+            "gradients_per_s": 256 / (fwd + adj),
+            "failed_instances": int((ctx["status"] != 0).sum()),
+            "finite": bool(torch.isfinite(grad).all())}
 
 
 def run_profile_case(a):
@@ -427,6 +500,12 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--clock-ms", type=int, default=500,
                     help="nvidia-smi sampling period during the timed region (0: off)")
+    ap.add_argument("--serve", type=int, default=600,
+                    help="requests in the served stream (0: skip serving)")
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-budget", type=int, default=32, help="GiB the server may hold")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="also time 256 IM gradients at pts [100,110,120]")
     ap.add_argument("--profile-items", type=int, default=0,
                     help="run only a small batch (this many seed-0 instances with 200-800 "
                          "steps, twice) for profiler captures, then exit")

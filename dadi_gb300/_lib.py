@@ -6,6 +6,7 @@ the compiled library and a CUDA device and raises otherwise.
 """
 import ctypes
 import os
+import threading
 
 import numpy as np
 
@@ -30,7 +31,8 @@ EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
            "dgb_batch2d_integrate", "dgb_batch2d_count_steps", "dgb_probe_fp64_fma",
            "dgb_probe_rcp", "dgb_integrate2d_noalloc", "dgb_sched2d_deriv",
            "dgb_batch2d_integrate_ckpt", "dgb_adjoint2d_scratch_bytes", "dgb_adjoint2d",
-           "dgb_items2d_integrate", "dgb_sched2d_host"]
+           "dgb_items2d_integrate", "dgb_sched2d_host", "dgb_from_phi2d_smem_bytes",
+           "dgb_from_phi2d", "dgb_extrap_ll"]
 
 
 class PForm(ctypes.Structure):
@@ -91,8 +93,11 @@ def _declare(L):
                                            _vp, _vp, i, _vp, sz, _vp]),
         "dgb_adjoint2d_scratch_bytes": (sz, [i, i, i]),
         "dgb_items2d_integrate": (i, [_vp, i, i, _vp, _vp, _vp, _vp, _vp, _vp,
-                                      ctypes.POINTER(Settings), _vp, sz, _vp]),
+                                      ctypes.POINTER(Settings), i, _vp, sz, _vp]),
         "dgb_sched2d_host": (i, [_vp, i, ctypes.POINTER(Settings), lg, d, _vp, _vp, _vp, _vp]),
+        "dgb_from_phi2d_smem_bytes": (sz, [i, i]),
+        "dgb_from_phi2d": (i, [_vp, i, i, i, _vp]),
+        "dgb_extrap_ll": (i, [_vp, i, d, _vp]),
         "dgb_adjoint2d": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp, _vp,
                               _vp, _vp, i, _vp, _vp, _vp, ctypes.POINTER(Settings), _vp, sz,
                               _vp]),
@@ -151,8 +156,43 @@ def dptr(t):
 
 
 def to_device(torch, arr, dtype=None):
+    """Host array -> device tensor, staged through pinned memory and copied
+    asynchronously on the current stream.  (A copy from pageable memory is
+    synchronous and, in the driver, serialises with every other thread's
+    pageable copies, so one thread waiting for its stream would stall the
+    others.)"""
     a = np.ascontiguousarray(arr, dtype=dtype if dtype is not None else np.float64)
-    return torch.from_numpy(a).to("cuda", non_blocking=False)
+    return torch.from_numpy(a).pin_memory().to("cuda", non_blocking=True)
+
+
+def to_host(torch, t):
+    """Device tensor -> numpy array: copied into pinned memory on the
+    current stream, which alone is then synchronised."""
+    out = torch.empty(tuple(t.shape), dtype=t.dtype, pin_memory=True)
+    out.copy_(t, non_blocking=True)
+    torch.cuda.current_stream().synchronize()
+    return out.numpy()
+
+
+_upload_streams = {}
+_upload_lock = threading.Lock()
+
+
+def upload_resident(torch, arr, dtype=None):
+    """Host array -> device tensor that is complete on return and may be
+    read from any stream: copied on a private stream that is synchronised
+    alone, so the call never waits for work queued on the caller's streams.
+    For long-lived constants (grids, tables, initial densities)."""
+    a = np.ascontiguousarray(arr, dtype=dtype if dtype is not None else np.float64)
+    dev = torch.cuda.current_device()
+    with _upload_lock:
+        s = _upload_streams.get(dev)
+        if s is None:
+            s = _upload_streams[dev] = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            t = torch.from_numpy(a).pin_memory().to("cuda", non_blocking=True)
+        s.synchronize()
+    return t
 
 
 def workspace(torch, nbytes):

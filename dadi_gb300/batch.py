@@ -17,7 +17,7 @@ import ctypes
 
 import numpy as np
 
-from . import _lib, integration, numerics, phimanip, spectrum
+from . import _lib, epilogue, integration, numerics, phimanip, spectrum
 
 INST_DTYPE = np.dtype({
     "names": ["T", "initial_t", "nu", "m12", "m21", "gamma", "h", "theta0", "frozen", "nomut"],
@@ -149,7 +149,7 @@ class Batch2D:
                                    self.max_steps, 0, _lib.dptr(cnt), None, None, None, sh),
                    "dgb_sched2d(count)")
         ends = torch.cumsum(cnt.to(torch.int64), 0)
-        total = int(ends[-1].item())
+        total = int(_lib.to_host(torch, ends[-1:])[0])
         off = (ends - cnt.to(torch.int64)).contiguous()
         table = torch.empty(max(total, 1) * 11, dtype=torch.float64, device="cuda")
         status = torch.zeros(n, dtype=torch.int32, device="cuda")
@@ -169,7 +169,7 @@ class Batch2D:
         ng = len(self.pts_l)
         st = settings_from_globals(self.gam_placement)
         rec = np.ascontiguousarray(rec)
-        d_rec = torch.from_numpy(rec.view(np.uint8)).to("cuda")
+        d_rec = _lib.to_device(torch, rec.view(np.uint8), np.uint8)
         table, off, cnt, status = self.schedule(d_rec, n)
         Lsq = torch.tensor([L * L for L in self.pts_l], dtype=torch.int64, device="cuda")
         if order is None:
@@ -177,9 +177,9 @@ class Batch2D:
             cost = (steps * Lsq[None, :]).reshape(-1)
             d_order = torch.argsort(-cost, stable=True).to(torch.int32)
         else:
-            d_order = torch.from_numpy(np.ascontiguousarray(order, dtype=np.int32)).to("cuda")
+            d_order = _lib.to_device(torch, order, np.int32)
         masks = (rec["frozen"].astype(np.int32) & 0xff) | ((rec["nomut"].astype(np.int32) & 0xff) << 8)
-        d_masks = torch.from_numpy(np.ascontiguousarray(masks)).to("cuda")
+        d_masks = _lib.to_device(torch, masks, np.int32)
         total = sum(n * L * L for L in self.pts_l)
         d_out = torch.empty(total, dtype=torch.float64, device="cuda")
         nws = _lib.lib().dgb_workspace_bytes(1, 2, max(self.pts_l), n * ng)
@@ -209,10 +209,13 @@ class Batch2D:
         return ll.detach(), grad, ctx["status"]
 
     def forward_for_adjoint(self, params, data, scale=1.0, ckpt_every=None, seeds=None,
-                            rec=None):
+                            rec=None, tail_per_set=False):
         """Forward pass that keeps what the adjoint needs: schedules,
         derivative rows, checkpoints and the differentiable tail (from_phi,
-        extrapolation, likelihood) as a torch graph."""
+        extrapolation, likelihood) as a torch graph.  tail_per_set evaluates
+        the tail one parameter set at a time, so each set's spectrum,
+        likelihood and gradient are bitwise independent of the other sets in
+        the batch (batched matrix products may order sums by batch size)."""
         torch = self.torch
         lib = _lib.lib()
         if rec is None:
@@ -224,10 +227,10 @@ class Batch2D:
         if st.use_delj_trick:
             raise NotImplementedError("the adjoint does not support the delj trick")
         sh = _lib.stream_handle(torch)
-        d_rec = torch.from_numpy(rec.view(np.uint8)).to("cuda")
+        d_rec = _lib.to_device(torch, rec.view(np.uint8), np.uint8)
         table, off, cnt, status = self.schedule(d_rec, n)
         seeds = im_seeds(n) if seeds is None else np.ascontiguousarray(seeds)
-        d_seed = torch.from_numpy(seeds.view(np.uint8)).to("cuda")
+        d_seed = _lib.to_device(torch, seeds.view(np.uint8), np.uint8)
         drows = torch.empty(max(int(table.numel() // 11), 1) * 60, dtype=torch.float64,
                             device="cuda")
         _lib.check(lib.dgb_sched2d_deriv(_lib.dptr(d_rec), _lib.dptr(d_seed), n, ng,
@@ -237,14 +240,15 @@ class Batch2D:
         Lsq = torch.tensor([L * L for L in self.pts_l], dtype=torch.int64, device="cuda")
         cost = (steps * Lsq[None, :]).reshape(-1)
         d_order = torch.argsort(-cost, stable=True).to(torch.int32)
-        smax = int(steps.max().item())
+        smax = int(_lib.to_host(torch, steps.max().reshape(1))[0])
         C = int(ckpt_every) if ckpt_every else max(8, min(256, int(np.ceil(np.sqrt(max(smax, 1))))))
         per_item = ((steps + C - 1) // C).expand(n, ng) * Lsq[None, :]
         ends = torch.cumsum(per_item.reshape(-1), 0)
         ck_off = (ends - per_item.reshape(-1)).contiguous()
-        ckpt = torch.empty(max(int(ends[-1].item()), 1), dtype=torch.float64, device="cuda")
+        ckpt = torch.empty(max(int(_lib.to_host(torch, ends[-1:])[0]), 1), dtype=torch.float64,
+                           device="cuda")
         masks = (rec["frozen"].astype(np.int32) & 0xff) | ((rec["nomut"].astype(np.int32) & 0xff) << 8)
-        d_masks = torch.from_numpy(np.ascontiguousarray(masks)).to("cuda")
+        d_masks = _lib.to_device(torch, masks, np.int32)
         total = sum(n * L * L for L in self.pts_l)
         d_out = torch.empty(total, dtype=torch.float64, device="cuda")
         nws = lib.dgb_workspace_bytes(1, 2, max(self.pts_l), n * ng)
@@ -260,9 +264,18 @@ class Batch2D:
             o += n * L * L
         d = data if torch.is_tensor(data) else _lib.to_device(torch, data)
         with torch.enable_grad():
-            fs = self.extrapolate(self.spectra(phis))
-            ll = self.loglik(fs, d, scale)
-        ctx = dict(phis=phis, ll=ll, table=table, off=off, cnt=cnt, drows=drows, ckpt=ckpt,
+            if tail_per_set:
+                fss, lls = [], []
+                for i in range(n):
+                    fs_i = self.extrapolate(self.spectra([p[i:i + 1] for p in phis]))
+                    fss.append(fs_i)
+                    lls.append(self.loglik(fs_i, d, scale))
+                fs = torch.cat(fss)
+                ll = torch.cat(lls)
+            else:
+                fs = self.extrapolate(self.spectra(phis))
+                ll = self.loglik(fs, d, scale)
+        ctx = dict(phis=phis, ll=ll, fs=fs.detach(), table=table, off=off, cnt=cnt, drows=drows, ckpt=ckpt,
                    ck_off=ck_off, C=C, masks=d_masks, order=d_order, status=status, n=n, st=st)
         return ll, ctx
 
@@ -276,7 +289,7 @@ class Batch2D:
                          for l, p in zip(lams, phis)]).contiguous()
         n = ctx["n"]
         ng = len(self.pts_l)
-        grad = torch.zeros(n, 6, dtype=torch.float64, device="cuda")
+        part = torch.empty(n, ng, 6, dtype=torch.float64, device="cuda")
         C = ctx["C"]
         Lmax = max(self.pts_l)
         per_cta = lib.dgb_adjoint2d_scratch_bytes(Lmax, C, 1)
@@ -286,9 +299,12 @@ class Batch2D:
         _lib.check(lib.dgb_adjoint2d(
             _lib.dptr(ctx["masks"]), n, self.Ls, ng, _lib.dptr(self.d_xx), _lib.dptr(ctx["table"]),
             _lib.dptr(ctx["drows"]), _lib.dptr(ctx["off"]), _lib.dptr(ctx["cnt"]),
-            _lib.dptr(ctx["ckpt"]), _lib.dptr(ctx["ck_off"]), C, _lib.dptr(lam), _lib.dptr(grad),
+            _lib.dptr(ctx["ckpt"]), _lib.dptr(ctx["ck_off"]), C, _lib.dptr(lam), _lib.dptr(part),
             _lib.dptr(ctx["order"]), ctypes.byref(st), _lib.dptr(ws), nws,
             _lib.stream_handle(torch)), "dgb_adjoint2d")
+        grad = part[:, 0].clone()
+        for gi in range(1, ng):
+            grad += part[:, gi]
         return grad
 
     def spectra(self, phis):
@@ -322,13 +338,24 @@ class Batch2D:
             - torch.lgamma(d + 1.0)
         return torch.where(ok, term, torch.zeros_like(term)).sum(dim=(1, 2))
 
+    def spectra_ll(self, phis, data=None, scale=1.0):
+        """The device epilogue (dgb_from_phi2d + dgb_extrap_ll, two launches
+        for the whole batch): extrapolated spectra (n, n1+1, n2+1) and, with
+        data, Poisson log-likelihoods (n,); CUDA tensors."""
+        torch = self.torch
+        d = None
+        if data is not None:
+            d = data if torch.is_tensor(data) else _lib.to_device(torch, data)
+            d = d.to(torch.float64).contiguous()
+        return epilogue.spectra_2d_batch(torch, [p.contiguous() for p in phis], self.xxs,
+                                         self.ns, d, scale)
+
     def run(self, params, data=None, scale=1.0):
         """IM parameter rows -> (extrapolated spectra (n, n1+1, n2+1), ll or
         None, status), all CUDA tensors."""
         rec = im_instances(params)
         phis, status = self.integrate(rec)
-        fs = self.extrapolate(self.spectra(phis))
-        ll = self.loglik(fs, data, scale) if data is not None else None
+        fs, ll = self.spectra_ll(phis, data, scale)
         return fs, ll, status
 
 

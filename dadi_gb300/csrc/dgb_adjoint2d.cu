@@ -568,7 +568,7 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
                 __syncthreads();
             }
         }
-        // block reduction of acc into grad[inst]
+        // block reduction of acc into this work item's row of grad
 #pragma unroll
         for (int p = 0; p < NPAR; p++) {
             double v = acc[p];
@@ -582,7 +582,7 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
             double v = 0;
             for (int wv = 0; wv < (int)(blockDim.x >> 5); wv++)
                 v += red[wv][tid];
-            atomicAdd(A.grad + (size_t)inst * NPAR + tid, v);
+            A.grad[((size_t)inst * A.ngrids + gi) * NPAR + tid] = v;
         }
         __syncthreads();
     }

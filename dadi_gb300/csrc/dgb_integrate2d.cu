@@ -700,8 +700,8 @@ extern "C" int dgb_batch2d_integrate_ckpt(const int *masks, int ninst, const int
 extern "C" int dgb_items2d_integrate(const dgb_item2d *items, int nitems, int Lmax,
                                      const double *xx_all, double *phi_out, const double *table,
                                      const long *row_off, const int *row_cnt, const int *order,
-                                     const dgb_settings *settings, void *ws, size_t ws_bytes,
-                                     void *stream)
+                                     const dgb_settings *settings, int one_per_cta, void *ws,
+                                     size_t ws_bytes, void *stream)
 {
     using namespace dgb;
     if (!items || nitems < 1 || Lmax < 3 || !xx_all || !phi_out || !table || !row_off ||
@@ -730,13 +730,26 @@ extern "C" int dgb_items2d_integrate(const dgb_item2d *items, int nitems, int Lm
     int nsm = k2_num_sms();
     int nblocks;
     size_t smem;
+    size_t slice = (size_t)Lmax * Lmax * sizeof(double);
+    if (one_per_cta) {
+        // CTA b integrates item order[b] (or b) and retires: no queue
+        A.counter = nullptr;
+        nblocks = nitems;
+        A.gam_smem = fit_s ? 1 : 0;
+        smem = fit_s ? bytes_s : bytes_g;
+        if (!fit_s) {
+            if ((ws_bytes - 256) / slice < (size_t)nitems)
+                return DGB_ERR_WORKSPACE;
+            A.gam_glob = (double *)((char *)ws + 256);
+        }
+        return k2_launch(A, nblocks, smem, (cudaStream_t)stream);
+    }
     if (fit_s) {
         A.gam_smem = 1;
         nblocks = nsm * k2_occupancy(A.use_delj, bytes_s + sizeof(K2Shared));
         smem = bytes_s;
     } else {
         A.gam_smem = 0;
-        size_t slice = (size_t)Lmax * Lmax * sizeof(double);
         nblocks = (int)std::min<size_t>((ws_bytes - 256) / slice,
                                         (size_t)nsm * k2_occupancy(A.use_delj, bytes_g + 256));
         A.gam_glob = (double *)((char *)ws + 256);

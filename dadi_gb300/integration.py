@@ -147,7 +147,7 @@ def run_table(phi, xx, table, frozen_mask=0, nomut_mask=0):
                                         len(table), int(frozen_mask), int(nomut_mask), int(delj),
                                         _lib.dptr(ws), nws, _lib.stream_handle(torch))
     _lib.check(rc, "dgb_integrate_table")
-    return d_phi.cpu().numpy()
+    return _lib.to_host(torch, d_phi)
 
 
 def step_lengths(dt, T, initial_t):
@@ -179,7 +179,7 @@ def run_precalc(phi, xx, abc, dts, theta0, frozen_mask=0, nomut_mask=0):
                                           int(frozen_mask), int(nomut_mask), _lib.dptr(ws), nws,
                                           _lib.stream_handle(torch))
     _lib.check(rc, "dgb_integrate_precalc")
-    return d_phi.cpu().numpy()
+    return _lib.to_host(torch, d_phi)
 
 
 # -------------------------------------------------- constant-coefficient build

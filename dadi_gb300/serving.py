@@ -12,29 +12,39 @@ Scheduling:
   are read back; requests wait while the budget is exhausted.
 * 2-D requests (IM, and IM with selection as used for DFE caches,
   dadi/DFE/DemogSelModels.py:162-197) are batched into *waves*: one wave is
-  one persistent launch over an explicit work-item list
-  (dgb_items2d_integrate), so requests with different grid sizes and sample
-  sizes share a launch.  Each wave runs on its own CUDA stream; a wave formed
-  while earlier ones are still running is launched immediately, and its CTAs
-  take SMs as the earlier waves' CTAs retire, so arrivals join work already
-  on the device instead of waiting for it to finish.  Densities stay on the
-  device from the initial condition to the spectrum; only spectra,
-  likelihoods and gradients come back.
-* 3-D and 4-D requests, and gradient requests, run on worker threads with
-  their own streams, overlapping the waves.
+  one launch over an explicit work-item list (dgb_items2d_integrate) with one
+  CTA per (request, grid) item, so requests with different grid sizes and
+  sample sizes share a launch.  Each wave's integration runs on its own
+  lowest-priority CUDA stream and its CTAs retire item by item, so a wave
+  launched while earlier ones are still running takes SMs as soon as any CTA
+  finishes: arrivals join work already on the device instead of waiting for
+  it to drain.  Waiting requests stay on the host, cheapest first, and are
+  launched while fewer than `slots` work items are in flight, so the host
+  keeps the order and new work never queues behind a deep device backlog.
+  When the host sees a wave's integration finish it queues the wave's
+  spectra, extrapolation and likelihoods on one highest-priority stream.
+  Densities stay on the device from the initial condition to the spectrum;
+  only spectra and likelihoods come back, in one copy per wave.
+* Gradient requests that share grid sizes, sample sizes and observed data
+  are grouped the same way into one forward-with-checkpoints launch and one
+  adjoint launch; they and the 3-D and 4-D requests run on worker threads
+  with their own streams, overlapping the waves.
 
 Every request records arrival, admission and completion times; latency is
-completion minus arrival.
+completion minus arrival.  The server uses up to max_inflight + 2 * workers
++ 2 streams at once; with CUDA_DEVICE_MAX_CONNECTIONS=32 in the environment
+before CUDA starts, they do not share hardware queues.
 """
 import ctypes
+import sys
 import threading
 import time
 from concurrent.futures import ThreadPoolExecutor
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 
-from . import _lib, batch, integration, models, numerics, phimanip, spectrum
+from . import _lib, batch, epilogue, models, numerics, phimanip, spectrum
 
 ITEM_DTYPE = np.dtype([("L", "i4"), ("masks", "i4"), ("xx_off", "i8"), ("out_off", "i8"),
                        ("sched", "i8")])
@@ -79,22 +89,60 @@ def _inst_record(req):
     raise ValueError(req.kind)
 
 
+class _Wave:
+    """One 2-D wave: phase 0 while its integration runs on its own stream,
+    phase 1 once its spectra are queued on the tail stream."""
+
+    def __init__(self, reqs, stream):
+        self.reqs = reqs
+        self.stream = stream
+        self.slots = []
+        self.shapes = []
+        self.phase = 0
+        self.event = None
+        self.nitems = 0
+
+    def finish(self):
+        """Copy results into the requests (the tail event has completed)."""
+        h = self.host.numpy()
+        lls = self.host_ll.numpy()
+        o = 0
+        for k, r in enumerate(self.reqs):
+            m = int(np.prod(self.shapes[k]))
+            r.fs = h[o:o + m].reshape(self.shapes[k]).copy()
+            o += m
+            if r.data is not None:
+                r.ll = float(lls[k])
+            r.status = int(self.status[k])
+        self.keep = self.d_phi = self.host = self.host_ll = None
+
+
 class Server:
     """hbm_budget: bytes of device memory requests may hold at once;
-    max_wave: most requests per 2-D wave; workers: threads for 3-D/4-D and
-    gradient requests."""
+    max_wave / min_wave: most / fewest requests per 2-D wave (fewer when
+    fewer are waiting); max_inflight: waves in flight at once (one CUDA
+    stream each); slots: most 2-D work items in flight (default two per
+    SM); workers: threads for 3-D/4-D requests, and as many again for
+    gradient groups."""
 
-    def __init__(self, hbm_budget=16 << 30, max_wave=512, workers=3, max_inflight=4):
+    def __init__(self, hbm_budget=16 << 30, max_wave=512, workers=4, max_inflight=16,
+                 min_wave=8, slots=None):
         self.torch = _lib.require_cuda()
         self.budget = int(hbm_budget)
         self.max_wave = max_wave
         self.max_inflight = max_inflight
+        self.min_wave = min_wave
+        if slots is None:
+            slots = 2 * self.torch.cuda.get_device_properties(
+                self.torch.cuda.current_device()).multi_processor_count
+        self.slots = int(slots)
         self.workers = workers
         self._used = 0
         self._lock = threading.Lock()
         self._grids = {}
         self._phi0 = {}
         self._engines = {}
+        self._obs = {}
 
     # ----------------------------------------------------------- resources
 
@@ -122,7 +170,7 @@ class Server:
         torch = self.torch
         if L not in self._grids:
             xx = numerics.default_grid(L)
-            self._grids[L] = (xx, torch.from_numpy(xx).cuda())
+            self._grids[L] = (xx, _lib.upload_resident(torch, xx))
         return self._grids[L]
 
     def _initial(self, L, gamma1):
@@ -131,16 +179,39 @@ class Server:
         if key not in self._phi0:
             xx = self._grid(L)[0]
             phi = phimanip.phi_1D_to_2D(xx, phimanip.phi_1D(xx, gamma=gamma1))
-            self._phi0[key] = self.torch.from_numpy(phi.ravel()).cuda()
+            self._phi0[key] = _lib.upload_resident(self.torch, phi.ravel())
         return self._phi0[key]
 
     # --------------------------------------------------------------- waves
 
+    def _data(self, data):
+        """Observed spectrum as a device tensor, uploaded once per array."""
+        if self.torch.is_tensor(data):
+            return data
+        key = id(data)
+        with self._lock:
+            hit = self._obs.get(key)
+            if hit is None or hit[0] is not data:
+                hit = self._obs[key] = (data, _lib.upload_resident(self.torch, data))
+        return hit[1]
+
+    def prepare(self, pts, ns_list):
+        """Upload ahead of time what 2-D requests at these grid sizes and
+        sample sizes need (grids, sampling tables, initial densities), so
+        the first requests of each size do not pay for it."""
+        for L in pts:
+            xx = self._grid(L)[0]
+            self._initial(L, 0.0)
+            for ns in ns_list:
+                for n in set(ns):
+                    spectrum._device_tables(self.torch, n, xx, self.torch.device("cuda"))
+
     def _launch_wave(self, reqs, stream):
-        """Enqueue one 2-D wave on `stream`; returns a finisher."""
+        """Enqueue one 2-D wave's integration on `stream` (lowest priority)
+        without waiting for the device; returns the _Wave."""
         torch = self.torch
         lib = _lib.lib()
-        n = len(reqs)
+        w = _Wave(reqs, stream)
         with torch.cuda.stream(stream):
             sh = _lib.stream_handle(torch)
             recs = np.stack([_inst_record(r) for r in reqs])
@@ -152,7 +223,6 @@ class Server:
                 o += L
             d_xx = torch.cat(xs)
             items, phi0s, off = [], [], 0
-            slots = []
             for k, r in enumerate(reqs):
                 g1 = r.params[6] if r.kind == "im_sel" else 0.0
                 sl = []
@@ -161,159 +231,239 @@ class Server:
                     phi0s.append(self._initial(L, g1))
                     sl.append((off, L))
                     off += L * L
-                slots.append(sl)
-            d_phi = torch.cat(phi0s)
-            d_items = torch.from_numpy(np.array(items, dtype=ITEM_DTYPE).view(np.uint8)).cuda()
+                w.slots.append(sl)
+            items = np.array(items, dtype=ITEM_DTYPE)
+            w.nitems = len(items)
+            w.d_phi = torch.cat(phi0s)
             st = batch.settings_from_globals()
-            table_h, roff_h, cnt_h, status_h = host_schedules(recs, st, self._grid(Ls[0])[0][1])
-            table = torch.from_numpy(table_h).cuda()
-            roff = torch.from_numpy(roff_h).cuda()
-            cnt = torch.from_numpy(cnt_h).cuda()
-            sched = torch.tensor([it[4] for it in items], dtype=torch.int64, device="cuda")
-            Lsq = torch.tensor([it[0] ** 2 for it in items], dtype=torch.int64, device="cuda")
-            order = torch.argsort(-(cnt.to(torch.int64)[sched] * Lsq), stable=True).to(torch.int32)
+            if st.use_old_timestep:
+                # dt depends on the grid: one schedule per item
+                req_of_item = items["sched"].copy()
+                table_h, roff_h, cnt_h, status_i = _item_schedules(
+                    recs, req_of_item, items["L"], st, {L: self._grid(L)[0][1] for L in Ls})
+                items["sched"] = np.arange(len(items))
+                w.status = np.zeros(len(reqs), np.int32)
+                np.bitwise_or.at(w.status, req_of_item, status_i)
+            else:
+                table_h, roff_h, cnt_h, w.status = host_schedules(recs, st,
+                                                                  self._grid(Ls[0])[0][1])
+            cost = cnt_h[items["sched"]].astype(np.int64) * items["L"].astype(np.int64) ** 2
+            order_h = np.argsort(-cost, kind="stable").astype(np.int32)
+            d_items = _lib.to_device(torch, items.view(np.uint8), np.uint8)
+            table = _lib.to_device(torch, table_h)
+            roff = _lib.to_device(torch, roff_h, np.int64)
+            cnt = _lib.to_device(torch, cnt_h, np.int32)
+            order = _lib.to_device(torch, order_h, np.int32)
             Lmax = max(Ls)
-            ws, nws = _lib.workspace(torch, lib.dgb_workspace_bytes(1, 2, Lmax, len(items)))
+            ws, nws = _lib.workspace(torch, lib.dgb_workspace_bytes(3, 2, Lmax, len(items)))
             _lib.check(lib.dgb_items2d_integrate(
-                _lib.dptr(d_items), len(items), Lmax, _lib.dptr(d_xx), _lib.dptr(d_phi),
+                _lib.dptr(d_items), len(items), Lmax, _lib.dptr(d_xx), _lib.dptr(w.d_phi),
                 _lib.dptr(table), _lib.dptr(roff), _lib.dptr(cnt), _lib.dptr(order),
-                ctypes.byref(st), _lib.dptr(ws), nws, sh), "dgb_items2d_integrate")
-            # spectra per (request): from_phi on each grid, extrapolate, ll
-            outs = []
-            for k, r in enumerate(reqs):
-                fs_l = []
-                for (o2, L) in slots[k]:
-                    phi = d_phi[o2:o2 + L * L].view(1, L, L)
-                    fs_l.append(spectrum.from_phi_2D_batch(torch, phi, r.ns[0], r.ns[1],
-                                                           self._grid(L)[0])[0])
-                x_l = [self._grid(L)[0][1] for L in r.pts_l]
-                fs = _extrap_torch(torch, fs_l, x_l)
-                ll = None
-                if r.data is not None:
-                    ll = _loglik_torch(torch, fs, r.data, r.scale)
-                outs.append((fs, ll))
-            done = torch.cuda.Event()
-            done.record(stream)
-        keep = (d_phi, d_items, table, ws, order, cnt, roff)
+                ctypes.byref(st), 1, _lib.dptr(ws), nws, sh), "dgb_items2d_integrate")
+            w.event = torch.cuda.Event()
+            w.event.record(stream)
+        w.keep = [d_items, table, ws, order, cnt, roff, d_xx]
+        return w
 
-        def finish():
-            done.synchronize()
-            for k, r in enumerate(reqs):
-                fs, ll = outs[k]
-                r.fs = fs.cpu().numpy()
-                r.ll = None if ll is None else float(ll.item())
-                r.status = int(status_h[k])
-            return keep
-        return done, finish
+    def _launch_tail(self, w, tail):
+        """A wave whose integration has finished: its spectra, extrapolation
+        and likelihoods (two launches, dgb_from_phi2d and dgb_extrap_ll) on
+        the shared high-priority `tail` stream, copied into pinned host
+        buffers."""
+        torch = self.torch
+        with torch.cuda.stream(tail):
+            jobs = []
+            for k, r in enumerate(w.reqs):
+                phis = [w.d_phi[o2:o2 + L * L].view(L, L) for (o2, L) in w.slots[k]]
+                xxs = [self._grid(L)[0] for L in r.pts_l]
+                data = self._data(r.data) if r.data is not None else None
+                jobs.append((phis, xxs, tuple(r.ns), data, r.scale))
+                w.shapes.append((r.ns[0] + 1, r.ns[1] + 1))
+            _, ll, flat = epilogue.spectra_2d(torch, jobs)
+            w.host = torch.empty(flat.numel(), dtype=torch.float64, pin_memory=True)
+            w.host.copy_(flat, non_blocking=True)
+            w.host_ll = torch.empty(ll.numel(), dtype=torch.float64, pin_memory=True)
+            w.host_ll.copy_(ll, non_blocking=True)
+            w.event = torch.cuda.Event()
+            w.event.record(tail)
+        w.phase = 1
 
     # ------------------------------------------------------------- workers
 
-    def _run_other(self, req):
+    def _engine(self, pts_l, ns):
+        key = (tuple(pts_l), tuple(ns))
+        with self._lock:
+            if key not in self._engines:
+                self._engines[key] = batch.Batch2D(pts_l, ns)
+            return self._engines[key]
+
+    def _run_grad_group(self, reqs):
+        """Gradient requests sharing grid sizes, sample sizes and data: one
+        forward-with-checkpoints and one adjoint launch for the group."""
         torch = self.torch
-        s = torch.cuda.Stream()
+        s = torch.cuda.Stream(priority=-1)
+        with torch.cuda.stream(s):
+            r0 = reqs[0]
+            eng = self._engine(r0.pts_l, r0.ns)
+            params = np.array([r.params for r in reqs], dtype=np.float64)
+            ll, ctx = eng.forward_for_adjoint(params, r0.data, scale=r0.scale,
+                                              tail_per_set=True)
+            grad = eng.adjoint(ctx, torch.ones_like(ll))
+            fs = _lib.to_host(torch, ctx["fs"])
+            ll = _lib.to_host(torch, ll.detach())
+            grad = _lib.to_host(torch, grad)
+            st = _lib.to_host(torch, ctx["status"])
+        for k, r in enumerate(reqs):
+            r.fs, r.ll, r.grad, r.status = fs[k], float(ll[k]), grad[k], int(st[k])
+        return reqs
+
+    def _run_other(self, req):
+        """3-D and 4-D requests: the drop-in drivers on a worker stream."""
+        torch = self.torch
+        s = torch.cuda.Stream(priority=-1)
         with torch.cuda.stream(s):
             if req.kind == "growth3":
                 f = numerics.make_extrap_func(models.growth3)
-                fs = f(req.params, req.ns, list(req.pts_l))
             elif req.kind == "four":
                 f = numerics.make_extrap_func(models.four_split)
-                fs = f(req.params, req.ns, list(req.pts_l))
-            elif req.kind == "im" and req.want_grad:
-                key = (tuple(req.pts_l), tuple(req.ns))
-                if key not in self._engines:
-                    self._engines[key] = batch.Batch2D(req.pts_l, req.ns)
-                eng = self._engines[key]
-                ll, grad, st = eng.loglik_and_grad(np.asarray(req.params)[None, :], req.data,
-                                                   scale=req.scale)
-                fs_t, _, _ = eng.run(np.asarray(req.params)[None, :])
-                req.fs = fs_t.cpu().numpy()[0]
-                req.ll = float(ll.item())
-                req.grad = grad.cpu().numpy()[0]
-                req.status = int(st.abs().sum())
-                return req
             else:
                 raise ValueError(req.kind)
+            fs = f(req.params, req.ns, list(req.pts_l))
             req.fs = np.asarray(fs.data)
             if req.data is not None:
                 from . import inference
                 req.ll = float(inference.ll(req.scale * fs, spectrum.Spectrum(req.data)))
-        return req
+        return [req]
 
     # ----------------------------------------------------------------- run
 
+    def _cost(self, req):
+        return self._steps(req) * sum(L * L for L in req.pts_l)
+
     def run(self, requests, clock=time.perf_counter):
         """Serve `requests` (arrival in seconds from now); returns them with
-        results and timings filled in."""
+        results and timings filled in.
+
+        2-D requests wait on the host, cheapest first (cost = steps x grid
+        points), and are launched in waves while the device has CTA slots
+        to spare: at most `slots` work items are in flight, so a new wave
+        never queues behind a deep backlog of CTAs already submitted, and the
+        host keeps the freedom to reorder what waits.  A wave takes an equal
+        share of the waiting requests per free stream, between min_wave and
+        max_wave, so waves hold requests of similar cost."""
+        torch = self.torch
         reqs = sorted(requests, key=lambda r: r.arrival)
         t0 = clock()
-        pending, inflight, futures = [], [], []
-        streams = [self.torch.cuda.Stream() for _ in range(self.max_inflight)]
-        free_streams = list(streams)
+        waiting2d, inflight, futures = [], [], []
+        # integrations at the lowest priority, spectra at the highest (torch
+        # clamps to the device's range)
+        free_streams = [torch.cuda.Stream(priority=0) for _ in range(self.max_inflight)]
+        tail = torch.cuda.Stream(priority=-8)
         pool = ThreadPoolExecutor(max_workers=self.workers)
+        gpool = ThreadPoolExecutor(max_workers=self.workers)
+        # the scheduling loop must get the interpreter back quickly from
+        # worker threads that build tables in Python
+        switch = sys.getswitchinterval()
+        sys.setswitchinterval(min(switch, 5e-4))
         nxt = 0
         remaining = len(reqs)
-        while remaining:
-            now = clock() - t0
-            while nxt < len(reqs) and reqs[nxt].arrival <= now:
-                pending.append(reqs[nxt])
-                nxt += 1
-            # admit 2-D spectrum requests into a wave; others to the workers
-            wave, keep = [], []
-            for r in pending:
-                fp = self.footprint(r)
-                if self._used + fp > self.budget and (inflight or futures or wave):
-                    keep.append(r)
-                    continue
-                r._fp = fp
-                self._used += fp
-                r.t_admit = clock() - t0
-                if r.kind in ("im", "im_sel") and not r.want_grad and len(wave) < self.max_wave:
-                    wave.append(r)
-                elif r.kind in ("im", "im_sel") and not r.want_grad:
-                    self._used -= fp
-                    keep.append(r)
-                else:
-                    futures.append((r, pool.submit(self._run_other, r)))
-            pending = keep
-            if wave:
-                if free_streams:
-                    s = free_streams.pop()
-                    ev, fin = self._launch_wave(wave, s)
-                    inflight.append((ev, fin, wave, s))
-                else:
-                    for r in wave:
-                        self._used -= r._fp
-                    pending = wave + pending
-            # completions
-            still = []
-            for ev, fin, wv, s in inflight:
-                if ev.query():
-                    fin()
-                    tdone = clock() - t0
-                    for r in wv:
-                        r.t_done = tdone
-                        self._used -= r._fp
-                        remaining -= 1
-                    free_streams.append(s)
-                else:
-                    still.append((ev, fin, wv, s))
-            inflight = still
-            fst = []
-            for r, fu in futures:
-                if fu.done():
-                    try:
-                        fu.result()
-                    except Exception as e:  # report per request, keep serving
-                        r.error = repr(e)
-                    r.t_done = clock() - t0
-                    self._used -= r._fp
-                    remaining -= 1
-                else:
-                    fst.append((r, fu))
-            futures = fst
-            if remaining:
-                time.sleep(2e-4)
-        pool.shutdown()
+        held = []   # non-wave requests waiting for budget
+
+        def busy():
+            return bool(inflight or futures)
+
+        try:
+            while remaining:
+                now = clock() - t0
+                arrived = []
+                while nxt < len(reqs) and reqs[nxt].arrival <= now:
+                    arrived.append(reqs[nxt])
+                    nxt += 1
+                # gradient groups and 3-D/4-D requests go to the workers
+                groups, keep = {}, []
+                for r in held + arrived:
+                    if r.kind in ("im", "im_sel") and not r.want_grad:
+                        waiting2d.append(r)
+                        continue
+                    fp = self.footprint(r)
+                    if self._used + fp > self.budget and (busy() or groups):
+                        keep.append(r)
+                        continue
+                    r._fp = fp
+                    self._used += fp
+                    r.t_admit = clock() - t0
+                    if r.kind == "im" and r.want_grad:
+                        key = (tuple(r.pts_l), tuple(r.ns), id(r.data), r.scale)
+                        groups.setdefault(key, []).append(r)
+                    else:
+                        futures.append(([r], pool.submit(self._run_other, r)))
+                held = keep
+                for grp in groups.values():
+                    futures.append((grp, gpool.submit(self._run_grad_group, grp)))
+                # 2-D waves, cheapest first, while streams and CTA slots are free
+                if waiting2d and arrived:
+                    waiting2d.sort(key=self._cost)
+                in_items = sum(w.nitems for w in inflight if w.phase == 0)
+                while waiting2d and free_streams and in_items < self.slots:
+                    share = -(-len(waiting2d) // len(free_streams))
+                    size = max(self.min_wave, min(self.max_wave, share))
+                    wave, items = [], 0
+                    for r in waiting2d:
+                        if len(wave) >= size or (wave and in_items + items >= self.slots):
+                            break
+                        fp = self.footprint(r)
+                        if self._used + fp > self.budget and (busy() or wave):
+                            break
+                        r._fp = fp
+                        self._used += fp
+                        r.t_admit = clock() - t0
+                        wave.append(r)
+                        items += len(r.pts_l)
+                    if not wave:
+                        break
+                    del waiting2d[:len(wave)]
+                    inflight.append(self._launch_wave(wave, free_streams.pop()))
+                    in_items += items
+                # completions
+                still = []
+                for w in inflight:
+                    if not w.event.query():
+                        still.append(w)
+                    elif w.phase == 0:
+                        # integration done: queue its spectra, free its stream
+                        self._launch_tail(w, tail)
+                        free_streams.append(w.stream)
+                        still.append(w)
+                    else:
+                        w.finish()
+                        tdone = clock() - t0
+                        for r in w.reqs:
+                            r.t_done = tdone
+                            self._used -= r._fp
+                            remaining -= 1
+                inflight = still
+                fst = []
+                for grp, fu in futures:
+                    if fu.done():
+                        try:
+                            fu.result()
+                        except Exception as e:  # report per request, keep serving
+                            for r in grp:
+                                r.error = repr(e)
+                        tdone = clock() - t0
+                        for r in grp:
+                            r.t_done = tdone
+                            self._used -= r._fp
+                            remaining -= 1
+                    else:
+                        fst.append((grp, fu))
+                futures = fst
+                if remaining:
+                    time.sleep(2e-4)
+        finally:
+            pool.shutdown()
+            gpool.shutdown()
+            sys.setswitchinterval(switch)
         return reqs
 
 
@@ -341,26 +491,21 @@ def host_schedules(recs, st, dx0, max_steps=10 ** 7):
     return table, off, cnt, status
 
 
-def _extrap_torch(torch, fs_l, x_l, fail_mag=10):
-    if len(fs_l) == 1:
-        return fs_l[0]
-    ex = numerics.linear_extrap(fs_l, x_l) if len(fs_l) == 2 else \
-        numerics.quadratic_extrap(fs_l, x_l)
-    best = fs_l[int(np.argmin(x_l))]
-    failed = torch.abs(torch.log10(ex / best)) > fail_mag
-    return torch.where(failed, best, ex)
-
-
-def _loglik_torch(torch, fs, data, scale):
-    model = scale * fs
-    d = data if torch.is_tensor(data) else torch.from_numpy(np.asarray(data, np.float64)).cuda()
-    mask = torch.zeros_like(model, dtype=torch.bool)
-    mask.view(-1)[0] = True
-    mask.view(-1)[-1] = True
-    ok = (~mask) & (model > 0)
-    term = -model + d * torch.log(torch.where(ok, model, torch.ones_like(model))) \
-        - torch.lgamma(d + 1.0)
-    return torch.where(ok, term, torch.zeros_like(term)).sum()
+def _item_schedules(recs, req_of_item, L_of_item, st, dx0_of_L):
+    """One schedule per work item (with use_old_timestep the step depends on
+    the grid spacing): item j's request evaluated with item j's grid."""
+    tabs, cnts, stats = [], [], []
+    for j in range(len(req_of_item)):
+        q = int(req_of_item[j])
+        t, _, c, sst = host_schedules(recs[q:q + 1], st, dx0_of_L[int(L_of_item[j])])
+        tabs.append(t[:int(c[0]) * 11])
+        cnts.append(int(c[0]))
+        stats.append(int(sst[0]))
+    cnt = np.array(cnts, dtype=np.int32)
+    off = np.zeros(len(cnt), dtype=np.int64)
+    off[1:] = np.cumsum(cnt.astype(np.int64))[:-1]
+    table = np.concatenate(tabs) if tabs else np.zeros(11)
+    return table, off, cnt, np.array(stats, dtype=np.int32)
 
 
 def config5_stream(n, seed=0, rate=2000.0, grad_frac=0.1, obs=None):
@@ -375,7 +520,6 @@ def config5_stream(n, seed=0, rate=2000.0, grad_frac=0.1, obs=None):
     gaps = rng.exponential(1.0 / rate, n)
     cls = rng.choice(4, size=n, p=[0.70, 0.20, 0.08, 0.02])
     gammas = -np.logspace(np.log10(2000), np.log10(1e-4), 50)
-    base = batch.IM_PARAMS
     im0 = (0.6233, 0.05171, 0.2775, 0.01061, 8.917, 7.671)
     draws = _im_draws(n, rng)
     reqs, t = [], 0.0
@@ -400,7 +544,6 @@ def config5_stream(n, seed=0, rate=2000.0, grad_frac=0.1, obs=None):
             p = int(rng.integers(30, 37))
             reqs.append(Request(k, "four", models.FOUR_DEFAULT, (p, p + 2, p + 4),
                                 (10, 10, 10, 10), arrival=t))
-    del base
     return reqs
 
 

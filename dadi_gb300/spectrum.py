@@ -128,14 +128,34 @@ def from_phi(phi, ns, xxs, mask_corners=True, pop_ids=None):
     return Spectrum(data, mask_corners=mask_corners, extrap_x=xxs[0][1], pop_ids=pop_ids)
 
 
+_device_cache = {}
+
+
+def _device_tables(torch, n, xx, dev):
+    """(dbeta1, dbeta2, xx) as device tensors, uploaded once per (n, grid,
+    device) and kept: later calls enqueue no host-to-device copy, so they
+    never wait for work already queued on their stream."""
+    from . import _lib
+    dev = torch.device(dev)
+    if dev.index is None:
+        dev = torch.device("cuda", torch.cuda.current_device())
+    key = (n, np.asarray(xx, dtype=np.float64).tobytes(), dev.index)
+    hit = _device_cache.get(key)
+    if hit is None:
+        d1, d2 = dbeta_tables(n, xx)
+        with torch.cuda.device(dev):
+            hit = tuple(_lib.upload_resident(torch, t) for t in (d1, d2, xx))
+        _device_cache[key] = hit
+    return hit
+
+
 def from_phi_2D_batch(torch, phi_b, n1, n2, xx):
     """Raw 2-D spectra of a batch of densities phi_b (B, L, L) resident on
     the GPU: the same contraction as _from_phi_2D, batched as FP64 GEMMs.
     Returns a (B, n1+1, n2+1) float64 CUDA tensor."""
     dev = phi_b.device
-    d1x, d2x = [torch.from_numpy(np.ascontiguousarray(t)).to(dev) for t in dbeta_tables(n1, xx)]
-    d1y, d2y = [torch.from_numpy(np.ascontiguousarray(t)).to(dev) for t in dbeta_tables(n2, xx)]
-    x = torch.from_numpy(np.ascontiguousarray(xx)).to(dev)
+    d1x, d2x, x = _device_tables(torch, n1, xx, dev)
+    d1y, d2y, _ = _device_tables(torch, n2, xx, dev)
     dxv = x[1:] - x[:-1]
     s_y = (phi_b[:, :, 1:] - phi_b[:, :, :-1]) / dxv
     c1_y = (phi_b[:, :, :-1] - s_y * x[:-1]) / (n2 + 1)

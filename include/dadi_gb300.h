@@ -78,8 +78,9 @@ int dgb_abi_version(void);
 const char *dgb_status_string(int status);
 
 /* Scratch bytes needed by a call.  kind: 0 = dgb_integrate_table /
- * dgb_integrate_precalc / the single sweeps, 1 = dgb_batch2d_integrate (with
- * n = number of work items), 2 = dgb_tridiag_batch. */
+ * dgb_integrate_precalc / the single sweeps, 1 = dgb_batch2d_integrate and
+ * dgb_items2d_integrate (with n = number of work items), 2 =
+ * dgb_tridiag_batch, 3 = dgb_items2d_integrate with one_per_cta. */
 size_t dgb_workspace_bytes(int kind, int ndim, int L, long n);
 
 /* Batched Numerical-Recipes tridiagonal solve of `batch` independent systems
@@ -204,8 +205,10 @@ int dgb_batch2d_integrate_ckpt(const int *masks, int ninst, const int *Ls, int n
                                void *stream);
 
 /* Discrete adjoint of those integrations.  lam (device, phi_out layout) holds
- * dJ/dphi_final on entry and is overwritten; grad (device, ninst x
- * DGB_AD_NPAR, zeroed by the caller) receives dJ/dtheta summed over the grids.
+ * dJ/dphi_final on entry and is overwritten; grad (device, ninst x ngrids x
+ * DGB_AD_NPAR) receives each (instance, grid) work item's part of
+ * dJ/dtheta (written, not accumulated, so the caller's sum over the grids is
+ * in a fixed order and the result does not depend on CTA timing).
  * Each work item recomputes its checkpoint segments forward and walks them
  * backwards through the transposed tridiagonal solves.  Scratch per CTA:
  * dgb_adjoint2d_scratch_bytes; ws = 256 bytes of counter + that scratch for
@@ -232,14 +235,17 @@ typedef struct {
 } dgb_item2d;
 
 /* The batched 2-D integration over an explicit list of work items, so one
- * persistent launch mixes grids of different sizes and integrations of
- * different requests (the serving engine's continuous batches).  Lmax bounds
- * every item's L; order (device, optional) gives the start order; ws as for
- * dgb_batch2d_integrate with Lmax. */
+ * launch mixes grids of different sizes and integrations of different
+ * requests (the serving engine's continuous batches).  Lmax bounds every
+ * item's L; order (device, optional) gives the start order.  one_per_cta = 0:
+ * a persistent launch sized to the device whose CTAs pull items from a queue
+ * (ws from dgb_workspace_bytes kind 1); one_per_cta = 1: one CTA per item,
+ * each retiring after its item, so launches on other streams take SMs as
+ * soon as any CTA finishes (ws from kind 3 with n = nitems). */
 int dgb_items2d_integrate(const dgb_item2d *items, int nitems, int Lmax, const double *xx_all,
                           double *phi_out, const double *table, const long *row_off,
                           const int *row_cnt, const int *order, const dgb_settings *settings,
-                          void *ws, size_t ws_bytes, void *stream);
+                          int one_per_cta, void *ws, size_t ws_bytes, void *stream);
 
 /* dgb_sched2d evaluated in C on the host (all arrays HOST): table == NULL
  * counts rows into row_cnt; otherwise writes the rows at table +
@@ -255,6 +261,45 @@ int dgb_sched2d_host(const dgb_inst2d *insts, int ninst, const dgb_settings *set
 int dgb_batch2d_count_steps(const dgb_inst2d *insts, int ninst,
                             const dgb_settings *settings, long max_steps,
                             long *steps_out);
+
+/* Spectrum epilogue of 2-D integrations (device-resident inputs, one launch
+ * per list).  dgb_from_phi2d: raw spectrum of each density,
+ * out[a][b] (n1+1 x n2+1) = the piecewise-linear integral of phi against
+ * binomial sampling (dadi/Spectrum_mod.py:1509-1547, _from_phi_2D_linalg),
+ * given the weight tables d1 = dbeta1, d2 = dbeta2 of cached_dbeta(n, xx)
+ * (:25-40), each (n+1) x (L-1) C-ordered.  The item array itself is in device
+ * memory; Lmax / nmax bound every item's L and n2 (they size the shared
+ * memory: dgb_from_phi2d_smem_bytes), items outside them are skipped.  The
+ * reference computes these on the host with numpy after copying phi back. */
+typedef struct {
+    const double *phi;        /* L x L density */
+    const double *xx;         /* the grid */
+    const double *d1x, *d2x;  /* weight tables for n1 */
+    const double *d1y, *d2y;  /* weight tables for n2 */
+    double *out;              /* (n1+1) x (n2+1) */
+    int L, n1, n2, pad_;
+} dgb_fs_item2d;
+size_t dgb_from_phi2d_smem_bytes(int Lmax, int nmax);
+int dgb_from_phi2d(const dgb_fs_item2d *items, int nitems, int Lmax, int nmax, void *stream);
+
+/* Extrapolation of 1-3 grids' spectra to zero grid spacing at x = 0
+ * (linear_extrap / quadratic_extrap, dadi/Numerics.py:644-669; x = each
+ * grid's xx[1], the Spectrum's extrap_x) with entries more than fail_mag
+ * orders of magnitude from the smallest-x grid's replaced by it
+ * (dadi/Numerics.py:449-464), written to out; with data and ll set, also the
+ * Poisson log-likelihood sum(-m + d log m - lgamma(d + 1)), m = scale * out,
+ * over entries with m > 0, excluding the first and last entry when
+ * mask_corners (dadi/Inference.py:466-509). */
+typedef struct {
+    const double *fs[3];
+    double x[3];
+    double *out;
+    const double *data;       /* NULL: no likelihood */
+    double *ll;               /* one double */
+    double scale;
+    int ngrids, size, mask_corners, pad_;
+} dgb_extrap_item;
+int dgb_extrap_ll(const dgb_extrap_item *items, int nitems, double fail_mag, void *stream);
 
 /* Allocation-free 2-D integration; it has no counterpart in the reference.
  * The same computation as dgb_integrate_table for ndim == 2 (one integration

@@ -181,10 +181,8 @@ def test_batched_matches_reference(cuda_lib, golden):
 
 
 def test_batched_alone_equals_in_mix(cuda_lib):
-    """Each instance's integrated densities are bitwise the same alone and
-    inside a batch; its spectrum agrees within 1e-10 (the from_phi matrix
-    products run through cuBLAS, whose summation order depends on the batch
-    size)."""
+    """Each instance's integrated densities and its spectrum are bitwise the
+    same alone and inside a batch (one CTA per item in every launch)."""
     from dadi_gb300 import batch
     draws = cases.im_draws(24)
     eng = batch.Batch2D((30, 40), (10, 10))
@@ -195,4 +193,4 @@ def test_batched_alone_equals_in_mix(cuda_lib):
         for pa, pm in zip(phis, phis_mix):
             assert np.array_equal(pa.cpu().numpy()[0], pm.cpu().numpy()[i])
         alone, _, _ = eng.run(draws[i:i + 1])
-        assert max_rel(alone.cpu().numpy()[0], fs_mix.cpu().numpy()[i]) < 1e-10
+        assert np.array_equal(alone.cpu().numpy()[0], fs_mix.cpu().numpy()[i])
