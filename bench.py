@@ -437,9 +437,10 @@ def run_serving(a, obs):
 
 def run_adjoint(a, obs):
     """Gradients of the Poisson log-likelihood for the first 256 seed-0 IM
-    parameter sets at pts [100,110,120], ns (40,40): forward with
+    parameter sets at pts [100,110,120], ns (40,40) (forward with
     checkpoints, from_phi/extrapolation/likelihood backward through torch,
-    and the discrete adjoint; CUDA-event timed."""
+    and the discrete adjoint; CUDA-event timed), and for 32 parameter sets of
+    the three-population growth model at pts 80."""
     import torch
     from dadi_gb300 import batch
     draws = im_draws(256, 0)
@@ -458,11 +459,34 @@ def run_adjoint(a, obs):
     torch.cuda.synchronize()
     fwd = e0.elapsed_time(e1) / 1e3
     adj = e1.elapsed_time(e2) / 1e3
-    return {"sets": 256, "pts_l": [100, 110, 120], "ns": list(NS),
-            "checkpoint_every": ctx["C"], "forward_s": fwd, "adjoint_s": adj,
-            "gradients_per_s": 256 / (fwd + adj),
-            "failed_instances": int((ctx["status"] != 0).sum()),
-            "finite": bool(torch.isfinite(grad).all())}
+    out = {"im2d": {"sets": 256, "pts_l": [100, 110, 120], "ns": list(NS),
+                    "checkpoint_every": ctx["C"], "forward_s": fwd, "adjoint_s": adj,
+                    "gradients_per_s": 256 / (fwd + adj),
+                    "failed_instances": int((ctx["status"] != 0).sum()),
+                    "finite": bool(torch.isfinite(grad).all())}}
+    # three populations: 32 sets of the growth model's parameters, each
+    # scaled by exp(U(log .5, log 2)) (seed 0), at pts 80, ns (20,20,20)
+    from dadi_gb300 import adjoint_nd, models
+    th0 = adjoint_nd.Growth3.from_model_params(models.GROWTH3_DEFAULT)
+    sets = th0 * np.exp(np.random.default_rng(0).uniform(np.log(.5), np.log(2), (32, 10)))
+    m3 = adjoint_nd.Growth3((80,), (20, 20, 20))
+    fs3, _ = m3.spectrum_ll(th0)
+    obs3 = np.random.default_rng(0).poisson(1e4 * np.abs(fs3.cpu().numpy())).astype(float)
+    d3 = torch.from_numpy(obs3).cuda()
+    m3.loglik_and_grad(sets[0], d3, 1e4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    finite = True
+    for th in sets:
+        _, g3, _ = m3.loglik_and_grad(th, d3, 1e4)
+        finite = finite and bool(torch.isfinite(g3).all())
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    out["growth3"] = {"sets": 32, "pts": 80, "ns": [20, 20, 20], "wall_s": wall,
+                      "gradients_per_s": 32 / wall, "finite": finite,
+                      "note": "one set at a time; host wall clock (forward with every "
+                              "step's density kept, adjoint, table derivatives)"}
+    return out
 
 
 def run_profile_case(a):

@@ -32,7 +32,8 @@ EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
            "dgb_probe_rcp", "dgb_integrate2d_noalloc", "dgb_sched2d_deriv",
            "dgb_batch2d_integrate_ckpt", "dgb_adjoint2d_scratch_bytes", "dgb_adjoint2d",
            "dgb_items2d_integrate", "dgb_sched2d_host", "dgb_from_phi2d_smem_bytes",
-           "dgb_from_phi2d", "dgb_extrap_ll"]
+           "dgb_from_phi2d", "dgb_extrap_ll", "dgb_integrate_table_states",
+           "dgb_adjoint_table_nd_gpart_doubles", "dgb_adjoint_table_nd"]
 
 
 class PForm(ctypes.Structure):
@@ -98,6 +99,9 @@ def _declare(L):
         "dgb_from_phi2d_smem_bytes": (sz, [i, i]),
         "dgb_from_phi2d": (i, [_vp, i, i, i, _vp]),
         "dgb_extrap_ll": (i, [_vp, i, d, _vp]),
+        "dgb_integrate_table_states": (i, [_vp, i, i, _vp, _vp, i, i, i, _vp, _vp]),
+        "dgb_adjoint_table_nd_gpart_doubles": (sz, [i, i]),
+        "dgb_adjoint_table_nd": (i, [_vp, i, i, _vp, _vp, i, i, i, _vp, _vp, _vp, sz, _vp]),
         "dgb_adjoint2d": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp, _vp,
                               _vp, _vp, i, _vp, _vp, _vp, ctypes.POINTER(Settings), _vp, sz,
                               _vp]),

@@ -1,0 +1,318 @@
+"""Gradients of spectrum log-likelihoods for N-population models
+(1-4 populations) by the discrete adjoint of the table-driven time loop
+(dgb_integrate_table_states, dgb_adjoint_table_nd).
+
+The adjoint gives dJ/d(parameter-table entry) for every step.  The table is
+a function of the model parameters through the schedule walk of the
+reference loop (dadi/Integration.py:504-553 for three populations: dt from
+the current parameters by _compute_dt, :147-176, the final partial step
+T - t, and the sizes evaluated at the next time); `table_dual` walks that
+schedule in forward-mode dual numbers, producing the table values exactly as
+integration.build_table does and their derivatives, and the chain rule
+dJ/dtheta = sum_k sum_j dJ/drow_kj drow_kj/dtheta finishes the gradient.
+
+The loss tail (from_phi, extrapolation, Poisson likelihood) is tiny and is
+differentiated by torch autograd; its gradient with respect to each grid's
+final density seeds the adjoint.
+
+`Growth3` is the three-population workload (three populations split from
+one, each growing exponentially from nu0_i to nuF_i over T, symmetric
+migration): parameters (nu0_1, nu0_2, nu0_3, nuF_1, nuF_2, nuF_3, m12, m13,
+m23, T) with fixed selection gammas.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib, integration, numerics, phimanip, spectrum
+
+PF_CONST, PF_EXPLOG = 0, 2
+
+
+class Form:
+    """A parameter as a function of time with derivative seeds: kind
+    PF_CONST (value a) or PF_EXPLOG (a * exp(log(b / a) * t / c), the
+    exponential-growth lambda of the workloads); da, db, dc are
+    d(a, b, c)/dtheta."""
+
+    def __init__(self, kind, a, b=0.0, c=1.0, da=None, db=None, dc=None, npar=0):
+        z = np.zeros(npar)
+        self.kind, self.a, self.b, self.c = kind, float(a), float(b), float(c)
+        self.da = z if da is None else np.asarray(da, float)
+        self.db = z if db is None else np.asarray(db, float)
+        self.dc = z if dc is None else np.asarray(dc, float)
+
+    def at(self, t, dtd):
+        """(value, d value/dtheta) at time t with dt/dtheta = dtd."""
+        if self.kind == PF_CONST:
+            return self.a, self.da.copy()
+        a, b, c = self.a, self.b, self.c
+        lq = np.log(b / a)
+        v = a * np.exp(lq * t / c)
+        e = v / a
+        dlq = self.db / b - self.da / a
+        dz = (dlq * t + lq * dtd) / c - (lq * t / c) * self.dc / c
+        return v, self.da * e + a * e * dz
+
+
+def _compute_dt_dual(nu, dnu, ms, dms, gamma, dgamma, h, dh, settings, dx0):
+    """_compute_dt (dadi/Integration.py:147-176) with its derivative along the
+    branch its max takes; the value is computed exactly as
+    integration._compute_dt does."""
+    tsf, otsf, old, _ = settings
+    npar = len(dnu)
+    if old:
+        return otsf * dx0, np.zeros(npar)
+    t1 = np.abs(h + (1 - 2 * h) * 0.5) * 0.5 * (1 - 0.5)
+    u2 = h + (1 - 2 * h) * 0.25
+    t2 = np.abs(u2) * 0.25 * (1 - 0.25)
+    tm = max(t1, t2)
+    cands = [0.25 / nu, sum(ms), abs(gamma) * 2 * tm]
+    maxVM = max(cands)
+    if not maxVM > 0:
+        return np.inf, np.zeros(npar)
+    br = cands.index(maxVM)
+    if br == 0:
+        dmx = -0.25 * dnu / (nu * nu)
+    elif br == 1:
+        dmx = np.sum(dms, axis=0) if len(dms) else np.zeros(npar)
+    else:
+        dtm = (np.sign(u2) * 0.5 * dh * 0.25 * (1 - 0.25)) if t2 > t1 else 0.0 * dh
+        dmx = np.sign(gamma) * dgamma * 2 * tm + abs(gamma) * 2 * dtm
+    dt = tsf / maxVM
+    if dt == 0:
+        raise ValueError('Timestep is zero.')
+    return dt, -tsf * dmx / (maxVM * maxVM)
+
+
+def table_dual(P, xx, T, dT, nu_forms, mig_forms, gamma_forms, h_forms, theta0_form,
+               initial_t=0.0):
+    """Parameter table of a P-population time loop (the layout of
+    integration.build_table, DGB_ROW_STRIDE(P) doubles per step) and its
+    derivative with respect to the npar model parameters: (table (n,
+    stride), drows (n, stride, npar)).  mig_forms[k][j] is the rate into k
+    from j; gamma, h and theta0 are Forms as well."""
+    settings = integration.current_settings()
+    npar = len(dT)
+    dx0 = xx[1] - xx[0]
+    stride = integration.row_stride(P)
+    offd = [(k, j) for k in range(P) for j in range(P) if j != k]
+    t, dtd = float(initial_t), np.zeros(npar)
+    nu = [f.at(t, dtd) for f in nu_forms]
+    gam = [f.at(t, dtd) for f in gamma_forms]
+    hh = [f.at(t, dtd) for f in h_forms]
+    mig = {kj: mig_forms[kj[0]][kj[1]].at(t, dtd) for kj in offd}
+    rows, drows = [], []
+    while t < T:
+        best = None
+        for k in range(P):
+            ms = [mig[(k, j)][0] for j in range(P) if j != k]
+            dms = [mig[(k, j)][1] for j in range(P) if j != k]
+            if P == 1:
+                ms, dms = [0], [np.zeros(npar)]
+            c = _compute_dt_dual(nu[k][0], nu[k][1], ms, dms, gam[k][0], gam[k][1],
+                                 hh[k][0], hh[k][1], settings, dx0)
+            if best is None or c[0] < best[0]:
+                best = c
+        rem, drem = T - t, dT - dtd
+        this, dthis = (best if best[0] <= rem else (rem, drem))
+        t, dtd = t + this, dtd + dthis
+        nu = [f.at(t, dtd) for f in nu_forms]
+        gam = [f.at(t, dtd) for f in gamma_forms]
+        hh = [f.at(t, dtd) for f in h_forms]
+        mig = {kj: mig_forms[kj[0]][kj[1]].at(t, dtd) for kj in offd}
+        th = theta0_form.at(t, dtd)
+        row = np.empty(stride)
+        drow = np.zeros((stride, npar))
+        row[0], drow[0] = this, dthis
+        row[1], drow[1] = th
+        for k in range(P):
+            row[2 + k], drow[2 + k] = nu[k]
+            row[2 + P + k], drow[2 + P + k] = gam[k]
+            row[2 + 2 * P + k], drow[2 + 2 * P + k] = hh[k]
+        row[2 + 3 * P] = 1.0
+        for q, kj in enumerate(offd):
+            row[3 + 3 * P + q], drow[3 + 3 * P + q] = mig[kj]
+        rows.append(row)
+        drows.append(drow)
+    return (np.array(rows, dtype=np.float64).reshape(len(rows), stride),
+            np.array(drows, dtype=np.float64).reshape(len(rows), stride, npar))
+
+
+class TableModel:
+    """An N-population model run through parameter tables on the GPU, with
+    the gradient of its Poisson log-likelihood by the discrete adjoint.
+    Subclasses give P, the initial density and the table with derivatives."""
+
+    P = None
+    npar = None
+
+    def __init__(self, pts_l, ns):
+        self.torch = _lib.require_cuda()
+        self.pts_l = [int(p) for p in np.atleast_1d(pts_l)]
+        self.ns = tuple(int(n) for n in ns)
+        self.xxs = [numerics.default_grid(L) for L in self.pts_l]
+
+    def initial(self, xx):
+        raise NotImplementedError
+
+    def table(self, params, xx):
+        raise NotImplementedError
+
+    def _forward(self, params, keep_states):
+        torch, lib = self.torch, _lib.lib()
+        P = self.P
+        out = []
+        for L, xx in zip(self.pts_l, self.xxs):
+            table, drows = self.table(params, xx)
+            d_phi = _lib.to_device(torch, self.initial(xx))
+            d_xx = _lib.to_device(torch, xx)
+            d_tab = _lib.to_device(torch, table)
+            n = len(table)
+            states = torch.empty(((n + 1) * L ** P if keep_states else L ** P),
+                                 dtype=torch.float64, device="cuda")
+            sh = _lib.stream_handle(torch)
+            if keep_states:
+                _lib.check(lib.dgb_integrate_table_states(
+                    _lib.dptr(d_phi), P, L, _lib.dptr(d_xx), _lib.dptr(d_tab), n, 0, 0,
+                    _lib.dptr(states), sh), "dgb_integrate_table_states")
+            else:
+                ws, nws = _lib.workspace(torch, lib.dgb_workspace_bytes(0, P, L, 0))
+                _lib.check(lib.dgb_integrate_table(
+                    _lib.dptr(d_phi), P, L, _lib.dptr(d_xx), _lib.dptr(d_tab), n, 0, 0, 0,
+                    _lib.dptr(ws), nws, sh), "dgb_integrate_table")
+            out.append(dict(L=L, xx=xx, d_xx=d_xx, d_tab=d_tab, n=n, drows=drows,
+                            phi=d_phi.view(*([L] * P)), states=states))
+        return out
+
+    def _tail(self, phis, data, scale):
+        """Extrapolated spectrum and Poisson log-likelihood (torch, so that
+        autograd gives dJ/dphi)."""
+        torch = self.torch
+        fs_l = [from_phi_torch(torch, p, self.ns, xx) for p, xx in zip(phis, self.xxs)]
+        x_l = [xx[1] for xx in self.xxs]
+        if len(fs_l) == 1:
+            fs = fs_l[0]
+        else:
+            ex = (numerics.linear_extrap(fs_l, x_l) if len(fs_l) == 2
+                  else numerics.quadratic_extrap(fs_l, x_l))
+            best = fs_l[int(np.argmin(x_l))]
+            failed = torch.abs(torch.log10(ex / best)) > 10
+            fs = torch.where(failed, best, ex)
+        if data is None:
+            return fs, None
+        d = data if torch.is_tensor(data) else _lib.to_device(torch, data)
+        model = scale * fs
+        mask = torch.zeros(tuple(model.shape), dtype=torch.bool, device=model.device)
+        mask.view(-1)[0] = True
+        mask.view(-1)[-1] = True
+        ok = (~mask) & (model > 0)
+        term = -model + d * torch.log(torch.where(ok, model, torch.ones_like(model))) \
+            - torch.lgamma(d + 1.0)
+        return fs, torch.where(ok, term, torch.zeros_like(term)).sum()
+
+    def spectrum_ll(self, params, data=None, scale=1.0):
+        """(extrapolated spectrum, log-likelihood or None) as CUDA tensors."""
+        runs = self._forward(params, keep_states=False)
+        return self._tail([r["phi"] for r in runs], data, scale)
+
+    def loglik_and_grad(self, params, data, scale=1.0):
+        """(ll, dll/dparams (npar,), spectrum) for one parameter set."""
+        torch, lib = self.torch, _lib.lib()
+        P = self.P
+        runs = self._forward(params, keep_states=True)
+        phis = [r["phi"].detach().requires_grad_(True) for r in runs]
+        with torch.enable_grad():
+            fs, ll = self._tail(phis, data, scale)
+        lams = torch.autograd.grad(ll, phis, allow_unused=True)
+        grad = torch.zeros(self.npar, dtype=torch.float64, device="cuda")
+        stride = integration.row_stride(P)
+        for r, lam in zip(runs, lams):
+            L, n = r["L"], r["n"]
+            if n == 0:
+                continue
+            lam = (lam if lam is not None else torch.zeros_like(r["phi"])).contiguous().clone()
+            per = lib.dgb_adjoint_table_nd_gpart_doubles(P, L)
+            gpart = torch.empty(n * per, dtype=torch.float64, device="cuda")
+            ws, nws = _lib.workspace(torch, max(P - 1, 1) * L ** P * 8)
+            _lib.check(lib.dgb_adjoint_table_nd(
+                _lib.dptr(lam), P, L, _lib.dptr(r["d_xx"]), _lib.dptr(r["d_tab"]), n, 0, 0,
+                _lib.dptr(r["states"]), _lib.dptr(gpart), _lib.dptr(ws), nws,
+                _lib.stream_handle(torch)), "dgb_adjoint_table_nd")
+            gp = gpart.view(n, per)
+            G = gp[:, :per - 2].reshape(n, -1, stride).sum(dim=1)
+            G[:, 0] += gp[:, per - 2]
+            G[:, 1] += gp[:, per - 1]
+            D = _lib.to_device(torch, r["drows"])
+            grad += torch.einsum("kj,kjp->p", G, D)
+            r["states"] = None
+        return ll.detach(), grad, fs.detach()
+
+
+class Growth3(TableModel):
+    """models.growth3 with parameters theta = (nu0_1, nu0_2, nu0_3, nuF_1,
+    nuF_2, nuF_3, m12, m13, m23, T) and fixed gammas (default: the
+    3-population workload's (-2, 0, 5)), h = 0.5, theta0 = 1."""
+
+    P = 3
+    npar = 10
+
+    def __init__(self, pts_l, ns, gammas=(-2.0, 0.0, 5.0)):
+        super().__init__(pts_l, ns)
+        self.gammas = tuple(float(g) for g in gammas)
+
+    @staticmethod
+    def from_model_params(p):
+        """models.growth3 parameters ((nu0..), (nuF..), (m12, m13, m23),
+        gammas, T) -> theta."""
+        nu0, nuF, m, _, T = p
+        return np.array(list(nu0) + list(nuF) + list(m) + [T], dtype=np.float64)
+
+    def model_params(self, theta):
+        th = [float(v) for v in theta]
+        return (tuple(th[0:3]), tuple(th[3:6]), tuple(th[6:9]), self.gammas, th[9])
+
+    def initial(self, xx):
+        phi = phimanip.phi_1D_to_2D(xx, phimanip.phi_1D(xx))
+        return phimanip.phi_2D_to_3D_split_2(xx, phi)
+
+    def table(self, theta, xx):
+        th = np.asarray(theta, dtype=np.float64)
+        e = np.eye(self.npar)
+        T = th[9]
+        nus = [Form(PF_EXPLOG, th[i], th[3 + i], T, da=e[i], db=e[3 + i], dc=e[9],
+                    npar=self.npar) for i in range(3)]
+        mi = {(0, 1): 6, (0, 2): 7, (1, 2): 8}
+        mig = [[None] * 3 for _ in range(3)]
+        for k in range(3):
+            for j in range(3):
+                if j != k:
+                    q = mi[(min(k, j), max(k, j))]
+                    mig[k][j] = Form(PF_CONST, th[q], da=e[q], npar=self.npar)
+        gam = [Form(PF_CONST, g, npar=self.npar) for g in self.gammas]
+        hs = [Form(PF_CONST, 0.5, npar=self.npar) for _ in range(3)]
+        th0 = Form(PF_CONST, 1.0, npar=self.npar)
+        return table_dual(3, xx, T, e[9], nus, mig, gam, hs, th0)
+
+
+def from_phi_torch(torch, phi, ns, xx):
+    """Spectrum.from_phi for 1-3 populations as differentiable torch ops on
+    the GPU (the contraction of dadi/Spectrum_mod.py:1509-1547, and for three
+    populations the loop over the third axis of :1774-1810 as one batched
+    product)."""
+    P = phi.dim()
+    if P == 2:
+        return spectrum.from_phi_2D_batch(torch, phi[None], ns[0], ns[1], xx)[0]
+    if P == 3:
+        nz = ns[2]
+        d1z, d2z, x = spectrum._device_tables(torch, nz, xx, phi.device)
+        dxv = x[1:] - x[:-1]
+        s_z = (phi[:, :, 1:] - phi[:, :, :-1]) / dxv
+        c1_z = (phi[:, :, :-1] - s_z * x[:-1]) / (nz + 1)
+        w = torch.arange(1, nz + 2, dtype=torch.float64, device=phi.device) / \
+            ((nz + 1) * (nz + 2))
+        over = torch.einsum("ijk,bk->bij", c1_z, d1z) + \
+            w[:, None, None] * torch.einsum("ijk,bk->bij", s_z, d2z)
+        fs = spectrum.from_phi_2D_batch(torch, over.contiguous(), ns[0], ns[1], xx)
+        return fs.permute(1, 2, 0).contiguous()
+    raise NotImplementedError("from_phi_torch handles 2 or 3 populations")

@@ -19,178 +19,9 @@
 #include <algorithm>
 #include <cstring>
 
-#include "dgb_common.cuh"
-#include "dgb_internal.h"
+#include "dgb_nd.cuh"
 
 namespace dgb {
-
-struct NDArgs {
-    double *phi;
-    const double *xx;
-    int ndim, L, axis;
-    long nlines, S, LS; // lines, stride of the axis, L*S
-    // parameters: from table row `step` when table != null, else explicit
-    const double *table;
-    long step;
-    double nu, gamma, h, beta, dt, theta0;
-    double mig[DGB_MAX_DIM];
-    int inject_mask; // populations whose mutations are injected by this sweep
-    // constant-coefficient mode
-    const double *ca, *cb, *cc;
-    const double *dts;
-};
-
-__host__ __device__ inline size_t nd_smem_doubles(int L, int nt, bool delj)
-{
-    return (size_t)L * (nt + 1) + (size_t)L * nt + (size_t)(delj ? 10 : 5) * L + 6 * (size_t)L;
-}
-
-struct NDShared {
-    AxisScalars s;
-    double vscale;
-    double inj[DGB_MAX_DIM];
-};
-
-// Coordinates (all axes) of the first point of line `line` along `axis`.
-__device__ __forceinline__ long nd_line_base(const NDArgs &A, long line, int *coord)
-{
-    long outer = line / A.S, inner = line - outer * A.S;
-    long base = outer * A.LS + inner;
-    long rem = base;
-    for (int k = A.ndim - 1; k >= 0; k--) {
-        coord[k] = (int)(rem % A.L);
-        rem /= A.L;
-    }
-    return base;
-}
-
-__device__ void nd_load_params(const NDArgs &A, NDShared &Sh, const GridVecs &g)
-{
-    const int P = A.ndim, ax = A.axis;
-    AxisScalars &s = Sh.s;
-    double beta = A.beta;
-    if (A.table) {
-        const double *row = A.table + A.step * row_stride(P);
-        s.dt = row[0];
-        Sh.inj[0] = row[1]; // theta0, used below
-        s.nu = row[row_nu(P, ax)];
-        s.gamma = row[row_gamma(P, ax)];
-        s.h = row[row_h(P, ax)];
-        beta = row[row_beta(P)];
-        for (int j = 0; j < P; j++)
-            s.mig[j] = (j == ax) ? 0.0 : row[row_mig(P, ax, j)];
-    } else {
-        s.dt = A.dt;
-        Sh.inj[0] = A.theta0;
-        s.nu = A.nu;
-        s.gamma = A.gamma;
-        s.h = A.h;
-        for (int j = 0; j < P; j++)
-            s.mig[j] = (j == ax) ? 0.0 : A.mig[j];
-    }
-    double theta0 = Sh.inj[0];
-    s.inv_nu = 1.0 / s.nu;
-    double msum = 0;
-    for (int j = 0; j < P; j++)
-        if (j != ax)
-            msum = msum + s.mig[j];
-    s.msum = msum;
-    const int L = A.L;
-    s.B1s = 0.5 * (s.dt * g.dfac[0]);
-    s.B1e = -0.5 * (s.dt * g.dfac[L - 1]);
-    corner_bc(P, ax, s.mig, s.nu, s.gamma, s.h, g.x[0], g.x[L - 1], g.dx[0], g.dx[L - 2], s.dt,
-              s.bcs, s.bce);
-    // Vfunc_beta's factor in 1-D (dadi/integration_shared.c:8-10)
-    Sh.vscale = (P == 1) ? pow(beta + 1, 2) / (4 * beta) : 1.0;
-    double val = inject_value(P, s.dt, theta0, g.x[0], g.x[1], g.x[2]);
-    for (int k = 0; k < DGB_MAX_DIM; k++)
-        Sh.inj[k] = (A.inject_mask >> k & 1) ? val : 0.0;
-}
-
-__device__ void nd_grid_consts(const NDArgs &A, GridVecs &g)
-{
-    const int L = A.L;
-    for (int i = threadIdx.x; i < L; i += blockDim.x) {
-        double x = A.xx[i];
-        g.x[i] = x;
-        g.xv[i] = x * (1. - x);
-        if (i < L - 1) {
-            double d = A.xx[i + 1] - x;
-            g.dx[i] = d;
-            g.ih[i] = 1.0 / (2 * d);
-            g.xInt[i] = 0.5 * (A.xx[i + 1] + x);
-        }
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < L; i += blockDim.x) {
-        if (i == 0)
-            g.dfac[i] = 2. / g.dx[0];
-        else if (i == L - 1)
-            g.dfac[i] = 2. / g.dx[L - 2];
-        else
-            g.dfac[i] = 2. / (g.dx[i] + g.dx[i - 1]);
-    }
-    __syncthreads();
-}
-
-__device__ __forceinline__ void nd_carve(double *smem, int L, int nt, bool delj, double *&tile,
-                                         double *&gam, GridVecs &g, AxisVecs &v)
-{
-    double *p = smem;
-    tile = p;
-    p += (size_t)L * (nt + 1);
-    gam = p;
-    p += (size_t)L * nt;
-    g.x = p; p += L;
-    g.xv = p; p += L;
-    g.dfac = p; p += L;
-    g.xInt = p; p += L;
-    g.ih = p; p += L;
-    g.dx = p; p += L;
-    v.A1 = p; p += L;
-    v.A0 = p; p += L;
-    v.C1 = p; p += L;
-    v.C0 = p; p += L;
-    v.B0 = p; p += L;
-    if (delj) {
-        v.G = p; p += L;
-        v.Pv = p; p += L;
-        v.Qv = p; p += L;
-        v.VI = p; p += L;
-        v.DF = p; p += L;
-    }
-}
-
-// Load (dir=0) or store (dir=1) the CTA's tile of lines [l0, l0+n).
-__device__ __forceinline__ void nd_tile_io(const NDArgs &A, double *tile, int nt, long l0, int n,
-                                           bool store)
-{
-    const int L = A.L, tp = nt + 1;
-    if (A.S == 1) {
-        // contiguous axis: the n lines are n*L consecutive doubles
-        double *g0 = A.phi + l0 * L;
-        for (int idx = threadIdx.x; idx < n * L; idx += blockDim.x) {
-            int t = idx / L, p = idx - t * L;
-            if (store)
-                g0[idx] = tile[p * tp + t];
-            else
-                tile[p * tp + t] = g0[idx];
-        }
-    } else {
-        int t = threadIdx.x;
-        if (t < n) {
-            long line = l0 + t;
-            long outer = line / A.S, inner = line - outer * A.S;
-            double *g0 = A.phi + outer * A.LS + inner;
-            for (int p = 0; p < L; p++) {
-                if (store)
-                    g0[p * A.S] = tile[p * tp + t];
-                else
-                    tile[p * tp + t] = g0[p * A.S];
-            }
-        }
-    }
-}
 
 template <bool DELJ>
 __global__ void k_sweep_nd(NDArgs A)
@@ -344,36 +175,6 @@ __global__ void k_tridiag_batch(const double *a, const double *b, const double *
         us[j] = fma(-gs[j + 1], us[j + 1], us[j]);
 }
 
-// ------------------------------------------------------------ host side
-
-static long ipow(int L, int p)
-{
-    long r = 1;
-    for (int i = 0; i < p; i++)
-        r *= L;
-    return r;
-}
-
-static int nd_threads(int L, long nlines)
-{
-    int nt = (L <= 48) ? 128 : 64;
-    if (nlines < nt)
-        nt = (int)std::max<long>(32, (nlines + 31) / 32 * 32);
-    return nt;
-}
-
-static void nd_fill(NDArgs &A, double *phi, int ndim, int L, int axis, const double *xx)
-{
-    A.phi = phi;
-    A.xx = xx;
-    A.ndim = ndim;
-    A.L = L;
-    A.axis = axis;
-    A.S = ipow(L, ndim - 1 - axis);
-    A.LS = A.S * L;
-    A.nlines = ipow(L, ndim - 1);
-}
-
 static int nd_launch_sweep(NDArgs &A, bool delj, cudaStream_t st)
 {
     int nt = nd_threads(A.L, A.nlines);
@@ -404,7 +205,8 @@ static int nd_launch_precalc(NDArgs &A, cudaStream_t st)
     return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
 }
 
-static bool shape_ok(int ndim, int L) { return ndim >= 1 && ndim <= DGB_MAX_DIM && L >= 3; }
+
+int nd_sweep(NDArgs &A, bool delj, cudaStream_t st) { return nd_launch_sweep(A, delj, st); }
 
 } // namespace dgb
 

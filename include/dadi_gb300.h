@@ -262,6 +262,32 @@ int dgb_batch2d_count_steps(const dgb_inst2d *insts, int ninst,
                             const dgb_settings *settings, long max_steps,
                             long *steps_out);
 
+/* Discrete adjoint of the N-dimensional table-driven time loop (1-4
+ * populations), for any parameter table.
+ *
+ * dgb_integrate_table_states: dgb_integrate_table through the per-axis
+ * sweeps that also records the density at the start of every step and at the
+ * end: states (device) holds (nsteps + 1) x L^ndim doubles.  (The delj trick
+ * is not differentiated.)
+ *
+ * dgb_adjoint_table_nd: lam (device, L^ndim) holds dJ/dphi_final on entry
+ * and dJ/dphi_initial on exit; gpart (device,
+ * nsteps x dgb_adjoint_table_nd_gpart_doubles) receives per step the partial
+ * sums of dJ/d(table row entries): for each swept axis j (in sweep order)
+ * one DGB_ROW_STRIDE(ndim) row per CTA of that sweep, followed by two
+ * doubles, the injection's dJ/d(dt) and dJ/d(theta0).  Summing a step's
+ * rows (any fixed order) and adding those two to entries 0 and 1 gives
+ * dJ/d(row) for that step.  ws: (active axes - 1) x L^ndim doubles.  The
+ * reference has no adjoint; its gradients come from finite differences
+ * (dadi/Godambe.py:131-185). */
+int dgb_integrate_table_states(double *phi, int ndim, int L, const double *xx,
+                               const double *table, int nsteps, int frozen_mask,
+                               int nomut_mask, double *states, void *stream);
+size_t dgb_adjoint_table_nd_gpart_doubles(int ndim, int L);
+int dgb_adjoint_table_nd(double *lam, int ndim, int L, const double *xx, const double *table,
+                         int nsteps, int frozen_mask, int nomut_mask, const double *states,
+                         double *gpart, double *ws, size_t ws_bytes, void *stream);
+
 /* Spectrum epilogue of 2-D integrations (device-resident inputs, one launch
  * per list).  dgb_from_phi2d: raw spectrum of each density,
  * out[a][b] (n1+1 x n2+1) = the piecewise-linear integral of phi against

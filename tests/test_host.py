@@ -116,3 +116,40 @@ def test_const_coefficients_match_oracle(P, axis):
     a2 = oint.precalc_coefficients(xx, P, axis, 0.7, ms, -1.2, 0.3)
     for u, v in zip(a1, a2):
         assert np.array_equal(u, v)
+
+
+def test_table_dual_values_equal_build_table():
+    """The dual-number schedule walk of the N-dimensional adjoint produces the
+    parameter table exactly as the drop-in's build_table does from the model's
+    own callables (dadi/Integration.py:504-553), and its derivative matches
+    finite differences of the table."""
+    from dadi_gb300 import adjoint_nd, integration, models, numerics
+    xx = numerics.default_grid(20)
+    (nu0, nuF, (m12, m13, m23), g, T) = models.GROWTH3_DEFAULT
+    # T / dt must not be an integer, or a perturbation adds or drops a step
+    # and the table has no elementwise derivative (the workload's default T
+    # is exactly 675 steps of 1e-3 / 4.5)
+    T = 0.1537
+    nus = [(lambda a, b: (lambda t: a * np.exp(np.log(b / a) * t / T)))(a, b)
+           for a, b in zip(nu0, nuF)]
+    f = integration.ensure_1arg_func
+    mig = [[None, f(m12), f(m13)], [f(m12), None, f(m23)], [f(m13), f(m23), None]]
+    ref, _ = integration.build_table(3, xx, T, 0.0, [f(v) for v in nus], mig,
+                                     [f(v) for v in g], [f(0.5)] * 3, f(1.0))
+    model = adjoint_nd.Growth3.__new__(adjoint_nd.Growth3)
+    model.gammas = tuple(g)
+    theta = adjoint_nd.Growth3.from_model_params(models.GROWTH3_DEFAULT)
+    theta[9] = T
+    tab, drows = model.table(theta, xx)
+    assert np.array_equal(tab, ref)
+    for k in range(10):
+        h = 1e-6 * theta[k]
+        tp, tm = theta.copy(), theta.copy()
+        tp[k] += h
+        tm[k] -= h
+        a, _ = model.table(tp, xx)
+        b, _ = model.table(tm, xx)
+        assert a.shape == b.shape == tab.shape
+        fd = (a - b) / (2 * h)
+        # finite-difference noise: an ulp of a table entry over 2h (~1e-9)
+        assert np.allclose(drows[:, :, k], fd, rtol=1e-6, atol=1e-8)
