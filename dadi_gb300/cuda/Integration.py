@@ -79,6 +79,22 @@ def _four_pops_temporal_params(phi, xx, T, initial_t, nu1_f, nu2_f, nu3_f, nu4_f
                      theta0_f, [frozen1, frozen2, frozen3, frozen4], [False] * 4, deme_ids)
 
 
+def _five_pops_temporal_params(phi, xx, T, initial_t, nu1_f, nu2_f, nu3_f, nu4_f, nu5_f,
+                               m12_f, m13_f, m14_f, m15_f, m21_f, m23_f, m24_f, m25_f, m31_f,
+                               m32_f, m34_f, m35_f, m41_f, m42_f, m43_f, m45_f, m51_f, m52_f,
+                               m53_f, m54_f, gamma1_f, gamma2_f, gamma3_f, gamma4_f, gamma5_f,
+                               h1_f, h2_f, h3_f, h4_f, h5_f, theta0_f, frozen1, frozen2,
+                               frozen3, frozen4, frozen5, deme_ids):
+    """dadi/cuda/Integration.py:753-994."""
+    mig_f = [[None, m12_f, m13_f, m14_f, m15_f], [m21_f, None, m23_f, m24_f, m25_f],
+             [m31_f, m32_f, None, m34_f, m35_f], [m41_f, m42_f, m43_f, None, m45_f],
+             [m51_f, m52_f, m53_f, m54_f, None]]
+    return _temporal(5, phi, xx, T, initial_t, [nu1_f, nu2_f, nu3_f, nu4_f, nu5_f], mig_f,
+                     [gamma1_f, gamma2_f, gamma3_f, gamma4_f, gamma5_f],
+                     [h1_f, h2_f, h3_f, h4_f, h5_f], theta0_f,
+                     [frozen1, frozen2, frozen3, frozen4, frozen5], [False] * 5, deme_ids)
+
+
 def _const(phi, xx, theta0, frozen, nomut, abc, current_t, dt, T):
     dts = _core.step_lengths(dt, T, current_t)
     out = _core.run_precalc(phi, xx, abc, dts, theta0, _masks(frozen), _masks(nomut))

@@ -338,6 +338,27 @@ def three_pops(phi, xx, T, nu1=1, nu2=1, nu3=1, m12=0, m13=0, m21=0, m23=0, m31=
                       enable_cuda_cached)
 
 
+def five_pops(phi, xx, T, nu1=1, nu2=1, nu3=1, nu4=1, nu5=1,
+              m12=0, m13=0, m14=0, m15=0, m21=0, m23=0, m24=0, m25=0,
+              m31=0, m32=0, m34=0, m35=0, m41=0, m42=0, m43=0, m45=0,
+              m51=0, m52=0, m53=0, m54=0,
+              gamma1=0, gamma2=0, gamma3=0, gamma4=0, gamma5=0,
+              h1=0.5, h2=0.5, h3=0.5, h4=0.5, h5=0.5,
+              theta0=1, initial_t=0, frozen1=False, frozen2=False,
+              frozen3=False, frozen4=False, frozen5=False, deme_ids=None):
+    """dadi/Integration.py:729-937 on the GPU; returns a new array (the
+    reference's CPU path updates phi in place)."""
+    phi = np.array(phi, dtype=np.float64, copy=True)
+    if T - initial_t == 0:
+        return phi
+    _check_T(T, initial_t)
+    mig = [[0, m12, m13, m14, m15], [m21, 0, m23, m24, m25], [m31, m32, 0, m34, m35],
+           [m41, m42, m43, 0, m45], [m51, m52, m53, m54, 0]]
+    return _integrate(5, phi, xx, T, initial_t, [nu1, nu2, nu3, nu4, nu5], mig,
+                      [gamma1, gamma2, gamma3, gamma4, gamma5], [h1, h2, h3, h4, h5], theta0,
+                      [frozen1, frozen2, frozen3, frozen4, frozen5], [False] * 5, False)
+
+
 def four_pops(phi, xx, T, nu1=1, nu2=1, nu3=1, nu4=1, m12=0, m13=0, m14=0, m21=0, m23=0,
               m24=0, m31=0, m32=0, m34=0, m41=0, m42=0, m43=0, gamma1=0, gamma2=0, gamma3=0,
               gamma4=0, h1=0.5, h2=0.5, h3=0.5, h4=0.5, theta0=1, initial_t=0, frozen1=False,

@@ -34,7 +34,7 @@ extern "C" {
 #define DGB_ERR_WORKSPACE (-4)   /* workspace missing or too small */
 #define DGB_ERR_TOO_LARGE (-5)   /* grid larger than dgb_integrate2d_noalloc's static scratch */
 
-#define DGB_MAX_DIM 4
+#define DGB_MAX_DIM 5
 #define DGB_ROW_STRIDE(P) (3 + 3 * (P) + (P) * ((P)-1))
 
 /* Parametric time dependence of one parameter, evaluated on the device.

@@ -319,6 +319,34 @@ def three_pops(phi, xx, T, nu1=1, nu2=1, nu3=1, m12=0, m13=0, m21=0, m23=0, m31=
                               f(theta0), [frozen1, frozen2, frozen3])
 
 
+def five_pops(phi, xx, T, nu1=1, nu2=1, nu3=1, nu4=1, nu5=1,
+              m12=0, m13=0, m14=0, m15=0, m21=0, m23=0, m24=0, m25=0,
+              m31=0, m32=0, m34=0, m35=0, m41=0, m42=0, m43=0, m45=0,
+              m51=0, m52=0, m53=0, m54=0,
+              gamma1=0, gamma2=0, gamma3=0, gamma4=0, gamma5=0,
+              h1=0.5, h2=0.5, h3=0.5, h4=0.5, h5=0.5,
+              theta0=1, initial_t=0, frozen1=False, frozen2=False, frozen3=False,
+              frozen4=False, frozen5=False):
+    """Like dadi/Integration.py:729-937 this integrates phi in place (no copy)."""
+    if T - initial_t == 0:
+        return phi
+    if T - initial_t < 0:
+        raise ValueError('Final integration time T is less than intial_time.')
+    mig = [[0, m12, m13, m14, m15], [m21, 0, m23, m24, m25], [m31, m32, 0, m34, m35],
+           [m41, m42, m43, 0, m45], [m51, m52, m53, m54, 0]]
+    fr = [frozen1, frozen2, frozen3, frozen4, frozen5]
+    for k in range(5):
+        if fr[k] and any(mig[k][j] != 0 or mig[j][k] != 0 for j in range(5) if j != k):
+            raise ValueError('Population cannot be frozen and have non-zero '
+                             'migration to or from it.')
+    f = ensure_1arg_func
+    mig_f = [[None if j == k else f(mig[k][j]) for j in range(5)] for k in range(5)]
+    return integrate_temporal(phi, xx, T, initial_t,
+                              [f(v) for v in (nu1, nu2, nu3, nu4, nu5)], mig_f,
+                              [f(v) for v in (gamma1, gamma2, gamma3, gamma4, gamma5)],
+                              [f(v) for v in (h1, h2, h3, h4, h5)], f(theta0), fr)
+
+
 def four_pops(phi, xx, T, nu1=1, nu2=1, nu3=1, nu4=1,
               m12=0, m13=0, m14=0, m21=0, m23=0, m24=0,
               m31=0, m32=0, m34=0, m41=0, m42=0, m43=0,

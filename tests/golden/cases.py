@@ -101,6 +101,28 @@ for _f in range(16):
                                                   "theta_t", 0.0] +
              [bool(_f & 1), bool(_f & 2), bool(_f & 4), bool(_f & 8)]))
 
+# five_pops(phi, xx, T, nu1..nu5, m12, m13, m14, m15, m21, m23, m24, m25, m31, m32,
+#           m34, m35, m41, m42, m43, m45, m51, m52, m53, m54, gamma1..5, h1..5,
+#           theta0, initial_t, frozen1..5)
+FIVE_POPS = [
+    dict(name="5d_default7", grid="default", pts=7, seed=55,
+         args=[0.05, 1, 2, 0.5, 1.5, 0.8] + [0.3, 0.2, 0.1, 0.4, 1, 0.6, 0.2, 0.3, 0.7,
+                                             0.2, 0.5, 0.1, 0.9, 1, 0.4, 0.3, 0.2, 0.6,
+                                             0.5, 0.1] +
+              [-1, 2, 0.5, 0, 1.5, 0.3, 0.4, 0.5, 0.6, 0.7, "theta_t", 0.01]),
+    dict(name="5d_temporal_lin6", grid="lin", pts=6, seed=56,
+         args=[0.05, "lin_nu3", 2, 0.5, 1.5, 0.8] + [0.3, 0.2, 0.1, 0.4, "lin_m23", 0.6, 0.2,
+                                                     0.3, 0.7, 0.2, 0.5, 0.1, 0.9, 1, 0.4,
+                                                     0.3, 0.2, 0.6, 0.5, 0.1] +
+              [-1, 2, "ident", 0, 1.5, 0.3, 0.4, 0.5, "h_t", 0.7, 1.0, 0.0]),
+]
+for _f in (1, 6, 21, 31):
+    FIVE_POPS.append(dict(
+        name="5d_frozen%d" % _f, grid="default", pts=6, seed=500 + _f,
+        args=[0.05, 1, 2, 0.5, 1.5, 0.8] + [0] * 20 + [-1, 2, 0.5, 0, 1.5, 0.3, 0.4, 0.5,
+                                                      0.6, 0.7, "theta_t", 0.0] +
+             [bool(_f & 1), bool(_f & 2), bool(_f & 4), bool(_f & 8), bool(_f & 16)]))
+
 # one_pop(phi, xx, T, nu, gamma, h, theta0, initial_t, frozen, beta)
 ONE_POP = [
     dict(name="1d_const", grid="default", pts=40, seed=10,
@@ -118,8 +140,11 @@ SWEEPS = [
     ("3Dx", 3, 0, 12, "lin"), ("3Dy", 3, 1, 12, "default"), ("3Dz", 3, 2, 12, "default"),
     ("4Dx", 4, 0, 7, "default"), ("4Dy", 4, 1, 7, "lin"), ("4Dz", 4, 2, 7, "default"),
     ("4Da", 4, 3, 7, "default"),
+    ("5Dx", 5, 0, 6, "default"), ("5Dy", 5, 1, 6, "lin"), ("5Dz", 5, 2, 6, "default"),
+    ("5Da", 5, 3, 6, "default"), ("5Db", 5, 4, 6, "default"),
 ]
-SWEEP_PARAMS = dict(nu=0.7, mig=[0.3, 1.2, 0.5, 2.0], gamma=-1.5, h=0.3, beta=1.3, dt=0.004)
+SWEEP_PARAMS = dict(nu=0.7, mig=[0.3, 1.2, 0.5, 2.0, 0.8], gamma=-1.5, h=0.3, beta=1.3,
+                    dt=0.004)
 
 #: Config-1 workload (split_mig) and the IM parameter draws of the batched workload.
 SPLIT_MIG = dict(params=(2.0, 0.5, 0.2, 1.0), ns=(20, 20), pts_l=[40, 50, 60])

@@ -60,9 +60,11 @@ def gen_integrations(dadi, out):
     for group, fn, nd in [("two", dadi.Integration.two_pops, 2),
                           ("three", dadi.Integration.three_pops, 3),
                           ("four", dadi.Integration.four_pops, 4),
+                          ("five", dadi.Integration.five_pops, 5),
                           ("one", dadi.Integration.one_pop, 1)]:
         lst = {"two": cases.TWO_POPS, "three": cases.THREE_POPS,
-               "four": cases.FOUR_POPS, "one": cases.ONE_POP}[group]
+               "four": cases.FOUR_POPS, "five": cases.FIVE_POPS,
+               "one": cases.ONE_POP}[group]
         for case in lst:
             xx = cases.grid(case["grid"], case["pts"])
             phi0 = cases.initial_phi(case["seed"], (case["pts"],) * nd)
@@ -76,9 +78,10 @@ def gen_sweeps(dadi, out):
     ic = dadi.integration_c
     p = cases.SWEEP_PARAMS
     rng = np.random.default_rng(77)
+    rng5 = np.random.default_rng(78)  # the 5-D cases, added later, draw apart
     for name, nd, axis, pts, g in cases.SWEEPS:
         xx = cases.grid(g, pts)
-        phi0 = rng.uniform(size=(pts,) * nd)
+        phi0 = (rng5 if nd == 5 else rng).uniform(size=(pts,) * nd)
         for delj in (0, 1):
             phi = phi0.copy()
             mig = [p["mig"][j] for j in range(nd) if j != axis]

@@ -24,6 +24,11 @@ SWEEP_TOL = 1e-12
 # to lower accuracy" (dadi/Integration.py:24).
 DELJ_SWEEP_TOL = 1e-8
 INT_TOL = 1e-9
+# Five populations: the kernels form the drift sum_k m_k (x_k - x) of four
+# migration terms as W - msum * x with W = sum_k m_k x_k per line, which
+# reassociates four partly cancelling terms (measured 2.8e-12 on the last
+# axis, where the rates into population 5 sum to 4).
+SWEEP_TOL_5D = 5e-12
 
 
 def _dev(torch, a):
@@ -43,13 +48,13 @@ def test_single_sweep(cuda_lib, golden, name, nd, axis, pts, gk, delj):
     p = cases.SWEEP_PARAMS
     xx = cases.grid(gk, pts)
     phi = _dev(torch, g["sweep_%s_phi0" % name])
-    mig = (ctypes.c_double * 4)(*p["mig"])
+    mig = (ctypes.c_double * len(p["mig"]))(*p["mig"])
     rc = cuda_lib.dgb_implicit_sweep(_lib.dptr(phi), nd, pts, axis, _lib.dptr(_dev(torch, xx)),
                                      p["nu"], mig, p["gamma"], p["h"], p["beta"], p["dt"], delj,
                                      None, 0, _lib.stream_handle(torch))
     assert rc == 0
     out = phi.cpu().numpy()
-    tol = DELJ_SWEEP_TOL if delj else SWEEP_TOL
+    tol = DELJ_SWEEP_TOL if delj else (SWEEP_TOL_5D if nd == 5 else SWEEP_TOL)
     assert _rel(out, g["sweep_%s_delj%d" % (name, delj)]) < tol
 
 
@@ -88,7 +93,7 @@ def test_tridiag_batch(cuda_lib, golden):
 def test_integration_case(cuda_lib, golden, group, case):
     from dadi_gb300 import integration as gi
     fn = {"one": gi.one_pop, "two": gi.two_pops, "three": gi.three_pops,
-          "four": gi.four_pops}[group]
+          "four": gi.four_pops, "five": gi.five_pops}[group]
     xx, phi0, args, kw = case_inputs(group, case)
     out = fn(phi0.copy(), xx, *args, **kw)
     assert _rel(out, golden["integrate"]["int_" + case["name"]]) < INT_TOL
@@ -194,3 +199,22 @@ def test_batched_alone_equals_in_mix(cuda_lib):
             assert np.array_equal(pa.cpu().numpy()[0], pm.cpu().numpy()[i])
         alone, _, _ = eng.run(draws[i:i + 1])
         assert np.array_equal(alone.cpu().numpy()[0], fs_mix.cpu().numpy()[i])
+
+
+def test_dropin_five_pops_signature(cuda_lib, golden):
+    """dadi.cuda.Integration._five_pops_temporal_params (the call
+    dadi/Integration.py:864-872 makes under cuda_enabled) with the reference
+    signature, against dadi's own five_pops."""
+    from dadi_gb300.cuda import Integration as CI
+    from dadi_gb300 import integration as gi
+    f = gi.ensure_1arg_func
+    case = cases.FIVE_POPS[0]
+    xx, phi0, a, kw = case_inputs("five", case)
+    T = a[0]
+    nus, ms, gs, hs = a[1:6], a[6:26], a[26:31], a[31:36]
+    th, t0 = a[36], a[37]
+    out = CI._five_pops_temporal_params(phi0.copy(), xx, T, t0, *[f(v) for v in nus],
+                                        *[f(v) for v in ms], *[f(v) for v in gs],
+                                        *[f(v) for v in hs], f(th), False, False, False, False,
+                                        False, None)
+    assert _rel(out, golden["integrate"]["int_" + case["name"]]) < INT_TOL

@@ -12,7 +12,7 @@ from util import ALL_CASES, case_inputs
 @pytest.mark.parametrize("group,case", ALL_CASES, ids=[c["name"] for _, c in ALL_CASES])
 def test_integration_bitwise(golden, group, case):
     fn = {"one": oint.one_pop, "two": oint.two_pops, "three": oint.three_pops,
-          "four": oint.four_pops}[group]
+          "four": oint.four_pops, "five": oint.five_pops}[group]
     xx, phi0, args, kw = case_inputs(group, case)
     out = fn(phi0.copy(), xx, *args, **kw)
     assert np.array_equal(out, golden["integrate"]["int_" + case["name"]])

@@ -15,7 +15,7 @@ def max_rel(a, b, floor=0.0):
 
 
 def case_inputs(group, case):
-    nd = {"one": 1, "two": 2, "three": 3, "four": 4}[group]
+    nd = {"one": 1, "two": 2, "three": 3, "four": 4, "five": 5}[group]
     xx = cases.grid(case["grid"], case["pts"])
     phi0 = cases.initial_phi(case["seed"], (case["pts"],) * nd)
     args = [cases.resolve(v) for v in case["args"]]
@@ -24,7 +24,7 @@ def case_inputs(group, case):
 
 
 GROUPS = [("one", cases.ONE_POP), ("two", cases.TWO_POPS), ("three", cases.THREE_POPS),
-          ("four", cases.FOUR_POPS)]
+          ("four", cases.FOUR_POPS), ("five", cases.FIVE_POPS)]
 ALL_CASES = [(g, c) for g, lst in GROUPS for c in lst]
 
 
