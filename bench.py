@@ -511,6 +511,44 @@ def run_profile_case(a):
     return 0
 
 
+def run_profile_kernel(a):
+    """Small cases of the other kernels for ncu captures (each launch well
+    under 0.1 s, a few hundred MB on the device at most), run twice."""
+    import torch
+    from dadi_gb300 import adjoint_nd, batch, build, epilogue, models
+    build.build()
+    for _ in range(2):
+        t = time.perf_counter()
+        if a.profile == "epilogue":
+            # the epilogue of the full 4096-instance batch: 12288 densities
+            eng = batch.Batch2D(PTS_L, NS)
+            phis = [torch.rand(NINST, L, L, dtype=torch.float64, device="cuda")
+                    for L in PTS_L]
+            fs, ll = epilogue.spectra_2d_batch(torch, phis, eng.xxs, NS,
+                                               torch.ones(41, 41, dtype=torch.float64,
+                                                          device="cuda"), 1.0)
+        elif a.profile == "sweep3d":
+            # the 3-population growth model at pts 70 (675 steps x 3 sweeps)
+            m = adjoint_nd.Growth3((70,), (20, 20, 20))
+            m.spectrum_ll(adjoint_nd.Growth3.from_model_params(models.GROWTH3_DEFAULT))
+        elif a.profile == "adjoint2d":
+            draws = im_draws(NINST, 0)
+            steps = batch.count_steps(batch.im_instances(draws))
+            sel = np.where((steps >= 200) & (steps <= 400))[0][:16]
+            eng = batch.Batch2D(PTS_L, NS)
+            eng.loglik_and_grad(draws[sel], torch.ones(41, 41, dtype=torch.float64,
+                                                       device="cuda"), 1.0)
+        elif a.profile == "adjointnd":
+            m = adjoint_nd.Growth3((40,), (10, 10, 10))
+            th = adjoint_nd.Growth3.from_model_params(models.GROWTH3_DEFAULT)
+            m.loglik_and_grad(th, torch.ones(11, 11, 11, dtype=torch.float64,
+                                             device="cuda"), 1.0)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+    print(json.dumps({"mode": "profile", "case": a.profile, "seconds": dt}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -533,9 +571,14 @@ def main():
     ap.add_argument("--profile-items", type=int, default=0,
                     help="run only a small batch (this many seed-0 instances with 200-800 "
                          "steps, twice) for profiler captures, then exit")
+    ap.add_argument("--profile", default=None,
+                    choices=["epilogue", "sweep3d", "adjoint2d", "adjointnd"],
+                    help="run a small case of another kernel for profiler captures, then exit")
     a = ap.parse_args()
     if a.profile_items:
         return run_profile_case(a)
+    if a.profile:
+        return run_profile_kernel(a)
     world, rank, local = dist_init()
     if a.impl == "reference":
         rc = run_reference(a, world, rank)

@@ -188,6 +188,10 @@ static long ipow(int L, int p)
     return r;
 }
 
+// Lines per CTA of a sweep launch.  (Halving it to one warp so that small
+// launches reach every SM was measured slower for 3-D grids of L = 70-90: the
+// per-CTA setup of grid constants and coefficient vectors grows with fewer
+// threads.)
 static int nd_threads(int L, long nlines)
 {
     int nt = (L <= 48) ? 128 : 64;

@@ -63,6 +63,31 @@ def extrapolate(result_l, x_l, fail_mag=10, extrap_log=False):
     return ex
 
 
+def _map_grids(fn, pts_l):
+    """fn over the grid sizes.  With a GPU, the grids run concurrently, each
+    on its own thread and CUDA stream: one integration of a few grids leaves
+    most SMs idle (a 3-D sweep at L = 70 is 77 CTAs), and the integrations of
+    different grids are independent.  The results are the same as one at a
+    time."""
+    if len(pts_l) < 2:
+        return [fn(p) for p in pts_l]
+    try:
+        import torch
+        gpu = torch.cuda.is_available()
+    except ImportError:
+        gpu = False
+    if not gpu:
+        return [fn(p) for p in pts_l]
+    from concurrent.futures import ThreadPoolExecutor
+    dev = torch.cuda.current_device()
+
+    def one(p):
+        with torch.cuda.device(dev), torch.cuda.stream(torch.cuda.Stream()):
+            return fn(p)
+    with ThreadPoolExecutor(max_workers=len(pts_l)) as ex:
+        return list(ex.map(one, pts_l))
+
+
 def make_extrap_func(func, extrap_x_l=None, extrap_log=False, fail_mag=10):
     """Version of func(params, ns, pts) taking a list of pts and returning the
     extrapolated result (dadi/Numerics.py:334-475).  x values come from the
@@ -77,7 +102,7 @@ def make_extrap_func(func, extrap_x_l=None, extrap_log=False, fail_mag=10):
         if np.isscalar(pts_l):
             pts_l = [pts_l]
         partial = functools.partial(func, *other_args, **kwargs)
-        result_l = list(map(partial, pts_l))
+        result_l = _map_grids(partial, pts_l)
         if no_extrap:
             return result_l
         if extrap_x_l is None:
