@@ -46,6 +46,7 @@ NINST = 4096
 BYTES_PER_PS = 16      # algorithmic HBM bytes per point-sweep (phi read + write)
 FLOPS_PER_PS = 30      # algorithmic FP64 flops per point-sweep (reference formulation)
 FP64_INSTR_PER_PS = 10  # FP64 pipe instructions per point-sweep in k_integrate2d
+K2_TRAFFIC_BYTES = 2.86e9 + 0.807e9  # ncu dram__bytes_read.sum + dram__bytes_write.sum
 
 
 def im_draws(n, seed):
@@ -350,12 +351,10 @@ def run_ours(a, world, rank, local):
     peak, src = load_peaks()
     kmean = float(np.mean(kern_ms)) / 1e3
     achieved = ps * BYTES_PER_PS / kmean / 1e9
-    traffic = None
-    tr_file = os.path.join(ROOT, "profiles", "traffic_integrate2d.json")
-    if os.path.exists(tr_file):
-        with open(tr_file) as fh:
-            tr = json.load(fh)
-        traffic = tr.get("bytes_per_point_sweep", 0) * ps
+    # DRAM bytes (read + write) of one k_integrate2d launch on this workload,
+    # from one ncu capture of the timed launch (1-pass metrics)
+    traffic = K2_TRAFFIC_BYTES if (NINST, PTS_L, NS) == (4096, (80, 90, 100), (40, 40)) \
+        else None
     fp64_achieved = ps * FLOPS_PER_PS / kmean / 1e12
     fp64_instr = ps * FP64_INSTR_PER_PS * 2 / kmean / 1e12
     fp64_peak = fp64_peak_measured
