@@ -97,6 +97,11 @@ def settings_from_globals(gam_placement=0):
     return _lib.settings_struct(tsf, otsf, old, delj, gam_placement)
 
 
+#: dgb_item2d (dadi_gb300.h): one (integration, grid) work item.
+ITEM2D_DTYPE = np.dtype([("L", "i4"), ("masks", "i4"), ("xx_off", "i8"), ("out_off", "i8"),
+                         ("sched", "i8")])
+
+
 def count_steps(rec, settings=None, max_steps=10 ** 8):
     """Steps each instance takes (host C, used to order work longest-first)."""
     rec = np.ascontiguousarray(rec, dtype=INST_DTYPE)
@@ -197,6 +202,52 @@ class Batch2D:
         for L in self.pts_l:
             phis.append(d_out[o:o + n * L * L].view(n, L, L))
             o += n * L * L
+        return phis, status
+
+    def integrate_from(self, rec, phi0s):
+        """integrate() with per-instance initial densities: phi0s[g] is an
+        (n, L_g, L_g) float64 CUDA tensor for grid g (e.g. phi_1D with each
+        instance's own selection, as the DFE models start from).  One
+        persistent launch over explicit work items (dgb_items2d_integrate).
+        Returns (per-grid phi tensors (n, L, L), status)."""
+        torch = self.torch
+        lib = _lib.lib()
+        n = len(rec)
+        ng = len(self.pts_l)
+        st = settings_from_globals(self.gam_placement)
+        rec = np.ascontiguousarray(rec)
+        d_rec = _lib.to_device(torch, rec.view(np.uint8), np.uint8)
+        table, off, cnt, status = self.schedule(d_rec, n)
+        blocks, o = [], 0
+        for L in self.pts_l:
+            blocks.append(o)
+            o += n * L * L
+        d_out = torch.empty(o, dtype=torch.float64, device="cuda")
+        for g, L in enumerate(self.pts_l):
+            assert tuple(phi0s[g].shape) == (n, L, L)
+            d_out[blocks[g]:blocks[g] + n * L * L].copy_(phi0s[g].reshape(-1))
+        masks = (rec["frozen"].astype(np.int32) & 0xff) | ((rec["nomut"].astype(np.int32) & 0xff) << 8)
+        items = np.zeros((n, ng), dtype=ITEM2D_DTYPE)
+        xo = np.cumsum([0] + self.pts_l[:-1])
+        idx = np.arange(n, dtype=np.int64)
+        for g, L in enumerate(self.pts_l):
+            items["L"][:, g] = L
+            items["masks"][:, g] = masks
+            items["xx_off"][:, g] = xo[g]
+            items["out_off"][:, g] = blocks[g] + idx * L * L
+            items["sched"][:, g] = idx * ng + g if st.use_old_timestep else idx
+        Lsq = torch.tensor([L * L for L in self.pts_l], dtype=torch.int64, device="cuda")
+        steps = cnt.to(torch.int64).view(n, -1)
+        cost = (steps * Lsq[None, :]).reshape(-1)
+        d_order = torch.argsort(-cost, stable=True).to(torch.int32)
+        d_items = _lib.to_device(torch, items.reshape(-1).view(np.uint8), np.uint8)
+        ws, nws = _lib.workspace(torch, lib.dgb_workspace_bytes(1, 2, max(self.pts_l), n * ng))
+        _lib.check(lib.dgb_items2d_integrate(
+            _lib.dptr(d_items), n * ng, max(self.pts_l), _lib.dptr(self.d_xx), _lib.dptr(d_out),
+            _lib.dptr(table), _lib.dptr(off), _lib.dptr(cnt), _lib.dptr(d_order),
+            ctypes.byref(st), 0, _lib.dptr(ws), nws, _lib.stream_handle(torch)),
+            "dgb_items2d_integrate")
+        phis = [d_out[b:b + n * L * L].view(n, L, L) for b, L in zip(blocks, self.pts_l)]
         return phis, status
 
     def loglik_and_grad(self, params, data, scale=1.0, ckpt_every=None, seeds=None, rec=None):

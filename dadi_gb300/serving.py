@@ -46,8 +46,7 @@ import numpy as np
 
 from . import _lib, batch, epilogue, models, numerics, phimanip, spectrum
 
-ITEM_DTYPE = np.dtype([("L", "i4"), ("masks", "i4"), ("xx_off", "i8"), ("out_off", "i8"),
-                       ("sched", "i8")])
+ITEM_DTYPE = batch.ITEM2D_DTYPE
 
 
 @dataclass

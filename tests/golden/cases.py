@@ -167,3 +167,9 @@ def im_draws(n=4096, seed=0):
 GROWTH3 = dict(params=((0.5, 1.0, 2.0), (5.0, 0.2, 10.0), (0.5, 1.5, 3.0), (-2.0, 0.0, 5.0),
                        0.15),
                ns=(20, 20, 20), pts_l=[70, 80, 90])
+
+
+#: A small two-population DFE cache (dadi.DFE.Cache2D with DemogSelModels.IM_sel)
+#: and its integration over a bivariate lognormal (dadi.DFE.PDFs.biv_lognormal).
+DFE = dict(params=(0.4, 1.5, 0.6, 0.1, 1.0, 0.5), ns=(6, 6), pts=[12, 16, 20], gamma_pts=3,
+           sel_params=(1.0, 2.0, 0.5), theta=1000.0)

@@ -216,6 +216,22 @@ def gen_grad(dadi, out):
     out["grad_godambe"] = np.asarray(dadi.Godambe.get_grad(func, p0, 1e-4)).ravel()
 
 
+def gen_dfe(dadi, out):
+    from dadi.DFE import Cache2D_mod, DemogSelModels, PDFs
+    d = cases.DFE
+    c = Cache2D_mod.Cache2D(d["params"], d["ns"], DemogSelModels.IM_sel, d["pts"],
+                            gamma_pts=d["gamma_pts"], cpus=1)
+    out["dfe_gammas"] = c.gammas
+    out["dfe_spectra"] = np.asarray(c.spectra)
+    fs = c.integrate(d["sel_params"], None, PDFs.biv_lognormal, d["theta"], None)
+    out["dfe_fs"] = np.asarray(fs.data)
+    fs = c.integrate(d["sel_params"], None, PDFs.biv_lognormal, d["theta"], None,
+                     exterior_int=False)
+    out["dfe_fs_interior"] = np.asarray(fs.data)
+    x = np.array([0.5, 3.0, 40.0])
+    out["dfe_pdf"] = PDFs.biv_lognormal(x, x, np.array(d["sel_params"]))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -224,7 +240,7 @@ def main():
     a = ap.parse_args()
     dadi = load_dadi(a.ref, a.build)
     for name, gen in [("integrate", gen_integrations), ("sweeps", gen_sweeps),
-                      ("host", gen_host), ("grad", gen_grad)]:
+                      ("host", gen_host), ("grad", gen_grad), ("dfe", gen_dfe)]:
         out = {}
         gen(dadi, out)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)

@@ -153,3 +153,33 @@ def test_table_dual_values_equal_build_table():
         fd = (a - b) / (2 * h)
         # finite-difference noise: an ulp of a table entry over 2h (~1e-9)
         assert np.allclose(drows[:, :, k], fd, rtol=1e-6, atol=1e-8)
+
+
+def _dfe_cache_from_golden(golden):
+    """A Cache2D holding the reference's own cached spectra."""
+    from dadi_gb300 import dfe
+    g = golden["dfe"]
+    c = dfe.Cache2D.__new__(dfe.Cache2D)
+    c.gammas = c.neg_gammas = g["dfe_gammas"]
+    c.spectra = g["dfe_spectra"]
+    return c
+
+
+def test_dfe_pdf_and_integrate_match_reference(golden):
+    """Cache2D.integrate (trapezoid over the gamma grid plus the quadrature of
+    the mass beyond it, dadi/DFE/Cache2D_mod.py:209-310) and the bivariate
+    lognormal (dadi/DFE/PDFs.py:41-76), on the reference's cached spectra,
+    against dadi's results."""
+    import cases
+    from dadi_gb300 import dfe
+    g = golden["dfe"]
+    d = cases.DFE
+    x = np.array([0.5, 3.0, 40.0])
+    assert np.allclose(dfe.biv_lognormal(x, x, np.array(d["sel_params"])), g["dfe_pdf"],
+                       rtol=1e-13, atol=0)
+    c = _dfe_cache_from_golden(golden)
+    fs = c.integrate(d["sel_params"], None, dfe.biv_lognormal, d["theta"], None)
+    assert np.allclose(np.asarray(fs.data), g["dfe_fs"], rtol=1e-12, atol=0)
+    fs = c.integrate(d["sel_params"], None, dfe.biv_lognormal, d["theta"], None,
+                     exterior_int=False)
+    assert np.allclose(np.asarray(fs.data), g["dfe_fs_interior"], rtol=1e-12, atol=0)
