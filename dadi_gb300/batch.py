@@ -250,17 +250,20 @@ class Batch2D:
         phis = [d_out[b:b + n * L * L].view(n, L, L) for b, L in zip(blocks, self.pts_l)]
         return phis, status
 
-    def loglik_and_grad(self, params, data, scale=1.0, ckpt_every=None, seeds=None, rec=None):
+    def loglik_and_grad(self, params, data, scale=1.0, ckpt_every=None, seeds=None, rec=None,
+                        mask=None, multinom=False):
         """Poisson log-likelihood of scale * (extrapolated IM spectrum) against
-        data for each parameter row, and its gradient with respect to
-        (s, nu1, nu2, T, m12, m21) by the discrete adjoint.  Returns CUDA
-        tensors (ll (n,), grad (n, 6), status (n,))."""
-        ll, ctx = self.forward_for_adjoint(params, data, scale, ckpt_every, seeds, rec)
+        data for each parameter row (or its multinomial form, see loglik), and
+        its gradient with respect to (s, nu1, nu2, T, m12, m21) by the
+        discrete adjoint.  Returns CUDA tensors (ll (n,), grad (n, 6),
+        status (n,))."""
+        ll, ctx = self.forward_for_adjoint(params, data, scale, ckpt_every, seeds, rec,
+                                           mask=mask, multinom=multinom)
         grad = self.adjoint(ctx, self.torch.ones_like(ll))
         return ll.detach(), grad, ctx["status"]
 
     def forward_for_adjoint(self, params, data, scale=1.0, ckpt_every=None, seeds=None,
-                            rec=None, tail_per_set=False):
+                            rec=None, tail_per_set=False, mask=None, multinom=False):
         """Forward pass that keeps what the adjoint needs: schedules,
         derivative rows, checkpoints and the differentiable tail (from_phi,
         extrapolation, likelihood) as a torch graph.  tail_per_set evaluates
@@ -320,12 +323,12 @@ class Batch2D:
                 for i in range(n):
                     fs_i = self.extrapolate(self.spectra([p[i:i + 1] for p in phis]))
                     fss.append(fs_i)
-                    lls.append(self.loglik(fs_i, d, scale))
+                    lls.append(self.loglik(fs_i, d, scale, mask, multinom))
                 fs = torch.cat(fss)
                 ll = torch.cat(lls)
             else:
                 fs = self.extrapolate(self.spectra(phis))
-                ll = self.loglik(fs, d, scale)
+                ll = self.loglik(fs, d, scale, mask, multinom)
         ctx = dict(phis=phis, ll=ll, fs=fs.detach(), table=table, off=off, cnt=cnt, drows=drows, ckpt=ckpt,
                    ck_off=ck_off, C=C, masks=d_masks, order=d_order, status=status, n=n, st=st)
         return ll, ctx
@@ -378,13 +381,22 @@ class Batch2D:
         failed = torch.abs(torch.log10(ex / best)) > fail_mag
         return torch.where(failed, best, ex)
 
-    def loglik(self, fs, data, scale=1.0):
-        """Poisson log-likelihood of scale*fs against data over unmasked entries
-        with positive model (dadi/Inference.py:466-509); shape (n,)."""
+    def loglik(self, fs, data, scale=1.0, mask=None, multinom=False):
+        """Poisson log-likelihood of scale*fs against data over entries
+        unmasked (the corners, or `mask`, a boolean array: True = masked) with
+        positive model (dadi/Inference.py:466-509); shape (n,).  multinom:
+        the multinomial form, scale = sum(data)/sum(fs) over unmasked entries
+        for each spectrum (ll_multinom, :559-575 with optimal_sfs_scaling,
+        :668-685), kept inside the autograd graph."""
         torch = self.torch
-        model = scale * fs
         d = data if torch.is_tensor(data) else _lib.to_device(torch, data)
-        ok = (~torch.from_numpy(self.mask).to(model.device)) & (model > 0)
+        m = self.mask if mask is None else (np.asarray(mask, dtype=bool) | self.mask)
+        um = ~torch.from_numpy(m).to(fs.device)
+        if multinom:
+            scale = (d * um).sum() / (fs * um).sum(dim=(1, 2))
+            scale = scale[:, None, None]
+        model = scale * fs
+        ok = um & (model > 0)
         term = -model + d * torch.log(torch.where(ok, model, torch.ones_like(model))) \
             - torch.lgamma(d + 1.0)
         return torch.where(ok, term, torch.zeros_like(term)).sum(dim=(1, 2))
