@@ -144,12 +144,27 @@ def barrier(world):
 
 
 def max_over_ranks(torch, world, x):
+    """The largest x over the ranks (the job's time is its slowest rank's)."""
     if world == 1:
         return x
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_draws(rank):
+    """Rank r integrates its own 4096 instances, drawn like the workload's
+    with seed r (weak scaling: per-GPU work is fixed as ranks are added;
+    ranks exchange nothing but the timing)."""
+    return im_draws(NINST, rank)
+
+
+def job_value(world, ms_per_step):
+    """Whole-job spectra/s: every rank's instances over the slowest rank's
+    step time."""
+    return world * NINST / (ms_per_step / 1e3)
 
 
 def point_sweeps(steps, pts_l):
@@ -239,7 +254,7 @@ def run_ours(a, world, rank, local):
     torch.cuda.set_device(local)
     from dadi_gb300 import batch, build
     build.build()
-    draws = im_draws(NINST, rank)
+    draws = replica_draws(rank)
     rec = batch.im_instances(draws)
     steps = batch.count_steps(rec)   # host walk of the same schedules: point-sweep count
     ps = point_sweeps(steps, PTS_L)
@@ -295,7 +310,7 @@ def run_ours(a, world, rank, local):
     clk = clocks.stop()
     total_ms = max_over_ranks(torch, world, total_ms)
     ms_per_step = total_ms / a.steps
-    value = world * NINST / (ms_per_step / 1e3)
+    value = job_value(world, ms_per_step)
     bad = int((status != 0).sum())
 
     # end to end through the public API (host arrays in and out)
