@@ -259,6 +259,11 @@ def run_ours(a, world, rank, local):
     steps = batch.count_steps(rec)   # host walk of the same schedules: point-sweep count
     ps = point_sweeps(steps, PTS_L)
     eng = batch.Batch2D(PTS_L, NS, gam_placement=a.gam)
+    tuned = None
+    if a.gam == 0 and not a.no_tune:
+        # launch configuration chosen by timing the candidates on a sample
+        from dadi_gb300 import autotune
+        tuned = autotune.tune_batch2d(eng, rec)
     # synthetic observed data: Poisson(5e4 * model(set 0)), as a device tensor
     fs0, _, _ = eng.run(im_draws(1, 0))
     obs = np.random.default_rng(0).poisson(5e4 * fs0.cpu().numpy()[0]).astype(np.float64)
@@ -333,18 +338,29 @@ def run_ours(a, world, rank, local):
     plain = None
     if rank == 0 and not a.no_plain:
         from dadi_gb300 import models, numerics
-        f = numerics.make_extrap_func(models.IM)
         rng = np.random.default_rng(7)
         sample = [i for i in rng.permutation(NINST) if 500 <= steps[i] <= 3000][:3]
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for i in sample:
-            f(draws[i], NS, list(PTS_L))
-        wall = time.perf_counter() - t0
         sps = point_sweeps(steps[sample], PTS_L)
-        plain = {"value": NINST * (sps / wall) / ps, "unit": "spectra/s",
-                 "sample": "%d seed-0 instances through the one-at-a-time drop-in "
-                           "(two_pops per grid), scaled by point-sweeps" % len(sample)}
+
+        def one_at_a_time(p):
+            # as dadi's make_extrap_func runs it: the grids one after another
+            res = [models.IM(p, NS, L) for L in PTS_L]
+            return numerics.extrapolate(res, [r.extrap_x for r in res])
+        concurrent = numerics.make_extrap_func(models.IM)  # the grids on three streams
+        rates = {}
+        for name, f in (("seq", one_at_a_time),
+                        ("conc", lambda p: concurrent(p, NS, list(PTS_L)))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for i in sample:
+                f(draws[i])
+            rates[name] = NINST * (sps / (time.perf_counter() - t0)) / ps
+        plain = {"value": rates["seq"], "unit": "spectra/s",
+                 "concurrent_grids_value": rates["conc"],
+                 "sample": "%d seed-0 instances through the drop-in one at a time (two_pops "
+                           "per grid, grids in sequence as dadi's make_extrap_func runs them; "
+                           "concurrent_grids_value: the three grids on three streams), "
+                           "scaled by point-sweeps" % len(sample)}
 
     # CPU baseline (oracle restatement, bounded sample), rank 0 only
     cpu = None
@@ -384,7 +400,11 @@ def run_ours(a, world, rank, local):
                    "global_batch": NINST * world, "pts_l": list(PTS_L), "ns": list(NS),
                    "point_sweeps_per_step": ps, "parallelism": "replicas x%d" % world,
                    "l2": "flushed between iterations (256 MB write); phi outputs 803 MB > L2",
-                   "gam_placement": a.gam},
+                   "gam_placement": eng.gam_placement, "launch_mode": eng.launch_mode},
+        "autotune": None if tuned is None else {
+            "choice": list(tuned["choice"]), "sample_instances": tuned["sample"],
+            "ms": {"%s/%s" % (m, "shared" if g == 1 else "workspace"): v
+                   for (m, g), v in tuned["ms"].items()}},
         "e2e": {"value": e2e_value, "unit": "spectra/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -574,6 +594,8 @@ def main():
     ap.add_argument("--gam", type=int, default=0, help="0 auto, 1 shared, 2 workspace")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the launch-configuration autotuner (use --gam's placement)")
     ap.add_argument("--clock-ms", type=int, default=500,
                     help="nvidia-smi sampling period during the timed region (0: off)")
     ap.add_argument("--serve", type=int, default=600,

@@ -130,6 +130,7 @@ class Batch2D:
         self.ns = tuple(ns)
         self.max_steps = int(max_steps)
         self.gam_placement = gam_placement
+        self.launch_mode = "persistent"
         self.xxs = [numerics.default_grid(p) for p in self.pts_l]
         phi0 = [phimanip.phi_1D_to_2D(xx, phimanip.phi_1D(xx)) for xx in self.xxs]
         self.d_xx = _lib.to_device(torch, np.concatenate(self.xxs))
@@ -168,8 +169,17 @@ class Batch2D:
         """Run the integrations of dgb_inst2d records `rec` (host structured
         array).  Returns (list of per-grid phi tensors (n, L, L), status).
         timer: optional pair of CUDA events recorded around the integration
-        kernel alone."""
+        kernel alone.  The launch follows self.launch_mode ("persistent": a
+        device-sized grid pulling work items from a queue; "one_per_cta": one
+        CTA per item) and self.gam_placement (0 auto, 1 shared memory, 2
+        workspace), the knobs autotune.tune_batch2d chooses."""
         torch = self.torch
+        if self.launch_mode == "one_per_cta":
+            n = len(rec)
+            phi0s = [self.d_phi0[o:o + L * L].view(1, L, L).expand(n, L, L)
+                     for o, L in zip(np.cumsum([0] + [L * L for L in self.pts_l[:-1]]),
+                                     self.pts_l)]
+            return self.integrate_from(rec, phi0s, one_per_cta=True, timer=timer)
         n = len(rec)
         ng = len(self.pts_l)
         st = settings_from_globals(self.gam_placement)
@@ -204,12 +214,13 @@ class Batch2D:
             o += n * L * L
         return phis, status
 
-    def integrate_from(self, rec, phi0s):
+    def integrate_from(self, rec, phi0s, one_per_cta=False, timer=None):
         """integrate() with per-instance initial densities: phi0s[g] is an
         (n, L_g, L_g) float64 CUDA tensor for grid g (e.g. phi_1D with each
-        instance's own selection, as the DFE models start from).  One
-        persistent launch over explicit work items (dgb_items2d_integrate).
-        Returns (per-grid phi tensors (n, L, L), status)."""
+        instance's own selection, as the DFE models start from).  One launch
+        over explicit work items (dgb_items2d_integrate): persistent, or with
+        one_per_cta one CTA per item.  Returns (per-grid phi tensors (n, L,
+        L), status)."""
         torch = self.torch
         lib = _lib.lib()
         n = len(rec)
@@ -225,7 +236,7 @@ class Batch2D:
         d_out = torch.empty(o, dtype=torch.float64, device="cuda")
         for g, L in enumerate(self.pts_l):
             assert tuple(phi0s[g].shape) == (n, L, L)
-            d_out[blocks[g]:blocks[g] + n * L * L].copy_(phi0s[g].reshape(-1))
+            d_out[blocks[g]:blocks[g] + n * L * L].view(n, L, L).copy_(phi0s[g])
         masks = (rec["frozen"].astype(np.int32) & 0xff) | ((rec["nomut"].astype(np.int32) & 0xff) << 8)
         items = np.zeros((n, ng), dtype=ITEM2D_DTYPE)
         xo = np.cumsum([0] + self.pts_l[:-1])
@@ -241,12 +252,22 @@ class Batch2D:
         cost = (steps * Lsq[None, :]).reshape(-1)
         d_order = torch.argsort(-cost, stable=True).to(torch.int32)
         d_items = _lib.to_device(torch, items.reshape(-1).view(np.uint8), np.uint8)
-        ws, nws = _lib.workspace(torch, lib.dgb_workspace_bytes(1, 2, max(self.pts_l), n * ng))
-        _lib.check(lib.dgb_items2d_integrate(
-            _lib.dptr(d_items), n * ng, max(self.pts_l), _lib.dptr(self.d_xx), _lib.dptr(d_out),
+        Lmax = max(self.pts_l)
+        if one_per_cta:
+            nws = lib.dgb_workspace_bytes(3, 2, Lmax, n * ng)
+        else:
+            nws = lib.dgb_workspace_bytes(1, 2, Lmax, n * ng)
+        ws, nws = _lib.workspace(torch, nws)
+        if timer is not None:
+            timer[0].record()
+        rc = lib.dgb_items2d_integrate(
+            _lib.dptr(d_items), n * ng, Lmax, _lib.dptr(self.d_xx), _lib.dptr(d_out),
             _lib.dptr(table), _lib.dptr(off), _lib.dptr(cnt), _lib.dptr(d_order),
-            ctypes.byref(st), 0, _lib.dptr(ws), nws, _lib.stream_handle(torch)),
-            "dgb_items2d_integrate")
+            ctypes.byref(st), int(bool(one_per_cta)), _lib.dptr(ws), nws,
+            _lib.stream_handle(torch))
+        if timer is not None:
+            timer[1].record()
+        _lib.check(rc, "dgb_items2d_integrate")
         phis = [d_out[b:b + n * L * L].view(n, L, L) for b, L in zip(blocks, self.pts_l)]
         return phis, status
 

@@ -541,11 +541,13 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     int occ_g = k2_occupancy(A.use_delj, bytes_g + sizeof(K2Shared));
     size_t slice = (size_t)Lmax * Lmax * sizeof(double);
     int max_g_blocks = (int)std::min<size_t>((ws_bytes - 256) / slice, (size_t)nsm * occ_g);
-    // gam in shared memory whenever it fits: measured on the 4096-instance IM
-    // batch at pts 80/90/100 it beats two CTAs per SM with gam in L2 (17.8 s
-    // vs 18.9 s), the FP64 pipe being saturated by one warp per SMSP
-    bool use_s = fit_s;
-    (void)occ_s;
+    // auto: gam in shared memory only when that does not cost CTAs per SM.
+    // Measured on the 4096-instance IM batch at pts 80/90/100: gam in the
+    // workspace (two CTAs per SM at L = 100, two warps per SMSP) 13.44 s,
+    // gam in shared memory (one CTA per SM) 17.11 s; the back substitution
+    // prefetches its L2 operands, and the second warp per SMSP fills the FP64
+    // pipe's dependency gaps.
+    bool use_s = fit_s && occ_s >= occ_g;
     if (settings->gam_placement == 1) {
         if (!fit_s)
             return DGB_ERR_UNSUPPORTED;
@@ -727,6 +729,16 @@ extern "C" int dgb_items2d_integrate(const dgb_item2d *items, int nitems, int Lm
     bool fit_s = k2_smem_fits(Lmax, true, A.use_delj, &bytes_s);
     if (!k2_smem_fits(Lmax, false, A.use_delj, &bytes_g))
         return DGB_ERR_UNSUPPORTED;
+    // gam placement: 0 shared memory when it fits, 1 shared (must fit),
+    // 2 the workspace
+    if (settings->gam_placement == 1 && !fit_s)
+        return DGB_ERR_UNSUPPORTED;
+    if (settings->gam_placement == 2)
+        fit_s = false;
+    else if (settings->gam_placement == 0 && fit_s &&
+             k2_occupancy(A.use_delj, bytes_s + sizeof(K2Shared)) <
+                 k2_occupancy(A.use_delj, bytes_g + sizeof(K2Shared)))
+        fit_s = false; // as in k2_batch: shared memory only if it costs no CTAs per SM
     int nsm = k2_num_sms();
     int nblocks;
     size_t smem;

@@ -245,11 +245,8 @@ extern "C" size_t dgb_workspace_bytes(int kind, int ndim, int L, long n)
         return k2_batch_ws_bytes(L, n);
     if (kind == 2)
         return (size_t)n * L * sizeof(double);
-    if (kind == 3) {
-        size_t b = 0;
-        bool fit = k2_smem_fits(L, true, false, &b) && k2_smem_fits(L, true, true, &b);
-        return 256 + (fit ? 0 : (size_t)n * L * L * sizeof(double));
-    }
+    if (kind == 3) // any gam placement: a slice per work item
+        return 256 + (size_t)n * L * L * sizeof(double);
     return 0;
 }
 

@@ -241,7 +241,10 @@ typedef struct {
  * a persistent launch sized to the device whose CTAs pull items from a queue
  * (ws from dgb_workspace_bytes kind 1); one_per_cta = 1: one CTA per item,
  * each retiring after its item, so launches on other streams take SMs as
- * soon as any CTA finishes (ws from kind 3 with n = nitems). */
+ * soon as any CTA finishes (ws from kind 3 with n = nitems).
+ * settings->gam_placement: 0 Thomas scratch in shared memory when it fits
+ * and costs no CTAs per SM, else the workspace; 1 shared memory
+ * (DGB_ERR_UNSUPPORTED if it does not fit); 2 the workspace. */
 int dgb_items2d_integrate(const dgb_item2d *items, int nitems, int Lmax, const double *xx_all,
                           double *phi_out, const double *table, const long *row_off,
                           const int *row_cnt, const int *order, const dgb_settings *settings,
