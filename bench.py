@@ -46,7 +46,7 @@ NINST = 4096
 BYTES_PER_PS = 16      # algorithmic HBM bytes per point-sweep (phi read + write)
 FLOPS_PER_PS = 30      # algorithmic FP64 flops per point-sweep (reference formulation)
 FP64_INSTR_PER_PS = 10  # FP64 pipe instructions per point-sweep in k_integrate2d
-K2_TRAFFIC_BYTES = 2.86e9 + 0.807e9  # ncu dram__bytes_read.sum + dram__bytes_write.sum
+K2_TRAFFIC_BYTES = 2.89e9 + 0.886e9  # ncu dram__bytes_read.sum + dram__bytes_write.sum
 
 
 def im_draws(n, seed):
