@@ -131,6 +131,7 @@ class Batch2D:
         self.max_steps = int(max_steps)
         self.gam_placement = gam_placement
         self.launch_mode = "persistent"
+        self.adjoint_ctas_per_sm = None  # None: sized to L2 (see adjoint)
         self.xxs = [numerics.default_grid(p) for p in self.pts_l]
         phi0 = [phimanip.phi_1D_to_2D(xx, phimanip.phi_1D(xx)) for xx in self.xxs]
         self.d_xx = _lib.to_device(torch, np.concatenate(self.xxs))
@@ -368,7 +369,18 @@ class Batch2D:
         C = ctx["C"]
         Lmax = max(self.pts_l)
         per_cta = lib.dgb_adjoint2d_scratch_bytes(Lmax, C, 1)
-        nblocks = min(n * ng, torch.cuda.get_device_properties(0).multi_processor_count * 2)
+        props = torch.cuda.get_device_properties(torch.cuda.current_device())
+        nsm = props.multi_processor_count
+        per_sm = self.adjoint_ctas_per_sm
+        if per_sm is None:
+            # each CTA streams ~5 L^2 arrays per step backwards through L2
+            # (segment state, chi, the next state, lambda, gam): keep the CTAs'
+            # per-step working set within 3/4 of L2.  Measured at pts
+            # 100/110/120 (256 sets): 1 CTA per SM 11.9 s, 2: 16.9 s, 3: 21.8 s.
+            l2 = getattr(props, "L2_cache_size", 0) or (96 << 20)
+            per_sm = int(0.75 * l2 // (nsm * 5 * Lmax * Lmax * 8))
+            per_sm = max(1, min(4, per_sm))
+        nblocks = min(n * ng, nsm * per_sm)
         ws, nws = _lib.workspace(torch, 256 + per_cta * nblocks)
         st = ctx["st"]
         _lib.check(lib.dgb_adjoint2d(
