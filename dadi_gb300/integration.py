@@ -128,17 +128,40 @@ def build_table(P, xx, T, initial_t, nu_f, mig_f, gamma_f, h_f, theta0_f, beta_f
     return table, hist
 
 
+def on_device(phi):
+    """True for a CUDA torch tensor: the integrators then keep the density on
+    the device (a new CUDA tensor is returned), so models chaining epochs and
+    splits never copy it to the host in between."""
+    return hasattr(phi, "is_cuda") and bool(phi.is_cuda)
+
+
+def _copy_in(phi):
+    """A new array to integrate: a host copy, or a device copy of a CUDA
+    tensor (float64, contiguous)."""
+    if on_device(phi):
+        import torch
+        return phi.detach().to(torch.float64).contiguous().clone()
+    return np.array(phi, dtype=np.float64, copy=True)
+
+
+def _device_phi(torch, phi):
+    """(device tensor to integrate in place, whether the caller gave one)."""
+    if on_device(phi):
+        return phi.detach().to(torch.float64).contiguous().clone(), True
+    return _lib.to_device(torch, np.ascontiguousarray(phi, dtype=np.float64)), False
+
+
 def run_table(phi, xx, table, frozen_mask=0, nomut_mask=0):
-    """Integrate phi (host ndarray) through a parameter table on the GPU;
-    returns a new host ndarray."""
+    """Integrate phi (host ndarray, or CUDA tensor kept on the device)
+    through a parameter table on the GPU; returns a new array of the same
+    kind."""
     torch = _lib.require_cuda()
-    phi = np.ascontiguousarray(phi, dtype=np.float64)
     P, L = phi.ndim, phi.shape[0]
     if any(s != L for s in phi.shape) or len(xx) != L:
         raise ValueError("phi must be square with len(xx) points per axis")
     if len(table) == 0:
-        return phi.copy()
-    d_phi = _lib.to_device(torch, phi)
+        return _copy_in(phi)
+    d_phi, dev = _device_phi(torch, phi)
     d_xx = _lib.to_device(torch, xx)
     d_tab = _lib.to_device(torch, table)
     ws, nws = _lib.workspace(torch, _lib.lib().dgb_workspace_bytes(0, P, L, 0))
@@ -147,7 +170,7 @@ def run_table(phi, xx, table, frozen_mask=0, nomut_mask=0):
                                         len(table), int(frozen_mask), int(nomut_mask), int(delj),
                                         _lib.dptr(ws), nws, _lib.stream_handle(torch))
     _lib.check(rc, "dgb_integrate_table")
-    return _lib.to_host(torch, d_phi)
+    return d_phi if dev else _lib.to_host(torch, d_phi)
 
 
 def step_lengths(dt, T, initial_t):
@@ -163,13 +186,13 @@ def step_lengths(dt, T, initial_t):
 
 
 def run_precalc(phi, xx, abc, dts, theta0, frozen_mask=0, nomut_mask=0):
-    """Constant-coefficient loop on the GPU (abc: 3*P arrays shaped like phi)."""
+    """Constant-coefficient loop on the GPU (abc: 3*P arrays shaped like phi);
+    phi a host ndarray or a CUDA tensor (kept on the device)."""
     torch = _lib.require_cuda()
-    phi = np.ascontiguousarray(phi, dtype=np.float64)
     P, L = phi.ndim, phi.shape[0]
     if len(dts) == 0:
-        return phi.copy()
-    d_phi = _lib.to_device(torch, phi)
+        return _copy_in(phi)
+    d_phi, dev = _device_phi(torch, phi)
     d_xx = _lib.to_device(torch, xx)
     d_abc = _lib.to_device(torch, np.stack([np.asarray(v, dtype=np.float64) for v in abc]))
     d_dts = _lib.to_device(torch, dts)
@@ -179,7 +202,7 @@ def run_precalc(phi, xx, abc, dts, theta0, frozen_mask=0, nomut_mask=0):
                                           int(frozen_mask), int(nomut_mask), _lib.dptr(ws), nws,
                                           _lib.stream_handle(torch))
     _lib.check(rc, "dgb_integrate_precalc")
-    return _lib.to_host(torch, d_phi)
+    return d_phi if dev else _lib.to_host(torch, d_phi)
 
 
 # -------------------------------------------------- constant-coefficient build
@@ -265,7 +288,7 @@ def _masks(flags):
 def one_pop(phi, xx, T, nu=1, gamma=0, h=0.5, theta0=1.0, initial_t=0, frozen=False, beta=1,
             deme_ids=None):
     """dadi/Integration.py:178-258 on the GPU (temporal loop for all inputs)."""
-    phi = np.array(phi, dtype=np.float64, copy=True)
+    phi = _copy_in(phi)
     if frozen or T - initial_t == 0:
         return phi
     _check_T(T, initial_t)
@@ -314,7 +337,7 @@ def two_pops(phi, xx, T, nu1=1, nu2=1, m12=0, m21=0, gamma1=0, gamma2=0, h1=0.5,
              theta0=1, initial_t=0, frozen1=False, frozen2=False, nomut1=False, nomut2=False,
              enable_cuda_cached=False, deme_ids=None):
     """dadi/Integration.py:260-387 on the GPU; returns a new array."""
-    phi = np.array(phi, dtype=np.float64, copy=True)
+    phi = _copy_in(phi)
     if T - initial_t == 0:
         return phi
     _check_T(T, initial_t)
@@ -328,7 +351,7 @@ def three_pops(phi, xx, T, nu1=1, nu2=1, nu3=1, m12=0, m13=0, m21=0, m23=0, m31=
                frozen1=False, frozen2=False, frozen3=False, enable_cuda_cached=False,
                deme_ids=None):
     """dadi/Integration.py:389-554 on the GPU; returns a new array."""
-    phi = np.array(phi, dtype=np.float64, copy=True)
+    phi = _copy_in(phi)
     if T - initial_t == 0:
         return phi
     _check_T(T, initial_t)
@@ -348,7 +371,7 @@ def five_pops(phi, xx, T, nu1=1, nu2=1, nu3=1, nu4=1, nu5=1,
               frozen3=False, frozen4=False, frozen5=False, deme_ids=None):
     """dadi/Integration.py:729-937 on the GPU; returns a new array (the
     reference's CPU path updates phi in place)."""
-    phi = np.array(phi, dtype=np.float64, copy=True)
+    phi = _copy_in(phi)
     if T - initial_t == 0:
         return phi
     _check_T(T, initial_t)
@@ -365,7 +388,7 @@ def four_pops(phi, xx, T, nu1=1, nu2=1, nu3=1, nu4=1, m12=0, m13=0, m14=0, m21=0
               frozen2=False, frozen3=False, frozen4=False, deme_ids=None):
     """dadi/Integration.py:556-727 on the GPU.  Like the reference's CUDA path
     this returns a new array (the reference's CPU path updates phi in place)."""
-    phi = np.array(phi, dtype=np.float64, copy=True)
+    phi = _copy_in(phi)
     if T - initial_t == 0:
         return phi
     _check_T(T, initial_t)

@@ -84,18 +84,34 @@ def check_xx(xx):
         raise ValueError('Input xx argument is not monotonically increasing.')
 
 
+def _is_cuda(a):
+    return hasattr(a, "is_cuda") and bool(a.is_cuda)
+
+
 def phi_1D_to_2D(xx, phi_1D, deme_ids=None):
-    """One-to-two split: mass on the diagonal (dadi/PhiManip.py:214-234)."""
+    """One-to-two split: mass on the diagonal (dadi/PhiManip.py:214-234).
+    A CUDA tensor phi_1D gives a CUDA tensor (the same arithmetic, on the
+    device)."""
     check_xx(xx)
     pts = len(xx)
-    phi_2D = np.zeros((pts, pts))
     idx = np.arange(1, pts - 1)
+    if _is_cuda(phi_1D):
+        import torch
+        dev = phi_1D.device
+        out = torch.zeros((pts, pts), dtype=torch.float64, device=dev)
+        den = torch.from_numpy(np.ascontiguousarray(xx[2:] - xx[:-2])).to(dev)
+        ti = torch.from_numpy(idx).to(dev)
+        out[ti, ti] = phi_1D[1:-1].to(torch.float64) * 2 / den
+        return out
+    phi_2D = np.zeros((pts, pts))
     phi_2D[idx, idx] = phi_1D[1:-1] * 2 / (xx[2:] - xx[:-2])
     return phi_2D
 
 
 def _admixture_intermediates(phi, ad_z, zz):
-    """Linear placement of admixed frequencies on zz (dadi/PhiManip.py:268-301)."""
+    """Linear placement of admixed frequencies on zz (dadi/PhiManip.py:268-301).
+    The placement depends only on the grids; with a CUDA tensor phi the
+    normalisation and the returned weights are device tensors."""
     upper = np.searchsorted(zz, ad_z)
     upper = np.minimum(upper, len(zz) - 1)
     upper = np.maximum(upper, 1)
@@ -106,20 +122,42 @@ def _admixture_intermediates(phi, ad_z, zz):
     delz2 = np.where(upper == len(zz) - 1, 0, zz[(upper + 1) % len(zz)] - zz[upper])
     frac_lower = (uz - ad_z) / (uz - lz)
     frac_upper = (ad_z - lz) / (uz - lz)
-    norm = 2 * phi / (frac_lower * delz0 + delz1 + frac_upper * delz2)
+    den = frac_lower * delz0 + delz1 + frac_upper * delz2
+    if _is_cuda(phi):
+        import torch
+        dev = phi.device
+        t = [torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+             for a in (lower, upper, frac_lower, frac_upper, den)]
+        lower, upper, frac_lower, frac_upper, den = t
+        return lower, upper, frac_lower, frac_upper, 2 * phi.to(torch.float64) / den
+    norm = 2 * phi / den
     return lower, upper, frac_lower, frac_upper, norm
+
+
+def _place(shape, lo, up, fl, fu, norm, like):
+    """out[..., lo] = fl * norm; out[..., up] += fu * norm over the leading
+    axes (host arrays or device tensors, as `like`)."""
+    lead = [np.arange(n).reshape([-1 if k == j else 1 for k in range(len(shape) - 1)])
+            for j, n in enumerate(shape[:-1])]
+    if _is_cuda(like):
+        import torch
+        dev = like.device
+        out = torch.zeros(shape, dtype=torch.float64, device=dev)
+        lead = [torch.from_numpy(a).to(dev) for a in lead]
+        out[(*lead, lo)] = fl * norm
+        out[(*lead, up)] += fu * norm
+        return out
+    out = np.zeros(shape)
+    out[(*lead, lo)] = fl * norm
+    out[(*lead, up)] += fu * norm
+    return out
 
 
 def phi_2D_to_3D_admix(phi, f1, xx, yy, zz, deme_ids=None):
     """Population 3 admixed from 1 and 2 (dadi/PhiManip.py:372-409)."""
     ad_z = f1 * xx[:, None] + (1 - f1) * yy[None, :]
     lo, up, fl, fu, norm = _admixture_intermediates(phi, ad_z, zz)
-    ii = np.arange(len(xx))[:, None]
-    jj = np.arange(len(yy))[None, :]
-    out = np.zeros((len(xx), len(yy), len(zz)))
-    out[ii, jj, lo] = fl * norm
-    out[ii, jj, up] += fu * norm
-    return out
+    return _place((len(xx), len(yy), len(zz)), lo, up, fl, fu, norm, phi)
 
 
 def phi_2D_to_3D_split_2(xx, phi_2D, deme_ids=None):
@@ -138,10 +176,17 @@ def phi_3D_to_4D(phi, f1, f2, xx, yy, zz, aa, deme_ids=None):
     """Population 4 from 1, 2 and 3 (dadi/PhiManip.py:412-450)."""
     ad_w = f1 * xx[:, None, None] + f2 * yy[None, :, None] + (1 - f1 - f2) * zz[None, None, :]
     lo, up, fl, fu, norm = _admixture_intermediates(phi, ad_w, aa)
-    ii = np.arange(len(xx))[:, None, None]
-    jj = np.arange(len(yy))[None, :, None]
-    kk = np.arange(len(zz))[None, None, :]
-    out = np.zeros((len(xx), len(yy), len(zz), len(aa)))
-    out[ii, jj, kk, lo] = fl * norm
-    out[ii, jj, kk, up] += fu * norm
-    return out
+    return _place((len(xx), len(yy), len(zz), len(aa)), lo, up, fl, fu, norm, phi)
+
+
+def phi_4D_to_5D(phi, f1, f2, f3, xx, yy, zz, aa, bb, deme_ids=None):
+    """Population 5 from populations 1-4 (dadi/PhiManip.py:453-490, with
+    _four_pop_admixture_intermediates :333-352)."""
+    if f1 + f2 + f3 > 1:
+        raise ValueError('Admixture proportions (f1=%f, f2 = %f, f3=%f) are '
+                         'non-sensible.' % (f1, f2, f3))
+    ad_w = f1 * xx[:, None, None, None] + f2 * yy[None, :, None, None] \
+        + f3 * zz[None, None, :, None] + (1 - f1 - f2 - f3) * aa[None, None, None, :]
+    lo, up, fl, fu, norm = _admixture_intermediates(phi, ad_w, bb)
+    return _place((len(xx), len(yy), len(zz), len(aa), len(bb)), lo, up, fl, fu, norm, phi)
+

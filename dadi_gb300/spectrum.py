@@ -108,9 +108,56 @@ def _from_phi_4D(nx, ny, nz, na, xx, yy, zz, aa, phi):
     return data
 
 
+def _from_phi_5D(nx, ny, nz, na, nb, xx, yy, zz, aa, bb, phi):
+    data = np.zeros((nx + 1, ny + 1, nz + 1, na + 1, nb + 1))
+    d1b, d2b = dbeta_tables(nb, bb)
+    s_bb = (phi[..., 1:] - phi[..., :-1]) / (bb[1:] - bb[:-1])
+    c1_bb = (phi[..., :-1] - s_bb * bb[:-1]) / (nb + 1)
+    for mm in range(nb + 1):
+        t1 = np.dot(c1_bb, d1b[mm])
+        t2 = np.dot(s_bb, d2b[mm])
+        t2 *= (mm + 1) / ((nb + 1) * (nb + 2))
+        data[..., mm] = _from_phi_4D(nx, ny, nz, na, xx, yy, zz, aa, t1 + t2)
+    return data
+
+
+def _from_phi_device(phi, ns, xxs):
+    """Raw spectrum of a CUDA-tensor density: two populations on one grid
+    through the device epilogue, three through the batched torch contraction;
+    the spectrum (not the density) comes back to the host."""
+    import torch
+    from . import _lib
+    P = phi.dim()
+    same = all(np.array_equal(xxs[0], x) for x in xxs[1:])
+    if P == 2 and same:
+        from . import epilogue
+        fs, _, _ = epilogue.spectra_2d(torch, [([phi.to(torch.float64).contiguous()],
+                                                [np.asarray(xxs[0], dtype=np.float64)],
+                                                tuple(ns), None, 1.0)])
+        return _lib.to_host(torch, fs[0])
+    if P == 3 and same:
+        from . import adjoint_nd
+        with torch.no_grad():
+            fs = adjoint_nd.from_phi_torch(torch, phi.to(torch.float64).contiguous(), ns,
+                                           np.asarray(xxs[0], dtype=np.float64))
+        return _lib.to_host(torch, fs)
+    return None
+
+
 def from_phi(phi, ns, xxs, mask_corners=True, pop_ids=None):
-    """Spectrum of sample sizes ns from phi on grids xxs (1-4 populations,
-    the linear-algebra paths of dadi/Spectrum_mod.py:1938-2061)."""
+    """Spectrum of sample sizes ns from phi on grids xxs (1-5 populations,
+    the linear-algebra paths of dadi/Spectrum_mod.py:1938-2061).  phi may be
+    a CUDA tensor (a density kept on the device): 2-D and 3-D spectra are
+    then computed there."""
+    if hasattr(phi, "is_cuda") and phi.is_cuda:
+        if not phi.dim() == len(ns) == len(xxs):
+            raise ValueError('Dimensionality of phi and lengths of ns and xxs do not all '
+                             'agree.')
+        data = _from_phi_device(phi, ns, xxs)
+        if data is not None:
+            return Spectrum(data, mask_corners=mask_corners, extrap_x=xxs[0][1],
+                            pop_ids=pop_ids)
+        phi = phi.detach().cpu().numpy()
     phi = np.asarray(phi)
     if not phi.ndim == len(ns) == len(xxs):
         raise ValueError('Dimensionality of phi and lengths of ns and xxs do not all agree.')
@@ -123,8 +170,10 @@ def from_phi(phi, ns, xxs, mask_corners=True, pop_ids=None):
         data = _from_phi_3D(*ns, *xxs, phi)
     elif P == 4:
         data = _from_phi_4D(*ns, *xxs, phi)
+    elif P == 5:
+        data = _from_phi_5D(*ns, *xxs, phi)
     else:
-        raise ValueError('Only implemented for dimensions 1-4.')
+        raise ValueError('Only implemented for dimensions 1-5.')
     return Spectrum(data, mask_corners=mask_corners, extrap_x=xxs[0][1], pop_ids=pop_ids)
 
 

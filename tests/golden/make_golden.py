@@ -126,11 +126,16 @@ def gen_host(dadi, out):
     phi3 = PM.phi_2D_to_3D_split_2(xs, PM.phi_1D_to_2D(xs, PM.phi_1D(xs)))
     out["phi3d_split2"] = phi3
     out["phi4d_from3d"] = PM.phi_3D_to_4D(phi3, 0.3, 0.2, xs, xs, xs, xs)
+    x6 = N.default_grid(6)
+    p4 = PM.phi_3D_to_4D(PM.phi_2D_to_3D_split_2(x6, PM.phi_1D_to_2D(x6, PM.phi_1D(x6))),
+                         0.3, 0.2, x6, x6, x6, x6)
+    out["phi5d_from4d"] = PM.phi_4D_to_5D(p4, 0.2, 0.3, 0.1, x6, x6, x6, x6, x6)
     rng = np.random.default_rng(5)
+    rng5 = np.random.default_rng(6)  # the 5-D case, added later, draws apart
     for nd, pts, ns in [(1, 25, (12,)), (2, 21, (8, 11)), (3, 11, (5, 6, 4)),
-                        (4, 7, (3, 4, 2, 3))]:
+                        (4, 7, (3, 4, 2, 3)), (5, 6, (2, 3, 2, 2, 3))]:
         xg = N.default_grid(pts)
-        phi = rng.uniform(size=(pts,) * nd)
+        phi = (rng5 if nd == 5 else rng).uniform(size=(pts,) * nd)
         fs = S.from_phi(phi, ns, (xg,) * nd)
         out["fromphi_%dd" % nd] = np.asarray(fs.data)
         out["fromphi_%dd_phi" % nd] = phi

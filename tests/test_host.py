@@ -28,7 +28,16 @@ def test_grid_and_phi(golden):
                           h["phi4d_from3d"])
 
 
-@pytest.mark.parametrize("nd,pts", [(1, 25), (2, 21), (3, 11), (4, 7)])
+def test_phi_4D_to_5D(golden):
+    h = golden["host"]
+    x6 = numerics.default_grid(6)
+    p4 = phimanip.phi_3D_to_4D(phimanip.phi_2D_to_3D_split_2(
+        x6, phimanip.phi_1D_to_2D(x6, phimanip.phi_1D(x6))), 0.3, 0.2, x6, x6, x6, x6)
+    assert np.array_equal(phimanip.phi_4D_to_5D(p4, 0.2, 0.3, 0.1, x6, x6, x6, x6, x6),
+                          h["phi5d_from4d"])
+
+
+@pytest.mark.parametrize("nd,pts", [(1, 25), (2, 21), (3, 11), (4, 7), (5, 6)])
 def test_from_phi(golden, nd, pts):
     h = golden["host"]
     xx = numerics.default_grid(pts)
