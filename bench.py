@@ -260,7 +260,9 @@ def run_ours(a, world, rank, local):
     ps = point_sweeps(steps, PTS_L)
     eng = batch.Batch2D(PTS_L, NS, gam_placement=a.gam)
     tuned = None
-    if a.gam == 0 and not a.no_tune:
+    if a.launch:
+        eng.launch_mode = a.launch
+    elif a.gam == 0 and not a.no_tune:
         # launch configuration chosen by timing the candidates on a sample
         from dadi_gb300 import autotune
         tuned = autotune.tune_batch2d(eng, rec)
@@ -596,6 +598,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the launch-configuration autotuner (use --gam's placement)")
+    ap.add_argument("--launch", default=None, choices=["persistent", "one_per_cta", "per_grid"],
+                    help="launch mode instead of the autotuner's choice (with --gam)")
     ap.add_argument("--clock-ms", type=int, default=500,
                     help="nvidia-smi sampling period during the timed region (0: off)")
     ap.add_argument("--serve", type=int, default=600,

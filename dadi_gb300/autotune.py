@@ -6,6 +6,9 @@ The knobs, each a real alternative the kernels implement:
   grid) work items from an atomic queue, longest first; "one_per_cta": one
   CTA per work item, each retiring after its item (what lets concurrent
   launches share SMs);
+* ... or "per_grid": one persistent launch per grid size, each shaped for
+  its own L (CTAs per SM, three or four warps per CTA), on side streams so
+  that one launch's tail overlaps the next;
 * gam placement — the Thomas recurrence's scratch in shared memory (fewer
   CTAs per SM when the density already fills it) or in a per-CTA slice of
   the workspace (more CTAs per SM, L2 traffic on the back substitution).
@@ -21,7 +24,8 @@ import numpy as np
 
 from . import _lib, batch
 
-CANDIDATES = [("persistent", 1), ("persistent", 2), ("one_per_cta", 1), ("one_per_cta", 2)]
+CANDIDATES = [("persistent", 1), ("persistent", 2), ("one_per_cta", 1), ("one_per_cta", 2),
+              ("per_grid", 1), ("per_grid", 2)]
 
 _cache = {}
 

@@ -175,6 +175,10 @@ class Batch2D:
         CTA per item) and self.gam_placement (0 auto, 1 shared memory, 2
         workspace), the knobs autotune.tune_batch2d chooses."""
         torch = self.torch
+        if self.launch_mode == "per_grid" and len(set(self.pts_l)) > 1:
+            out = self._integrate_per_grid(rec, timer)
+            if out is not None:
+                return out
         if self.launch_mode == "one_per_cta":
             n = len(rec)
             phi0s = [self.d_phi0[o:o + L * L].view(1, L, L).expand(n, L, L)
@@ -209,6 +213,59 @@ class Batch2D:
         if timer is not None:
             timer[1].record()
         _lib.check(rc, "dgb_batch2d_integrate")
+        phis, o = [], 0
+        for L in self.pts_l:
+            phis.append(d_out[o:o + n * L * L].view(n, L, L))
+            o += n * L * L
+        return phis, status
+
+    def _integrate_per_grid(self, rec, timer):
+        """One persistent launch per grid size, each shaped for its own L
+        (CTAs per SM, threads per CTA) instead of the largest, on side
+        streams so that one launch's tail overlaps the next's start.  None
+        when schedules are per grid (use_old_timestep)."""
+        torch = self.torch
+        lib = _lib.lib()
+        st = settings_from_globals(self.gam_placement)
+        if st.use_old_timestep:
+            return None
+        n = len(rec)
+        rec = np.ascontiguousarray(rec)
+        d_rec = _lib.to_device(torch, rec.view(np.uint8), np.uint8)
+        table, off, cnt, status = self.schedule(d_rec, n)
+        d_order = torch.argsort(-cnt.to(torch.int64), stable=True).to(torch.int32)
+        masks = (rec["frozen"].astype(np.int32) & 0xff) | ((rec["nomut"].astype(np.int32) & 0xff) << 8)
+        d_masks = _lib.to_device(torch, masks, np.int32)
+        total = sum(n * L * L for L in self.pts_l)
+        d_out = torch.empty(total, dtype=torch.float64, device="cuda")
+        cur = torch.cuda.current_stream()
+        if not hasattr(self, "_side"):
+            self._side = [torch.cuda.Stream() for _ in self.pts_l]
+        fork = torch.cuda.Event()
+        if timer is not None:
+            timer[0].record()
+        fork.record(cur)
+        xo = po = oo = 0
+        # largest grids first: their longest items set the end
+        for g in sorted(range(len(self.pts_l)), key=lambda k: -self.pts_l[k]):
+            L = self.pts_l[g]
+            xo = sum(self.pts_l[:g])
+            po = sum(l * l for l in self.pts_l[:g])
+            oo = sum(n * l * l for l in self.pts_l[:g])
+            side = self._side[g]
+            with torch.cuda.stream(side):
+                side.wait_event(fork)
+                ws, nws = _lib.workspace(torch, lib.dgb_workspace_bytes(1, 2, L, n))
+                Ls = (ctypes.c_int * 1)(L)
+                _lib.check(lib.dgb_batch2d_integrate(
+                    _lib.dptr(d_masks), n, Ls, 1, _lib.dptr(self.d_xx[xo:xo + L]),
+                    _lib.dptr(self.d_phi0[po:po + L * L]), _lib.dptr(d_out[oo:oo + n * L * L]),
+                    _lib.dptr(table), _lib.dptr(off), _lib.dptr(cnt), _lib.dptr(d_order),
+                    ctypes.byref(st), _lib.dptr(ws), nws, _lib.stream_handle(torch)),
+                    "dgb_batch2d_integrate")
+            cur.wait_stream(side)
+        if timer is not None:
+            timer[1].record()
         phis, o = [], 0
         for L in self.pts_l:
             phis.append(d_out[o:o + n * L * L].view(n, L, L))

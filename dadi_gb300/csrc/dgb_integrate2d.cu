@@ -406,16 +406,17 @@ int k2_smem_fits(int Lmax, bool gam_smem, bool delj, size_t *bytes)
     return l.total + sizeof(K2Shared) + 1024 <= (size_t)optin;
 }
 
-static int k2_launch(K2Args &A, int nblocks, size_t smem, cudaStream_t st)
+static int k2_launch(K2Args &A, int nblocks, size_t smem, cudaStream_t st,
+                     int threads = K2_THREADS)
 {
     if (A.use_delj) {
         if (raise_smem_limit(k_integrate2d<true>))
             return DGB_ERR_CUDA;
-        k_integrate2d<true><<<nblocks, K2_THREADS, smem, st>>>(A);
+        k_integrate2d<true><<<nblocks, threads, smem, st>>>(A);
     } else {
         if (raise_smem_limit(k_integrate2d<false>))
             return DGB_ERR_CUDA;
-        k_integrate2d<false><<<nblocks, K2_THREADS, smem, st>>>(A);
+        k_integrate2d<false><<<nblocks, threads, smem, st>>>(A);
     }
     return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
 }
@@ -424,17 +425,17 @@ static int k2_launch(K2Args &A, int nblocks, size_t smem, cudaStream_t st)
 // dynamic-smem limit is raised to the opt-in maximum first: the occupancy
 // query honours the current limit, so without this its answer would depend on
 // the previous launch.
-static int k2_occupancy(bool delj, size_t smem)
+static int k2_occupancy(bool delj, size_t smem, int threads = K2_THREADS)
 {
     int nb = 0;
     cudaError_t e;
     if (delj) {
         raise_smem_limit(k_integrate2d<true>);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate2d<true>, K2_THREADS,
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate2d<true>, threads,
                                                           smem);
     } else {
         raise_smem_limit(k_integrate2d<false>);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate2d<false>, K2_THREADS,
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate2d<false>, threads,
                                                           smem);
     }
     if (e != cudaSuccess) {
@@ -444,12 +445,37 @@ static int k2_occupancy(bool delj, size_t smem)
     return nb > 0 ? nb : 1;
 }
 
+// Threads per CTA for a launch whose grids are at most Lmax: 96 (three warps)
+// when that packs more lines per SMSP instruction stream than 128.  A sweep
+// of one line is one lane's chain, and the FP64 pipe charges a warp
+// instruction whatever its active lanes, so an SM's time per step is set by
+// the most warps any SMSP holds: with occ CTAs of w warps per SM, lines per
+// SMSP-stream = occ * Lmax / ceil(occ * w / 4).  At Lmax = 80 (four CTAs per
+// SM): 96 threads 106.7, 128 threads 80.  occ returns the chosen CTAs per SM.
+static int k2_threads(bool delj, size_t smem, int Lmax, int &occ);
+
 static int k2_num_sms()
 {
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     return nsm > 0 ? nsm : 1;
+}
+
+static int k2_threads(bool delj, size_t smem, int Lmax, int &occ)
+{
+    int best_t = K2_THREADS;
+    occ = k2_occupancy(delj, smem + sizeof(K2Shared), K2_THREADS);
+    if (Lmax > 96)
+        return best_t;
+    double best = (double)occ * Lmax / ((occ * 4 + 3) / 4);
+    int o3 = k2_occupancy(delj, smem + sizeof(K2Shared), 96);
+    double t3 = (double)o3 * Lmax / ((o3 * 3 + 3) / 4);
+    if (t3 > best) {
+        best_t = 96;
+        occ = o3;
+    }
+    return best_t;
 }
 
 int k2_integrate_table(double *phi, int L, const double *xx, const double *table, int nsteps,
@@ -540,7 +566,6 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     int occ_s = fit_s ? k2_occupancy(A.use_delj, bytes_s + sizeof(K2Shared)) : 0;
     int occ_g = k2_occupancy(A.use_delj, bytes_g + sizeof(K2Shared));
     size_t slice = (size_t)Lmax * Lmax * sizeof(double);
-    int max_g_blocks = (int)std::min<size_t>((ws_bytes - 256) / slice, (size_t)nsm * occ_g);
     // auto: gam in shared memory only when that does not cost CTAs per SM.
     // Measured on the 4096-instance IM batch at pts 80/90/100: gam in the
     // workspace (two CTAs per SM at L = 100, two warps per SMSP) 13.44 s,
@@ -557,6 +582,7 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     }
     int nblocks;
     size_t smem;
+    int threads = K2_THREADS;
     if (use_s) {
         A.gam_smem = 1;
         nblocks = nsm * occ_s;
@@ -564,15 +590,16 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     } else {
         A.gam_smem = 0;
         A.gam_glob = (double *)((char *)ws + 256);
-        nblocks = max_g_blocks;
         smem = bytes_g;
+        threads = k2_threads(A.use_delj, smem, A.Lmax, occ_g);
+        nblocks = (int)std::min<size_t>((ws_bytes - 256) / slice, (size_t)nsm * occ_g);
     }
     if (nblocks < 1)
         return DGB_ERR_WORKSPACE;
     nblocks = std::min(nblocks, A.nwork);
     if (cudaMemsetAsync(A.counter, 0, sizeof(int), st) != cudaSuccess)
         return DGB_ERR_CUDA;
-    return k2_launch(A, nblocks, smem, st);
+    return k2_launch(A, nblocks, smem, st, threads);
 }
 
 // ------------------------------------------- allocation-free entry point
