@@ -218,3 +218,22 @@ def test_dropin_five_pops_signature(cuda_lib, golden):
                                         *[f(v) for v in hs], f(th), False, False, False, False,
                                         False, None)
     assert _rel(out, golden["integrate"]["int_" + case["name"]]) < INT_TOL
+
+
+def test_edges_large_grid_and_zero_time(cuda_lib):
+    """A 2-D grid too large for the shared-memory-resident kernel (L = 180:
+    its density alone is 254 KB) runs through the per-axis sweeps and still
+    matches the oracle; T == initial_t returns an unchanged copy; frozen
+    populations with migration raise the reference's ValueError."""
+    from dadi_gb300 import integration as gi
+    from oracle import integration as oint
+    xx = cases.grid("default", 180)
+    phi0 = cases.initial_phi(7, (180, 180))
+    args = (0.002, 1.5, 0.7, 0.4, 0.9)
+    out = gi.two_pops(phi0.copy(), xx, *args)
+    ref = oint.two_pops(phi0.copy(), xx, *args)
+    assert _rel(out, ref) < INT_TOL
+    same = gi.two_pops(phi0, xx, 0.3, initial_t=0.3)
+    assert np.array_equal(same, phi0) and same is not phi0
+    with pytest.raises(ValueError):
+        gi.two_pops(phi0, xx, 0.1, m12=1.0, frozen1=True)
