@@ -231,6 +231,7 @@ struct ADArgs {
     int nwork;
     int *counter;
     double *scratch;      // per CTA: (ckpt_every + 3) * Lmax^2 doubles
+    int lam_smem;         // the item's adjoint held in shared memory (odd pitch)
     int Lmax;
 };
 
@@ -303,9 +304,12 @@ __device__ void ad_step_setup(ADShared &S, ADVecs &V, const GridVecs &g, int L, 
 // Solve all lines of axis a of the L x L row-major array u (in place), with
 // the forward or transposed vectors.
 __device__ void ad_sweep(double *u, double *gam, int L, int a, const AxisVecs &v,
-                         const AxisScalars &s, const GridVecs &g, int j0, int j1)
+                         const AxisScalars &s, const GridVecs &g, int j0, int j1, int pu = 0)
 {
-    const int sp = (a == 0) ? L : 1, sl = (a == 0) ? 1 : L;
+    // u has row pitch pu (L when 0): global arrays are row-major, the
+    // shared-memory adjoint uses an odd pitch (conflict-free both ways)
+    const int P = pu ? pu : L;
+    const int sp = (a == 0) ? P : 1, sl = (a == 0) ? 1 : P;
     for (int line = threadIdx.x; line < L; line += blockDim.x) {
         double W = s.mig[1 - a] * g.x[line];
         double bs = (line == j0) ? s.bcs : 0.0;
@@ -318,14 +322,18 @@ __device__ void ad_sweep(double *u, double *gam, int L, int a, const AxisVecs &v
 // thread, added into G[Q_DT], G[nu], G[m], G[gamma], G[h] of that axis.
 __device__ void ad_contract(const double *mu, const double *phi, const double *rhs,
                             const double *inj_pts, double inj, int L, int a,
-                            const AxisScalars &s, const GridVecs &g, int j0, int j1, double *G)
+                            const AxisScalars &s, const GridVecs &g, int j0, int j1, double *G,
+                            int pm = 0)
 {
+    // mu has row pitch pm (L when 0); phi and rhs are row-major
     const int sp = (a == 0) ? L : 1, sl = (a == 0) ? 1 : L;
+    const int PM = pm ? pm : L;
+    const int msp = (a == 0) ? PM : 1, msl = (a == 0) ? 1 : PM;
     const int qn = a ? Q_NU1 : Q_NU0, qm = a ? Q_M10 : Q_M01, qg = a ? Q_G1 : Q_G0,
               qh = a ? Q_H1 : Q_H0;
     const double dt = s.dt, inu = s.inv_nu, gam = s.gamma, hh = s.h;
     for (int line = threadIdx.x; line < L; line += blockDim.x) {
-        const double *m = mu + (size_t)line * sl, *p = phi + (size_t)line * sl,
+        const double *m = mu + (size_t)line * msl, *p = phi + (size_t)line * sl,
                      *r = rhs + (size_t)line * sl;
         const double o = g.x[line];
         double smr = 0, smp = 0, snu = 0, sm = 0, sg = 0, sh = 0;
@@ -343,7 +351,7 @@ __device__ void ad_contract(const double *mu, const double *phi, const double *r
             smr = fma(mi, ri, smr);
             smp = fma(mi, pi, smp);
             if (i < L - 1) {
-                double mn = m[(i + 1) * sp], pn = p[(i + 1) * sp];
+                double mn = m[(i + 1) * msp], pn = p[(i + 1) * sp];
                 double xi = g.xInt[i];
                 double Pi = inu * g.xv[i] * g.ih[i];
                 double Qi = inu * g.xv[i + 1] * g.ih[i];
@@ -368,7 +376,7 @@ __device__ void ad_contract(const double *mu, const double *phi, const double *r
         }
         if (line == j1 && s.bce != 0.0) {
             double xl = g.x[L - 1], f = dt * 2. / g.dx[L - 2];
-            double w = m[(L - 1) * sp] * p[(L - 1) * sp];
+            double w = m[(L - 1) * msp] * p[(L - 1) * sp];
             bnu += w * f * (-0.5 * inu * inu);
             bm += w * f * (1. - xl);
             bg += w * f * (2 * (hh + (1. - 2 * hh) * xl) * xl * (1. - xl));
@@ -414,6 +422,9 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
     GridVecs g;
     ADVecs V;
     ad_carve(smem, A.Lmax, g, V);
+    // the adjoint of the item in shared memory, after the vectors (26 Lmax)
+    const int lpitch = (A.Lmax % 2) ? A.Lmax : A.Lmax + 1;
+    double *lam_s = smem + (size_t)26 * A.Lmax;
     const size_t L2max = (size_t)A.Lmax * A.Lmax;
     double *seg = A.scratch + (size_t)blockIdx.x * (A.ckpt_every + 3) * L2max;
     double *W1 = seg + (size_t)(A.ckpt_every + 1) * L2max;
@@ -432,7 +443,19 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
         const int L = A.L[gi];
         const size_t LL = (size_t)L * L;
         const double *xx = A.xx_all + A.xx_off[gi];
-        double *lam = A.lam + A.out_off[gi] + (size_t)inst * LL;
+        double *lam_g = A.lam + A.out_off[gi] + (size_t)inst * LL;
+        // work on the adjoint in shared memory when it fits (lp = its pitch),
+        // else in place in global memory (lp = 0: row-major)
+        double *lam = A.lam_smem ? lam_s : lam_g;
+        const int lp = A.lam_smem ? lpitch : 0;
+        const int LP = lp ? lp : L;
+        if (A.lam_smem) {
+            for (size_t idx = threadIdx.x; idx < LL; idx += blockDim.x) {
+                const int r = (int)(idx / L), c = (int)(idx - (size_t)r * L);
+                lam_s[r * lpitch + c] = lam_g[idx];
+            }
+            __syncthreads();
+        }
         const int sidx = A.sched_per_grid ? wid : inst;
         const double *rows = A.table + A.row_off[sidx] * 11;
         const double *drows = A.drows + A.row_off[sidx] * NQ * NPAR;
@@ -540,20 +563,20 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
                 }
                 // y: mu = Y^{-T} lambda, contract with phi_{k+1}, rhs chi
                 if (!(frozen & 2)) {
-                    ad_sweep(lam, gam, L, 1, V.t[1], S.ax[1], g, j0, j1);
+                    ad_sweep(lam, gam, L, 1, V.t[1], S.ax[1], g, j0, j1, lp);
                     __syncthreads();
-                    ad_contract(lam, phin, W1, nullptr, 0.0, L, 1, S.ax[1], g, j0, j1, G);
+                    ad_contract(lam, phin, W1, nullptr, 0.0, L, 1, S.ax[1], g, j0, j1, G, lp);
                     __syncthreads();
                 }
                 // x: nu = X^{-T} mu, contract with chi, rhs psi
                 if (!(frozen & 1)) {
-                    ad_sweep(lam, gam, L, 0, V.t[0], S.ax[0], g, j0, j1);
+                    ad_sweep(lam, gam, L, 0, V.t[0], S.ax[0], g, j0, j1, lp);
                     __syncthreads();
-                    ad_contract(lam, W1, phik, inj_on, S.inj, L, 0, S.ax[0], g, j0, j1, G);
+                    ad_contract(lam, W1, phik, inj_on, S.inj, L, 0, S.ax[0], g, j0, j1, G, lp);
                 }
                 // injection: d psi(1,0), psi(0,1) / d(dt, theta0)
                 if (tid == 0) {
-                    double lin = (injx ? lam[1 * L + 0] : 0.0) + (injy ? lam[0 * L + 1] : 0.0);
+                    double lin = (injx ? lam[1 * LP + 0] : 0.0) + (injy ? lam[0 * LP + 1] : 0.0);
                     G[Q_DT] += lin * S.dinj_dt;
                     G[Q_TH] += lin * S.dinj_th;
                 }
@@ -566,6 +589,13 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
                     acc[p] = sacc;
                 }
                 __syncthreads();
+            }
+        }
+        if (A.lam_smem) {
+            // dJ/dphi_initial back to the caller's array
+            for (size_t idx = threadIdx.x; idx < LL; idx += blockDim.x) {
+                const int r = (int)(idx / L), c = (int)(idx - (size_t)r * L);
+                lam_g[idx] = lam_s[r * lpitch + c];
             }
         }
         // block reduction of acc into this work item's row of grad
@@ -665,6 +695,18 @@ extern "C" int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngr
     nblocks = std::min<long>(nblocks, A.nwork);
     A.scratch = (double *)((char *)ws + 256);
     size_t smem = (size_t)26 * Lmax * sizeof(double);
+    {
+        // the adjoint in shared memory when vectors + Lmax x odd pitch fit
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        const int lpitch = (Lmax % 2) ? Lmax : Lmax + 1;
+        size_t with_lam = smem + (size_t)Lmax * lpitch * sizeof(double);
+        if (with_lam + sizeof(ADShared) + 4096 <= (size_t)optin) {
+            A.lam_smem = 1;
+            smem = with_lam;
+        }
+    }
     if (raise_smem_limit(k_adjoint2d))
         return DGB_ERR_CUDA;
     if (cudaMemsetAsync(A.counter, 0, sizeof(int), (cudaStream_t)stream) != cudaSuccess)
