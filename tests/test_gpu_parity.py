@@ -237,3 +237,17 @@ def test_edges_large_grid_and_zero_time(cuda_lib):
     assert np.array_equal(same, phi0) and same is not phi0
     with pytest.raises(ValueError):
         gi.two_pops(phi0, xx, 0.1, m12=1.0, frozen1=True)
+
+
+def test_transpose_gpuarray(cuda_lib):
+    """dadi.cuda.transpose_gpuarray's contract (tests/test_CUDA.py:11-21 of
+    the reference) on device tensors."""
+    import torch
+    from dadi_gb300 import cuda as dcuda
+    a = np.random.default_rng(0).uniform(size=(2, 3))
+    a_gpu = torch.from_numpy(a).cuda()
+    aT_gpu = torch.empty(a.shape[::-1], dtype=a_gpu.dtype, device="cuda")
+    dcuda.transpose_gpuarray(a_gpu, aT_gpu)
+    assert np.array_equal(aT_gpu.cpu().numpy(), a.T)
+    with pytest.raises(ValueError):
+        dcuda.transpose_gpuarray(a_gpu, torch.empty(2, 3, dtype=a_gpu.dtype, device="cuda"))
