@@ -249,6 +249,24 @@ class TableModel:
         return ll.detach(), grad, fs.detach()
 
 
+    def loglik_and_grad_many(self, thetas, data, scale=1.0, workers=4):
+        """loglik_and_grad for several parameter sets, `workers` at a time on
+        their own threads and CUDA streams (one set's sweeps leave most SMs
+        idle).  Returns [(ll, grad, fs)] in the order of thetas."""
+        torch = self.torch
+        from concurrent.futures import ThreadPoolExecutor
+        dev = torch.cuda.current_device()
+        d = data if torch.is_tensor(data) else _lib.to_device(torch, data)
+
+        def one(th):
+            with torch.cuda.device(dev), torch.cuda.stream(torch.cuda.Stream()):
+                ll, g, fs = self.loglik_and_grad(th, d, scale)
+                torch.cuda.current_stream().synchronize()
+                return ll, g, fs
+        with ThreadPoolExecutor(max_workers=max(1, int(workers))) as ex:
+            return list(ex.map(one, list(thetas)))
+
+
 class Growth3(TableModel):
     """models.growth3 with parameters theta = (nu0_1, nu0_2, nu0_3, nuF_1,
     nuF_2, nuF_3, m12, m13, m23, T) and fixed gammas (default: the
