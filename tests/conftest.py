@@ -18,7 +18,7 @@ def golden():
     import numpy as np
     d = os.path.join(ROOT, "tests", "golden")
     return {name: np.load(os.path.join(d, name + ".npz"))
-            for name in ("integrate", "sweeps", "host", "models", "grad", "dfe")}
+            for name in ("integrate", "sweeps", "host", "models", "grad", "dfe", "settings")}
 
 
 @pytest.fixture(scope="session")

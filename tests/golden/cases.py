@@ -173,3 +173,15 @@ GROWTH3 = dict(params=((0.5, 1.0, 2.0), (5.0, 0.2, 10.0), (0.5, 1.5, 3.0), (-2.0
 #: and its integration over a bivariate lognormal (dadi.DFE.PDFs.biv_lognormal).
 DFE = dict(params=(0.4, 1.5, 0.6, 0.1, 1.0, 0.5), ns=(6, 6), pts=[12, 16, 20], gamma_pts=3,
            sel_params=(1.0, 2.0, 0.5), theta=1000.0)
+
+
+#: dadi's module-level integration settings (dadi/Integration.py:25-44)
+#: other than the defaults: each entry runs an IM model pipeline under one
+#: of them.  The IM parameters give a time-dependent nu, so dt varies.
+SETTINGS = [
+    ("old_timestep", dict(use_old_timestep=True, old_timescale_factor=0.1)),
+    ("delj", dict(use_delj_trick=True)),
+    ("timescale5e-3", dict(timescale_factor=5e-3)),
+]
+SETTINGS_IM = dict(params=(0.4, 1.5, 0.6, 0.05, 1.0, 0.5), ns=(8, 8), pts_l=[20, 25, 30])
+

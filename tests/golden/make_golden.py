@@ -221,6 +221,34 @@ def gen_grad(dadi, out):
     out["grad_godambe"] = np.asarray(dadi.Godambe.get_grad(func, p0, 1e-4)).ravel()
 
 
+def gen_settings(dadi, out):
+    """The IM pipeline and single two_pops / three_pops integrations under
+    each non-default setting of dadi.Integration."""
+    I = dadi.Integration
+    d = cases.SETTINGS_IM
+    f = dadi.Numerics.make_extrap_func(dadi.Demographics2D.IM)
+    for name, kw in cases.SETTINGS:
+        saved = {k: getattr(I, k) for k in kw}
+        try:
+            for k, v in kw.items():
+                setattr(I, k, v)
+            out["set_%s_im" % name] = np.asarray(f(d["params"], d["ns"], d["pts_l"]).data)
+            xx = dadi.Numerics.default_grid(18)
+            phi = dadi.PhiManip.phi_1D_to_2D(xx, dadi.PhiManip.phi_1D(xx))
+            out["set_%s_2d" % name] = I.two_pops(phi, xx, 0.04, 2.0, lambda t: 0.5 + t,
+                                                 1.0, 0.4, gamma1=-1.0, gamma2=2.0, h1=0.3)
+            phi3 = dadi.PhiManip.phi_2D_to_3D_split_2(xx, phi)
+            # a time-dependent size keeps three_pops on its temporal loop (its
+            # constant-parameter path raises IndexError under the delj trick,
+            # dadi/Integration.py:976)
+            out["set_%s_3d" % name] = I.three_pops(phi3, xx, 0.02, lambda t: 1.0 + t, 0.5,
+                                                   2.0, m12=1.0, m21=0.5, m23=0.3, m32=0.6,
+                                                   gamma3=1.5)
+        finally:
+            for k, v in saved.items():
+                setattr(I, k, v)
+
+
 def gen_dfe(dadi, out):
     from dadi.DFE import Cache2D_mod, DemogSelModels, PDFs
     d = cases.DFE
@@ -245,7 +273,8 @@ def main():
     a = ap.parse_args()
     dadi = load_dadi(a.ref, a.build)
     for name, gen in [("integrate", gen_integrations), ("sweeps", gen_sweeps),
-                      ("host", gen_host), ("grad", gen_grad), ("dfe", gen_dfe)]:
+                      ("host", gen_host), ("grad", gen_grad), ("dfe", gen_dfe),
+                      ("settings", gen_settings)]:
         out = {}
         gen(dadi, out)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)

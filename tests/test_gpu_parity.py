@@ -251,3 +251,42 @@ def test_transpose_gpuarray(cuda_lib):
     assert np.array_equal(aT_gpu.cpu().numpy(), a.T)
     with pytest.raises(ValueError):
         dcuda.transpose_gpuarray(a_gpu, torch.empty(2, 3, dtype=a_gpu.dtype, device="cuda"))
+
+
+@pytest.mark.parametrize("name,kw", cases.SETTINGS, ids=[n for n, _ in cases.SETTINGS])
+def test_dadi_settings(cuda_lib, golden, name, kw):
+    """The drop-in integrators and the batched engine under each non-default
+    setting of dadi.Integration (read at call time: use_old_timestep,
+    use_delj_trick, timescale_factor) against dadi run with the same
+    setting.  The delj trick amplifies last-ulp differences of exp (see
+    DELJ_SWEEP_TOL): 1e-7 on densities there; the spectrum bar otherwise."""
+    from dadi_gb300 import batch, integration as gi, models, numerics, phimanip
+    g = golden["settings"]
+    d = cases.SETTINGS_IM
+    tol = 1e-7 if name == "delj" else INT_TOL
+    saved = {k: getattr(gi, k) for k in kw}
+    try:
+        for k, v in kw.items():
+            setattr(gi, k, v)
+        xx = numerics.default_grid(18)
+        phi = phimanip.phi_1D_to_2D(xx, phimanip.phi_1D(xx))
+        p2 = gi.two_pops(phi, xx, 0.04, 2.0, lambda t: 0.5 + t, 1.0, 0.4, gamma1=-1.0,
+                         gamma2=2.0, h1=0.3)
+        assert _rel(p2, g["set_%s_2d" % name]) < tol
+        p3 = gi.three_pops(phimanip.phi_2D_to_3D_split_2(xx, phi), xx, 0.02,
+                           lambda t: 1.0 + t, 0.5, 2.0, m12=1.0, m21=0.5, m23=0.3, m32=0.6,
+                           gamma3=1.5)
+        assert _rel(p3, g["set_%s_3d" % name]) < tol
+        ref = g["set_%s_im" % name]
+        fs = numerics.make_extrap_func(models.IM)(d["params"], d["ns"], d["pts_l"])
+        fsb, _, st = batch.Batch2D(d["pts_l"], d["ns"]).run(np.array([d["params"]]))
+        assert int(st.abs().sum()) == 0
+        for f in (np.asarray(fs.data), fsb.cpu().numpy()[0]):
+            if name == "delj":
+                rel, _, _ = fs_parity(f, ref)
+                assert rel < 1e-7, rel
+            else:
+                assert_fs_parity(f, ref)
+    finally:
+        for k, v in saved.items():
+            setattr(gi, k, v)

@@ -137,3 +137,30 @@ def test_reference_noise_floor_tiny_entries(golden):
     assert rel_all > 1e-9          # the reference's own floor on tiny entries
     assert rel_big < 1e-10          # entries that matter move far less
     assert abs_small < 1e-21
+
+
+@pytest.mark.parametrize("name,kw", cases.SETTINGS, ids=[n for n, _ in cases.SETTINGS])
+def test_oracle_under_dadi_settings(golden, name, kw):
+    """The oracle under each non-default setting of dadi.Integration
+    (use_old_timestep, use_delj_trick, timescale_factor) equals dadi run with
+    the same setting, bit for bit."""
+    g = golden["settings"]
+    d = cases.SETTINGS_IM
+    saved = {k: getattr(oint, k) for k in kw}
+    try:
+        for k, v in kw.items():
+            setattr(oint, k, v)
+        fs = onum.extrap_model(onum.IM, d["params"], d["ns"], d["pts_l"])
+        assert np.array_equal(fs, g["set_%s_im" % name])
+        xx = onum.default_grid(18)
+        phi = onum.phi_1D_to_2D(xx, onum.phi_1D(xx))
+        p2 = oint.two_pops(phi.copy(), xx, 0.04, 2.0, lambda t: 0.5 + t, 1.0, 0.4,
+                           gamma1=-1.0, gamma2=2.0, h1=0.3)
+        assert np.array_equal(p2, g["set_%s_2d" % name])
+        phi3 = onum.phi_2D_to_3D_admix(phi, 0, xx, xx, xx)
+        p3 = oint.three_pops(phi3, xx, 0.02, lambda t: 1.0 + t, 0.5, 2.0, m12=1.0, m21=0.5,
+                             m23=0.3, m32=0.6, gamma3=1.5)
+        assert np.array_equal(p3, g["set_%s_3d" % name])
+    finally:
+        for k, v in saved.items():
+            setattr(oint, k, v)
