@@ -37,6 +37,23 @@ def ll_multinom(model, data):
     return ll(theta * model, data)
 
 
+def Anscombe_Poisson_residual(model, data, mask=None):
+    """Anscombe residuals of Poisson data given the model
+    (dadi/Inference.py:612-659): 1.5 (d' - m') / model^(1/6) with
+    x' = x^(2/3) - x^(-1/3) / 9, negated (positive where the model is high);
+    with `mask`, entries where both are <= mask or the data are 0 are masked.
+    (Folded spectra are not handled here.)"""
+    d = np.ma.asarray(data, dtype=np.float64)
+    m = np.ma.asarray(model, dtype=np.float64)
+    dt = d ** (2. / 3) - np.ma.power(d, -1. / 3) / 9
+    mt = m ** (2. / 3) - np.ma.power(m, -1. / 3) / 9
+    resid = 1.5 * (dt - mt) / m ** (1. / 6)
+    if mask is not None:
+        tomask = np.logical_or(np.logical_and(m <= mask, d <= mask), d == 0)
+        resid = np.ma.masked_where(tomask, resid)
+    return -resid
+
+
 # ------------------------------------------------------------ optimisation
 
 def _project_down(p, fixed):

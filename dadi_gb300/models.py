@@ -10,6 +10,21 @@ import numpy as np
 from . import integration, numerics, phimanip, spectrum
 
 
+def snm_1d(notused, ns, pts):
+    """Standard neutral model (dadi/Demographics1D.py:9-27): the equilibrium
+    density, no integration."""
+    xx = numerics.default_grid(pts)
+    return spectrum.from_phi(phimanip.phi_1D(xx), ns, (xx,))
+
+
+def two_epoch(params, ns, pts):
+    """Instantaneous size change to nu, T ago (dadi/Demographics1D.py:29-50)."""
+    nu, T = params
+    xx = numerics.default_grid(pts)
+    phi = integration.one_pop(phimanip.phi_1D(xx), xx, T, nu)
+    return spectrum.from_phi(phi, ns, (xx,))
+
+
 def split_mig(params, ns, pts):
     nu1, nu2, T, m = params
     xx = numerics.default_grid(pts)

@@ -18,7 +18,8 @@ def golden():
     import numpy as np
     d = os.path.join(ROOT, "tests", "golden")
     return {name: np.load(os.path.join(d, name + ".npz"))
-            for name in ("integrate", "sweeps", "host", "models", "grad", "dfe", "settings")}
+            for name in ("integrate", "sweeps", "host", "models", "grad", "dfe", "settings",
+                         "known")}
 
 
 @pytest.fixture(scope="session")

@@ -249,6 +249,14 @@ def gen_settings(dadi, out):
                 setattr(I, k, v)
 
 
+def gen_known_answers(dadi, ref, out):
+    """The ms-simulated IM spectrum the reference's tests/test_Results.py:24-41
+    compares against (tests/IM.fs of the reference), as data and mask."""
+    ms = dadi.Spectrum.from_file(os.path.join(ref, "tests", "IM.fs"))
+    out["im_ms_data"] = np.asarray(ms.data)
+    out["im_ms_mask"] = np.ma.getmaskarray(ms)
+
+
 def gen_dfe(dadi, out):
     from dadi.DFE import Cache2D_mod, DemogSelModels, PDFs
     d = cases.DFE
@@ -279,6 +287,10 @@ def main():
         gen(dadi, out)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print("wrote", name, len(out), flush=True)
+    out = {}
+    gen_known_answers(dadi, a.ref, out)
+    np.savez_compressed(os.path.join(HERE, "known.npz"), **out)
+    print("wrote known", len(out))
     out = {}
     gen_models(dadi, out, not a.no_big)
     np.savez_compressed(os.path.join(HERE, "models.npz"), **out)
