@@ -190,3 +190,26 @@ def phi_4D_to_5D(phi, f1, f2, f3, xx, yy, zz, aa, bb, deme_ids=None):
     lo, up, fl, fu, norm = _admixture_intermediates(phi, ad_w, bb)
     return _place((len(xx), len(yy), len(zz), len(aa), len(bb)), lo, up, fl, fu, norm, phi)
 
+
+#: dadi's name for phi_2D_to_3D_admix (dadi/PhiManip.py:410).
+phi_2D_to_3D = phi_2D_to_3D_admix
+
+
+def trapz(yy, xx, axis=-1):
+    """Composite trapezoid rule of yy over the 1-D grid xx along `axis`
+    (dadi/Numerics.py:303-332): sum of dx * (y_i + y_{i+1}) / 2."""
+    yy = np.asanyarray(yy)
+    nd = yy.ndim
+    dx = np.diff(xx)
+    s1 = [slice(None)] * nd
+    s2 = [slice(None)] * nd
+    sx = [None] * nd
+    s1[axis], s2[axis], sx[axis] = slice(1, None), slice(None, -1), slice(None)
+    return np.sum(dx[tuple(sx)] * (yy[tuple(s1)] + yy[tuple(s2)]) / 2.0, axis=axis)
+
+
+def remove_pop(phi, xx, popnum):
+    """Density with population popnum (numbered from 1) integrated out
+    (dadi/PhiManip.py:1036-1051)."""
+    return trapz(phi, xx, axis=popnum - 1)
+

@@ -31,6 +31,19 @@ class Spectrum(np.ma.MaskedArray):
         self.extrap_x = getattr(obj, "extrap_x", None)
         self.pop_ids = getattr(obj, "pop_ids", None)
 
+    def marginalize(self, over, mask_corners=True):
+        """Spectrum of the populations not in `over`, summing over those
+        (dadi/Spectrum_mod.py:444-490; masked entries are left out of the
+        sums, as the masked-array sum does)."""
+        out = np.ma.MaskedArray(self.data, mask=self.mask)
+        for axis in sorted(over)[::-1]:
+            out = out.sum(axis=axis)
+        pop_ids = None
+        if self.pop_ids is not None:
+            pop_ids = [p for k, p in enumerate(self.pop_ids) if k not in over]
+        return Spectrum(np.ma.getdata(out), mask=np.ma.getmaskarray(out),
+                        mask_corners=mask_corners, extrap_x=self.extrap_x, pop_ids=pop_ids)
+
 
 _dbeta_cache = {}
 
