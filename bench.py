@@ -452,7 +452,18 @@ def run_serving(a, obs):
     # warm-up stream: library handles, worker engines
     srv.run(serving.config5_stream(max(8, a.serve // 20), seed=1, rate=a.serve_rate,
                                    obs=obs))
-    reqs = serving.config5_stream(a.serve, seed=0, rate=a.serve_rate, obs=obs)
+    summ = _serve_stream(srv, a.serve, a.serve_rate, obs, a.serve_budget)
+    if a.serve_sustained > 0:
+        # the same mix at a rate the server keeps up with: latency without
+        # the backlog of a burst
+        summ["below_capacity"] = _serve_stream(srv, a.serve_sustained, a.serve_sustained_rate,
+                                               obs, a.serve_budget, seed=2)
+    return summ
+
+
+def _serve_stream(srv, n, rate, obs, budget, seed=0):
+    from dadi_gb300 import serving
+    reqs = serving.config5_stream(n, seed=seed, rate=rate, obs=obs)
     out = srv.run(reqs)
     summ = serving.latency_summary(out)
     by = {}
@@ -465,8 +476,8 @@ def run_serving(a, obs):
     if lat:
         by["im_grad"] = {"n": len(lat), "p50_s": float(np.percentile(lat, 50)),
                          "p99_s": float(np.percentile(lat, 99))}
-    summ.update({"arrival_rate_per_s": a.serve_rate, "arrival_span_s": float(out[-1].arrival),
-                 "hbm_budget_gib": a.serve_budget, "by_class": by,
+    summ.update({"arrival_rate_per_s": rate, "arrival_span_s": float(out[-1].arrival),
+                 "hbm_budget_gib": budget, "by_class": by,
                  "failed_status": sum(1 for r in out if r.status)})
     return summ
 
@@ -605,6 +616,9 @@ def main():
                     help="requests in the served stream (0: skip serving)")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-budget", type=int, default=32, help="GiB the server may hold")
+    ap.add_argument("--serve-sustained", type=int, default=200,
+                    help="requests of a second, below-capacity stream (0: skip)")
+    ap.add_argument("--serve-sustained-rate", type=float, default=20.0)
     ap.add_argument("--adjoint", action="store_true",
                     help="also time 256 IM gradients at pts [100,110,120]")
     ap.add_argument("--profile-items", type=int, default=0,
