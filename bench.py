@@ -174,12 +174,16 @@ def point_sweeps(steps, pts_l):
 # ------------------------------------------------------------------ CPU arm
 
 def _cpu_one(args):
-    """One extrapolated IM spectrum on the CPU restatement (Python time loop
-    over the C sweeps, as the reference runs)."""
-    p, pts_l, ns = args
+    """One extrapolated IM spectrum and its Poisson and multinomial
+    log-likelihoods on the CPU restatement (Python time loop over the C
+    sweeps, as the reference runs)."""
+    p, pts_l, ns, obs = args
     from oracle import numerics as onum
     t = time.perf_counter()
-    onum.extrap_model(onum.IM, p, ns, pts_l)
+    fs = onum.extrap_model(onum.IM, p, ns, pts_l)
+    mask = onum.corner_mask(fs.shape)
+    onum.ll(5e4 * fs, obs, mask)
+    onum.ll_multinom(fs, obs, mask)
     return time.perf_counter() - t
 
 
@@ -204,10 +208,14 @@ def cpu_rate(draws, steps_all, budget_s, cores):
         work += c
         if work > budget_s * cores * 0.8:
             break
+    # the observed spectrum as the GPU arm makes it: Poisson(5e4 * model(set 0))
+    from oracle import numerics as onum
+    fs0 = onum.extrap_model(onum.IM, draws[0], NS, PTS_L)
+    obs = np.random.default_rng(0).poisson(5e4 * fs0).astype(np.float64)
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
-        pool.map(_cpu_one, [(draws[i], PTS_L, NS) for i in chosen], chunksize=1)
+        pool.map(_cpu_one, [(draws[i], PTS_L, NS, obs) for i in chosen], chunksize=1)
     wall = time.perf_counter() - t0
     sample_ps = float(np.sum(ps_per_inst[chosen]))
     ps_rate = sample_ps / wall
@@ -234,7 +242,7 @@ def run_reference(a, world, rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seed-0 IM parameter draws)",
         "config": {"workload": "batched 2-D IM, 4096 instances, pts [80,90,100], ns (40,40), "
-                               "extrapolated + Poisson ll", "global_batch": NINST,
+                               "extrapolated + Poisson and multinomial ll", "global_batch": NINST,
                    "pts_l": list(PTS_L), "ns": list(NS)},
         "cpu_baseline": {"value": v, "unit": "spectra/s", "cores": cores, "kind": "port",
                          "sample": "%d seed-0 instances per step (%.3g point-sweeps, %.1f s on "
@@ -277,7 +285,7 @@ def run_ours(a, world, rank, local):
         # and the epilogue (from_phi, extrapolation, likelihood) all run on
         # the GPU, in 5 launches
         phis, status = eng.integrate(rec)
-        fs, ll = eng.spectra_ll(phis, d_obs, 5e4)
+        fs, ll, llm = eng.spectra_ll(phis, d_obs, 5e4, multinom=True)
         return fs, ll, status
 
     # warm-up
@@ -308,7 +316,7 @@ def run_ours(a, world, rank, local):
         k1 = torch.cuda.Event(enable_timing=True)
         t_start.record()
         phis, status = eng.integrate(rec, timer=(k0, k1))
-        fs, ll = eng.spectra_ll(phis, d_obs, 5e4)
+        fs, ll, llm = eng.spectra_ll(phis, d_obs, 5e4, multinom=True)
         t_end.record()
         torch.cuda.synchronize()
         total_ms += t_start.elapsed_time(t_end)
@@ -319,6 +327,11 @@ def run_ours(a, world, rank, local):
     ms_per_step = total_ms / a.steps
     value = job_value(world, ms_per_step)
     bad = int((status != 0).sum())
+    # the scores of the workload: Poisson ll of 5e4 * model and the
+    # multinomial ll (optimal scaling) against the observed spectrum
+    ll_h, llm_h = ll.cpu().numpy(), llm.cpu().numpy()
+    scores = {"ll_set0": float(ll_h[0]), "ll_multinom_set0": float(llm_h[0]),
+              "ll_best": float(np.nanmax(ll_h)), "ll_multinom_best": float(np.nanmax(llm_h))}
 
     # end to end through the public API (host arrays in and out)
     e2e_ms = 0.0
@@ -398,7 +411,7 @@ def run_ours(a, world, rank, local):
         "data": "synthetic (seed-%d IM parameter draws; observed spectrum Poisson(5e4*model))"
                 % rank,
         "config": {"workload": "batched 2-D IM, 4096 instances, pts [80,90,100], ns (40,40), "
-                               "extrapolated + Poisson ll",
+                               "extrapolated + Poisson and multinomial ll",
                    "global_batch": NINST * world, "pts_l": list(PTS_L), "ns": list(NS),
                    "point_sweeps_per_step": ps, "parallelism": "replicas x%d" % world,
                    "l2": "flushed between iterations (256 MB write); phi outputs 803 MB > L2",
@@ -428,6 +441,7 @@ def run_ours(a, world, rank, local):
         "clocks": clk,
         "gpu_launches": 5 * a.steps,  # per step: 2 schedule passes, the integration, 2 epilogue
         "failed_instances": bad,
+        "scores": scores,
         "plain": plain,
         "batched_over_plain": (value / plain["value"]) if plain else None,
         "cpu_baseline": cpu,

@@ -491,17 +491,21 @@ class Batch2D:
             - torch.lgamma(d + 1.0)
         return torch.where(ok, term, torch.zeros_like(term)).sum(dim=(1, 2))
 
-    def spectra_ll(self, phis, data=None, scale=1.0):
+    def spectra_ll(self, phis, data=None, scale=1.0, multinom=False):
         """The device epilogue (dgb_from_phi2d + dgb_extrap_ll, two launches
         for the whole batch): extrapolated spectra (n, n1+1, n2+1) and, with
-        data, Poisson log-likelihoods (n,); CUDA tensors."""
+        data, Poisson log-likelihoods (n,); CUDA tensors.  multinom: also the
+        multinomial log-likelihoods (n,), returned third."""
         torch = self.torch
         d = None
         if data is not None:
             d = data if torch.is_tensor(data) else _lib.to_device(torch, data)
             d = d.to(torch.float64).contiguous()
-        return epilogue.spectra_2d_batch(torch, [p.contiguous() for p in phis], self.xxs,
-                                         self.ns, d, scale)
+        res = epilogue.spectra_2d_batch(torch, [p.contiguous() for p in phis], self.xxs,
+                                        self.ns, d, scale, multinom=multinom and d is not None)
+        if multinom and d is None:
+            return res[0], None, None
+        return res
 
     def run(self, params, data=None, scale=1.0):
         """IM parameter rows -> (extrapolated spectra (n, n1+1, n2+1), ll or

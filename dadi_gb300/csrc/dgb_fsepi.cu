@@ -117,6 +117,28 @@ __global__ void __launch_bounds__(FS_THREADS) k_from_phi2d(const dgb_fs_item2d *
     }
 }
 
+// Fixed-order block sum of v over FS_THREADS threads (all threads get it).
+__device__ __forceinline__ double block_sum(double *red, double v)
+{
+    const int tid = threadIdx.x;
+    __syncthreads(); // red free: earlier readers are done
+    red[tid] = v;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (tid < s)
+            red[tid] += red[tid + s];
+        __syncthreads();
+    }
+    return red[0];
+}
+
+// Poisson term of one entry (dadi/Inference.py:482-509: entries with a
+// nonpositive model are masked by model.log()).
+__device__ __forceinline__ double poisson_term(double model, double d)
+{
+    return (model > 0) ? -model + d * log(model) - lgamma(d + 1.0) : 0.0;
+}
+
 __global__ void __launch_bounds__(FS_THREADS) k_extrap_ll(const dgb_extrap_item *items,
                                                           double fail_mag)
 {
@@ -139,7 +161,9 @@ __global__ void __launch_bounds__(FS_THREADS) k_extrap_ll(const dgb_extrap_item 
     for (int k = 1; k < g; k++)
         if (it.x[k] < it.x[best])
             best = k;
-    double acc = 0;
+    const bool pois = it.data && it.ll;
+    const bool mult = it.data && it.ll_multinom;
+    double acc = 0, sd = 0, sm = 0;
     for (int e = tid; e < it.size; e += blockDim.x) {
         const double y1 = it.fs[0][e];
         double ex;
@@ -157,26 +181,40 @@ __global__ void __launch_bounds__(FS_THREADS) k_extrap_ll(const dgb_extrap_item 
                 ex = bv;
         }
         it.out[e] = ex;
-        if (it.data && it.ll) {
-            const double model = it.scale * ex;
-            const bool masked = it.mask_corners && (e == 0 || e == it.size - 1);
-            if (!masked && model > 0) {
-                const double d = it.data[e];
-                acc += -model + d * log(model) - lgamma(d + 1.0);
+        const bool masked = it.mask_corners && (e == 0 || e == it.size - 1);
+        if ((pois || mult) && !masked) {
+            const double d = it.data[e];
+            if (pois)
+                acc += poisson_term(it.scale * ex, d);
+            if (mult) {
+                sd += d;
+                sm += ex;
             }
         }
     }
-    if (!(it.data && it.ll))
+    if (!(pois || mult))
         return;
-    red[tid] = acc;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (tid < s)
-            red[tid] += red[tid + s];
-        __syncthreads();
+    if (pois) {
+        const double tot = block_sum(red, acc);
+        if (tid == 0)
+            *it.ll = tot;
     }
+    if (!mult)
+        return;
+    // optimal scaling over the unmasked entries, then the Poisson sum at it;
+    // each thread re-reads the entries it wrote above
+    const double sdata = block_sum(red, sd);
+    const double smodel = block_sum(red, sm);
+    const double theta = sdata / smodel;
+    double acc2 = 0;
+    for (int e = tid; e < it.size; e += blockDim.x) {
+        const bool masked = it.mask_corners && (e == 0 || e == it.size - 1);
+        if (!masked)
+            acc2 += poisson_term(theta * it.out[e], it.data[e]);
+    }
+    const double tot2 = block_sum(red, acc2);
     if (tid == 0)
-        *it.ll = red[0];
+        *it.ll_multinom = tot2;
 }
 
 } // namespace dgb

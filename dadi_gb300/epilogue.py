@@ -1,6 +1,6 @@
 """Device spectrum epilogue for 2-D integrations: from_phi, extrapolation and
-the Poisson log-likelihood for many densities in two launches
-(dgb_from_phi2d, dgb_extrap_ll).
+the Poisson (and multinomial) log-likelihoods for many densities in two
+launches (dgb_from_phi2d, dgb_extrap_ll).
 
 Each spectrum is computed by one CTA from its own density alone, so a
 request's result does not depend on what else shares the launch.  The
@@ -16,8 +16,8 @@ FS_ITEM = np.dtype([("phi", "u8"), ("xx", "u8"), ("d1x", "u8"), ("d2x", "u8"), (
                     ("d2y", "u8"), ("out", "u8"), ("L", "i4"), ("n1", "i4"), ("n2", "i4"),
                     ("pad", "i4")])
 EX_ITEM = np.dtype([("fs", "u8", 3), ("x", "f8", 3), ("out", "u8"), ("data", "u8"),
-                    ("ll", "u8"), ("scale", "f8"), ("ngrids", "i4"), ("size", "i4"),
-                    ("mask_corners", "i4"), ("pad", "i4")])
+                    ("ll", "u8"), ("llm", "u8"), ("scale", "f8"), ("ngrids", "i4"),
+                    ("size", "i4"), ("mask_corners", "i4"), ("pad", "i4")])
 
 
 def spectra_2d(torch, jobs, fail_mag=10.0):
@@ -81,10 +81,13 @@ def spectra_2d(torch, jobs, fail_mag=10.0):
     return fs, ll, out
 
 
-def spectra_2d_batch(torch, phis, xxs, ns, data=None, scale=1.0, fail_mag=10.0):
+def spectra_2d_batch(torch, phis, xxs, ns, data=None, scale=1.0, fail_mag=10.0,
+                     multinom=False):
     """A batch sharing grids and sample sizes: phis[g] is an (n, L_g, L_g)
     contiguous CUDA tensor per grid.  Returns (fs (n, n1+1, n2+1), ll (n,)
-    or None), enqueued on the current stream."""
+    or None), enqueued on the current stream; with multinom (and data),
+    (fs, ll, ll_multinom): the multinomial log-likelihoods (n,) from the
+    same launch (dadi/Inference.py:559-575)."""
     lib = _lib.lib()
     dev = torch.device("cuda", torch.cuda.current_device())
     n = int(phis[0].shape[0])
@@ -94,6 +97,8 @@ def spectra_2d_batch(torch, phis, xxs, ns, data=None, scale=1.0, fail_mag=10.0):
     raw = torch.empty(ng * n * size, dtype=torch.float64, device=dev)
     out = torch.empty(n * size, dtype=torch.float64, device=dev)
     ll = torch.empty(n, dtype=torch.float64, device=dev) if data is not None else None
+    llm = torch.empty(n, dtype=torch.float64, device=dev) \
+        if (data is not None and multinom) else None
     fs_items = np.zeros((ng, n), dtype=FS_ITEM)
     ex_items = np.zeros(n, dtype=EX_ITEM)
     idx = np.arange(n, dtype=np.uint64)
@@ -118,10 +123,14 @@ def spectra_2d_batch(torch, phis, xxs, ns, data=None, scale=1.0, fail_mag=10.0):
         ex_items["data"] = data.data_ptr()
         ex_items["ll"] = np.uint64(ll.data_ptr()) + idx * np.uint64(8)
         ex_items["scale"] = scale
+        if llm is not None:
+            ex_items["llm"] = np.uint64(llm.data_ptr()) + idx * np.uint64(8)
     d_fs = _lib.to_device(torch, fs_items.reshape(-1).view(np.uint8), np.uint8)
     d_ex = _lib.to_device(torch, ex_items.view(np.uint8), np.uint8)
     sh = _lib.stream_handle(torch)
     _lib.check(lib.dgb_from_phi2d(_lib.dptr(d_fs), ng * n, Lmax, max(n1, n2), sh),
                "dgb_from_phi2d")
     _lib.check(lib.dgb_extrap_ll(_lib.dptr(d_ex), n, float(fail_mag), sh), "dgb_extrap_ll")
+    if multinom:
+        return out.view(n, n1 + 1, n2 + 1), ll, llm
     return out.view(n, n1 + 1, n2 + 1), ll

@@ -318,13 +318,17 @@ int dgb_from_phi2d(const dgb_fs_item2d *items, int nitems, int Lmax, int nmax, v
  * (dadi/Numerics.py:449-464), written to out; with data and ll set, also the
  * Poisson log-likelihood sum(-m + d log m - lgamma(d + 1)), m = scale * out,
  * over entries with m > 0, excluding the first and last entry when
- * mask_corners (dadi/Inference.py:466-509). */
+ * mask_corners (dadi/Inference.py:466-509); with data and ll_multinom set,
+ * the multinomial log-likelihood: the same sum with scale = sum(d) / sum(out)
+ * over the entries not excluded (ll_multinom with optimal_sfs_scaling,
+ * dadi/Inference.py:559-575, 668-685). */
 typedef struct {
     const double *fs[3];
     double x[3];
     double *out;
     const double *data;       /* NULL: no likelihood */
-    double *ll;               /* one double */
+    double *ll;               /* one double (NULL: no Poisson likelihood) */
+    double *ll_multinom;      /* one double (NULL: no multinomial likelihood) */
     double scale;
     int ngrids, size, mask_corners, pad_;
 } dgb_extrap_item;

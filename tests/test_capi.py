@@ -3,6 +3,7 @@ declares; host-only entry points run without a GPU."""
 import ctypes
 import os
 import re
+import shutil
 
 import numpy as np
 import pytest
@@ -43,6 +44,42 @@ def test_struct_layout():
     assert ctypes.sizeof(_lib.PForm) == 32
     assert ctypes.sizeof(_lib.Settings) == 32
     assert ctypes.sizeof(_lib.Inst2D) == 16 + 9 * 32 + 8
+
+
+def _c_layout(tmp_path, struct, fields):
+    """sizeof(struct) and offsetof(struct, f) for each field, from the header
+    compiled by the host C compiler."""
+    src = tmp_path / "layout.c"
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "dadi_gb300.h"',
+             'int main(void) {', '    printf("%%zu\\n", sizeof(%s));' % struct]
+    lines += ['    printf("%%zu\\n", offsetof(%s, %s));' % (struct, f) for f in fields]
+    lines += ['    return 0;', '}']
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    import subprocess
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    return int(out[0]), [int(v) for v in out[1:]]
+
+
+@pytest.mark.parametrize("struct,dtype,cfields", [
+    ("dgb_extrap_item", "EX_ITEM", ["fs", "x", "out", "data", "ll", "ll_multinom", "scale",
+                                    "ngrids", "size", "mask_corners", "pad_"]),
+    ("dgb_fs_item2d", "FS_ITEM", ["phi", "xx", "d1x", "d2x", "d1y", "d2y", "out", "L", "n1",
+                                  "n2", "pad_"]),
+    ("dgb_item2d", "ITEM2D_DTYPE", ["L", "masks", "xx_off", "out_off", "sched"]),
+])
+def test_record_dtypes_match_header(tmp_path, struct, dtype, cfields):
+    """The numpy record types the host fills match the C structs byte for
+    byte (size and every field offset)."""
+    if shutil.which("gcc") is None:
+        pytest.skip("no host C compiler")
+    from dadi_gb300 import batch, epilogue
+    dt = getattr(epilogue, dtype, None) or getattr(batch, dtype)
+    size, offs = _c_layout(tmp_path, struct, cfields)
+    assert dt.itemsize == size
+    assert [dt.fields[n][1] for n in dt.names] == offs
 
 
 def test_count_steps_matches_python_schedule(lib):

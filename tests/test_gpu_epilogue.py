@@ -121,3 +121,40 @@ def test_batch_and_list_forms_agree_bitwise(cuda_lib):
         alone, ll1, _ = epilogue.spectra_2d(torch, [jobs[i]])
         assert np.array_equal(alone[0].cpu().numpy(), fs_b[i].cpu().numpy())
         assert float(ll1[0]) == float(ll_b[i]) == float(ll_l[i])
+
+
+def test_multinomial_ll_in_epilogue(cuda_lib):
+    """The multinomial log-likelihood (optimal scaling over the unmasked
+    entries, dadi/Inference.py:559-575, 668-685) from the same epilogue
+    launch: against the oracle on the device spectra and against the torch
+    form Batch2D.loglik(multinom=True); the Poisson ll of that launch is
+    bitwise the one without it."""
+    import torch
+    from dadi_gb300 import batch, epilogue
+    from oracle import numerics as onum
+    import cases
+    ns = (12, 12)
+    eng = batch.Batch2D((30, 40, 50), ns)
+    draws = cases.im_draws(5)
+    phis, _ = eng.integrate(batch.im_instances(draws))
+    fs0 = epilogue.spectra_2d_batch(torch, phis, eng.xxs, ns)[0].cpu().numpy()
+    data = np.random.default_rng(3).poisson(2e3 * np.abs(fs0[0])).astype(np.float64)
+    d_data = torch.from_numpy(data).cuda()
+    fs_p, ll_p = epilogue.spectra_2d_batch(torch, phis, eng.xxs, ns, d_data, 2e3)
+    fs_m, ll_m, llm = epilogue.spectra_2d_batch(torch, phis, eng.xxs, ns, d_data, 2e3,
+                                                multinom=True)
+    assert np.array_equal(fs_p.cpu().numpy(), fs_m.cpu().numpy())
+    assert np.array_equal(ll_p.cpu().numpy(), ll_m.cpu().numpy())
+    fs = fs_m.cpu().numpy()
+    mask = onum.corner_mask(fs[0].shape)
+    torch_llm = eng.loglik(fs_m, d_data, multinom=True).cpu().numpy()
+    for i in range(len(draws)):
+        ref = onum.ll_multinom(fs[i], data, mask)
+        theta = np.sum(data[~mask]) / np.sum(fs[i][~mask])
+        m = theta * fs[i][~mask & (fs[i] > 0)]
+        d = data[~mask & (fs[i] > 0)]
+        scale = np.sum(np.abs(m)) + np.sum(np.abs(d * np.log(m)))
+        assert abs(float(llm[i]) - ref) <= 1e-12 * scale, (float(llm[i]), ref)
+        assert abs(float(torch_llm[i]) - ref) <= 1e-12 * scale
+    _, ll2, llm2 = eng.spectra_ll(phis, d_data, 2e3, multinom=True)
+    assert np.array_equal(llm2.cpu().numpy(), llm.cpu().numpy())
