@@ -99,7 +99,7 @@ def _declare(L):
         "dgb_from_phi2d_smem_bytes": (sz, [i, i]),
         "dgb_from_phi2d": (i, [_vp, i, i, i, _vp]),
         "dgb_extrap_ll": (i, [_vp, i, d, _vp]),
-        "dgb_integrate_table_states": (i, [_vp, i, i, _vp, _vp, i, i, i, _vp, _vp]),
+        "dgb_integrate_table_states": (i, [_vp, i, i, _vp, _vp, i, i, i, _vp, _vp, sz, _vp]),
         "dgb_adjoint_table_nd_gpart_doubles": (sz, [i, i]),
         "dgb_adjoint_table_nd": (i, [_vp, i, i, _vp, _vp, i, i, i, _vp, _vp, _vp, sz, _vp]),
         "dgb_adjoint2d": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp, _vp,

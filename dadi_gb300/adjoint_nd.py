@@ -172,12 +172,12 @@ class TableModel:
             states = torch.empty(((n + 1) * L ** P if keep_states else L ** P),
                                  dtype=torch.float64, device="cuda")
             sh = _lib.stream_handle(torch)
+            ws, nws = _lib.workspace(torch, lib.dgb_workspace_bytes(0, P, L, 0))
             if keep_states:
                 _lib.check(lib.dgb_integrate_table_states(
                     _lib.dptr(d_phi), P, L, _lib.dptr(d_xx), _lib.dptr(d_tab), n, 0, 0,
-                    _lib.dptr(states), sh), "dgb_integrate_table_states")
+                    _lib.dptr(states), _lib.dptr(ws), nws, sh), "dgb_integrate_table_states")
             else:
-                ws, nws = _lib.workspace(torch, lib.dgb_workspace_bytes(0, P, L, 0))
                 _lib.check(lib.dgb_integrate_table(
                     _lib.dptr(d_phi), P, L, _lib.dptr(d_xx), _lib.dptr(d_tab), n, 0, 0, 0,
                     _lib.dptr(ws), nws, sh), "dgb_integrate_table")
@@ -234,7 +234,7 @@ class TableModel:
             lam = (lam if lam is not None else torch.zeros_like(r["phi"])).contiguous().clone()
             per = lib.dgb_adjoint_table_nd_gpart_doubles(P, L)
             gpart = torch.empty(n * per, dtype=torch.float64, device="cuda")
-            ws, nws = _lib.workspace(torch, max(P - 1, 1) * L ** P * 8)
+            ws, nws = _lib.workspace(torch, lib.dgb_workspace_bytes(4, P, L, 0))
             _lib.check(lib.dgb_adjoint_table_nd(
                 _lib.dptr(lam), P, L, _lib.dptr(r["d_xx"]), _lib.dptr(r["d_tab"]), n, 0, 0,
                 _lib.dptr(r["states"]), _lib.dptr(gpart), _lib.dptr(ws), nws,

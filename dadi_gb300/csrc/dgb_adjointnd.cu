@@ -236,7 +236,8 @@ using namespace dgb;
 
 extern "C" int dgb_integrate_table_states(double *phi, int ndim, int L, const double *xx,
                                           const double *table, int nsteps, int frozen_mask,
-                                          int nomut_mask, double *states, void *stream)
+                                          int nomut_mask, double *states, void *ws,
+                                          size_t ws_bytes, void *stream)
 {
     if (!phi || !xx || !table || !states || !shape_ok(ndim, L) || nsteps < 0)
         return DGB_ERR_ARG;
@@ -246,12 +247,22 @@ extern "C" int dgb_integrate_table_states(double *phi, int ndim, int L, const do
     NDArgs A = {};
     nd_fill(A, phi, ndim, L, 0, xx);
     A.table = table;
+    double *coef = (ws && ws_bytes >= nd_coef_bytes(ndim, L)) ? (double *)ws : nullptr;
+    const int chunk = nd_chunk_steps(ndim, L);
+    long step0 = 0;
     for (long s = 0; s <= nsteps; s++) {
         if (cudaMemcpyAsync(states + s * N, phi, N * sizeof(double), cudaMemcpyDeviceToDevice,
                             st) != cudaSuccess)
             return DGB_ERR_CUDA;
         if (s == nsteps)
             break;
+        if (coef && s % chunk == 0) {
+            step0 = s;
+            int rc = nd_coef_chunk(A, false, s, (int)std::min<long>(chunk, nsteps - s),
+                                   frozen_mask, active, coef, st);
+            if (rc)
+                return rc;
+        }
         bool first = true;
         for (int ax = 0; ax < ndim; ax++) {
             if (frozen_mask >> ax & 1)
@@ -260,7 +271,7 @@ extern "C" int dgb_integrate_table_states(double *phi, int ndim, int L, const do
             A.step = s;
             A.inject_mask = first ? active : 0;
             first = false;
-            int rc = nd_sweep(A, false, st);
+            int rc = coef ? nd_sweep_rec(A, false, coef, step0, st) : nd_sweep(A, false, st);
             if (rc)
                 return rc;
         }
@@ -306,8 +317,22 @@ extern "C" int dgb_adjoint_table_nd(double *lam, int ndim, int L, const double *
     NDArgs F = {};
     nd_fill(F, nullptr, ndim, L, 0, xx);
     F.table = table;
+    // coefficient records of the recomputed sweeps, after the intermediate
+    // densities when the workspace holds them; chunks walk backwards
+    const size_t inter = (size_t)(na - 1) * N * sizeof(double);
+    double *coef = (na > 1 && ws_bytes >= inter + nd_coef_bytes(ndim, L))
+                       ? ws + (size_t)(na - 1) * N
+                       : nullptr;
+    const int chunk = nd_chunk_steps(ndim, L);
+    long lo = -1;
     for (long k = nsteps - 1; k >= 0; k--) {
         const double *phik = states + k * N, *phin = states + (k + 1) * N;
+        if (coef && (lo < 0 || k < lo)) {
+            lo = std::max(0L, k - chunk + 1);
+            int rc = nd_coef_chunk(F, false, lo, (int)(k - lo + 1), frozen_mask, active, coef, st);
+            if (rc)
+                return rc;
+        }
         // recompute s_1 .. s_{na-1} into ws
         for (int j = 0; j < na - 1; j++) {
             double *dst = ws + (size_t)j * N;
@@ -319,7 +344,7 @@ extern "C" int dgb_adjoint_table_nd(double *lam, int ndim, int L, const double *
             nd_set_axis(F, axes[j]);
             F.step = k;
             F.inject_mask = j ? 0 : active;
-            int rc = nd_sweep(F, false, st);
+            int rc = coef ? nd_sweep_rec(F, false, coef, lo, st) : nd_sweep(F, false, st);
             if (rc)
                 return rc;
         }

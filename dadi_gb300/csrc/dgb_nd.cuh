@@ -37,6 +37,68 @@ struct NDShared {
     double inj[DGB_MAX_DIM];
 };
 
+// Per-step coefficient records (k_coef_nd -> k_sweep_nd_rec, dgb_sweepnd.cu).
+// A coefficient buffer holds the grid constants (x, xv, dfac, xInt, ih, dx:
+// 6 L doubles, the GridVecs order) followed by one record per (step of the
+// chunk, axis): the head (the axis scalars and the injection amounts), then
+// the per-axis vectors A1, A0, C1, C0, B0 and, with the delj trick, G, Pv,
+// Qv, VI, DF (L doubles each).
+struct NDRecHead {
+    AxisScalars s;
+    double inj[DGB_MAX_DIM];
+};
+constexpr int ND_HEAD = (int)(sizeof(NDRecHead) / sizeof(double));
+static_assert(sizeof(NDRecHead) == ND_HEAD * sizeof(double), "record head is whole doubles");
+
+__host__ __device__ inline int nd_grid_doubles(int L) { return 6 * L; }
+
+__host__ __device__ inline size_t nd_rec_doubles(int L, bool delj)
+{
+    return (size_t)ND_HEAD + (size_t)(delj ? 10 : 5) * L;
+}
+
+// The per-axis vectors laid out from p on (a record's vectors start at
+// rec + ND_HEAD).
+__host__ __device__ inline void nd_vecs_at(double *p, int L, bool delj, AxisVecs &v)
+{
+    v.A1 = p;
+    v.A0 = p + L;
+    v.C1 = p + 2 * L;
+    v.C0 = p + 3 * L;
+    v.B0 = p + 4 * L;
+    v.G = v.Pv = v.Qv = v.VI = v.DF = nullptr;
+    if (delj) {
+        v.G = p + 5 * L;
+        v.Pv = p + 6 * L;
+        v.Qv = p + 7 * L;
+        v.VI = p + 8 * L;
+        v.DF = p + 9 * L;
+    }
+}
+
+// Shared memory of k_sweep_nd_rec: the tile, gam, x/xInt/dx and the vectors.
+__host__ __device__ inline size_t nd_rec_smem_doubles(int L, int nt, bool delj)
+{
+    return (size_t)L * (nt + 1) + (size_t)L * nt + 3 * (size_t)L + (size_t)(delj ? 10 : 5) * L;
+}
+
+// Steps per coefficient chunk: up to 256, with the records of a chunk kept
+// under 8 MB (sized for the delj layout, so one chunk length serves both).
+__host__ __device__ inline int nd_chunk_steps(int ndim, int L)
+{
+    const size_t per_step = (size_t)ndim * nd_rec_doubles(L, true) * sizeof(double);
+    size_t c = ((size_t)8 << 20) / per_step;
+    return (int)(c < 1 ? 1 : (c > 256 ? 256 : c));
+}
+
+// Bytes of a coefficient buffer for chunks of nd_chunk_steps steps.
+inline size_t nd_coef_bytes(int ndim, int L)
+{
+    return ((size_t)nd_grid_doubles(L) +
+            (size_t)nd_chunk_steps(ndim, L) * ndim * nd_rec_doubles(L, true)) *
+           sizeof(double);
+}
+
 // Coordinates (all axes) of the first point of line `line` along `axis`.
 __device__ __forceinline__ long nd_line_base(const NDArgs &A, long line, int *coord)
 {
@@ -216,5 +278,15 @@ static bool shape_ok(int ndim, int L) { return ndim >= 1 && ndim <= DGB_MAX_DIM 
 
 // One launch of the forward per-axis sweep (k_sweep_nd, dgb_sweepnd.cu).
 int nd_sweep(NDArgs &A, bool delj, cudaStream_t st);
+
+// Coefficient records of steps step0 .. step0+n-1 of A's table (every
+// unfrozen axis; the step's first swept axis injects `active`) into coef,
+// a buffer of nd_coef_bytes; n <= nd_chunk_steps.
+int nd_coef_chunk(const NDArgs &A, bool delj, long step0, int n, int frozen_mask, int active,
+                  double *coef, cudaStream_t st);
+
+// One sweep (A.axis, A.step, A.inject_mask) reading the records that
+// nd_coef_chunk wrote for the chunk starting at step0.
+int nd_sweep_rec(NDArgs &A, bool delj, const double *coef, long step0, cudaStream_t st);
 
 } // namespace dgb

@@ -23,12 +23,71 @@
 
 namespace dgb {
 
+// Solve the CTA's tile of lines [l0, l0+n) in shared memory: per line the
+// migration weight W and the corner flags from its other coordinates, the
+// fused mutation injection (dadi/Integration.py:70-122) when this is the
+// step's first sweep, then the Thomas solve.
+template <bool DELJ>
+__device__ __forceinline__ void nd_solve_tile(const NDArgs &A, double *tile, double *gam, int nt,
+                                              long l0, int n, const GridVecs &g,
+                                              const AxisVecs &v, const AxisScalars &s,
+                                              const double *inj)
+{
+    const int L = A.L, P = A.ndim, ax = A.axis;
+    // grid index of the corner coordinates (value exactly 0 / 1)
+    const int j0 = (g.x[0] == 0.0) ? 0 : -1;
+    const int j1 = (g.x[L - 1] == 1.0) ? L - 1 : -1;
+    const int t = threadIdx.x;
+    if (t >= n)
+        return;
+    int coord[DGB_MAX_DIM];
+    nd_line_base(A, l0 + t, coord);
+    double W = 0;
+    double mo[DGB_MAX_DIM], oo[DGB_MAX_DIM];
+    int no = 0;
+    bool all0 = true, all1 = true;
+    int n1 = 0, k1 = -1;
+    for (int k = 0; k < P; k++) {
+        if (k == ax)
+            continue;
+        W = fma(s.mig[k], g.x[coord[k]], W);
+        mo[no] = s.mig[k];
+        oo[no] = g.x[coord[k]];
+        no++;
+        all0 = all0 && coord[k] == j0;
+        all1 = all1 && coord[k] == j1;
+        if (coord[k] == 1) {
+            n1++;
+            k1 = k;
+        } else if (coord[k] != 0) {
+            n1 = 99;
+        }
+    }
+    if (P == 1)
+        all0 = all1 = true; // 1-D applies both boundary terms unconditionally
+    const int tp = nt + 1;
+    if (A.inject_mask) {
+        if (n1 == 0 && inj[ax] != 0.0)
+            tile[1 * tp + t] += inj[ax];
+        if (n1 == 1 && inj[k1] != 0.0)
+            tile[0 * tp + t] += inj[k1];
+    }
+    double bs = all0 ? s.bcs : 0.0;
+    double be = all1 ? s.bce : 0.0;
+    if (DELJ)
+        solve_line_delj(tile + t, tp, gam + t, nt, L, mo, oo, no, bs, be, g, v);
+    else
+        solve_line(tile + t, tp, gam + t, nt, L, W, bs, be, v, s);
+}
+
+// Sweep that builds its own step's coefficients: grid constants, the
+// parameter row (one thread) and the per-axis vectors, every CTA.
 template <bool DELJ>
 __global__ void k_sweep_nd(NDArgs A)
 {
     extern __shared__ __align__(16) double smem[];
     __shared__ NDShared Sh;
-    const int nt = blockDim.x, L = A.L, P = A.ndim, ax = A.axis;
+    const int nt = blockDim.x, L = A.L;
     double *tile, *gam;
     GridVecs g;
     AxisVecs v;
@@ -43,51 +102,102 @@ __global__ void k_sweep_nd(NDArgs A)
     const int n = (int)min((long)nt, A.nlines - l0);
     nd_tile_io(A, tile, nt, l0, n, false);
     __syncthreads();
-    // grid index of the corner coordinates (value exactly 0 / 1)
-    const int j0 = (g.x[0] == 0.0) ? 0 : -1;
-    const int j1 = (g.x[L - 1] == 1.0) ? L - 1 : -1;
-    const int t = threadIdx.x;
-    if (t < n) {
-        int coord[DGB_MAX_DIM];
-        nd_line_base(A, l0 + t, coord);
-        double W = 0;
-        double mo[DGB_MAX_DIM], oo[DGB_MAX_DIM];
-        int no = 0;
-        bool all0 = true, all1 = true;
-        int n1 = 0, k1 = -1;
-        for (int k = 0; k < P; k++) {
-            if (k == ax)
-                continue;
-            W = fma(Sh.s.mig[k], g.x[coord[k]], W);
-            mo[no] = Sh.s.mig[k];
-            oo[no] = g.x[coord[k]];
-            no++;
-            all0 = all0 && coord[k] == j0;
-            all1 = all1 && coord[k] == j1;
-            if (coord[k] == 1) {
-                n1++;
-                k1 = k;
-            } else if (coord[k] != 0) {
-                n1 = 99;
-            }
-        }
-        if (P == 1)
-            all0 = all1 = true; // 1-D applies both boundary terms unconditionally
-        const int tp = nt + 1;
-        // fused mutation injection (dadi/Integration.py:70-122)
-        if (A.inject_mask) {
-            if (n1 == 0 && Sh.inj[ax] != 0.0)
-                tile[1 * tp + t] += Sh.inj[ax];
-            if (n1 == 1 && Sh.inj[k1] != 0.0)
-                tile[0 * tp + t] += Sh.inj[k1];
-        }
-        double bs = all0 ? Sh.s.bcs : 0.0;
-        double be = all1 ? Sh.s.bce : 0.0;
-        if (DELJ)
-            solve_line_delj(tile + t, tp, gam + t, nt, L, mo, oo, no, bs, be, g, v);
-        else
-            solve_line(tile + t, tp, gam + t, nt, L, W, bs, be, v, Sh.s);
+    nd_solve_tile<DELJ>(A, tile, gam, nt, l0, n, g, v, Sh.s, Sh.inj);
+    __syncthreads();
+    nd_tile_io(A, tile, nt, l0, n, true);
+}
+
+// Per-step coefficient records of a chunk of steps: one CTA per (step,
+// axis) runs the setup k_sweep_nd repeats in every CTA -- grid constants,
+// the parameter row, the per-axis vectors -- once, and stores it (layout in
+// dgb_nd.cuh).  The CTA of the chunk's first step and first swept axis also
+// stores the grid constants.  Same functions, same arithmetic: the sweeps
+// that read the records compute what k_sweep_nd computes.
+template <bool DELJ>
+__global__ void k_coef_nd(NDArgs A, long step0, int frozen_mask, int active, double *coef)
+{
+    extern __shared__ __align__(16) double smem[];
+    __shared__ NDShared Sh;
+    const int P = A.ndim, L = A.L;
+    const int ax = (int)(blockIdx.x % P);
+    const long sl = blockIdx.x / P;
+    if (frozen_mask >> ax & 1)
+        return; // the whole CTA: no barrier is skipped by part of it
+    int first = 0;
+    while (frozen_mask >> first & 1)
+        first++;
+    GridVecs g;
+    g.x = smem;
+    g.xv = smem + L;
+    g.dfac = smem + 2 * L;
+    g.xInt = smem + 3 * L;
+    g.ih = smem + 4 * L;
+    g.dx = smem + 5 * L;
+    NDArgs B = A;
+    B.axis = ax;
+    B.step = step0 + sl;
+    B.inject_mask = (ax == first) ? active : 0;
+    nd_grid_consts(B, g);
+    if (threadIdx.x == 0)
+        nd_load_params(B, Sh, g);
+    __syncthreads();
+    double *rec = coef + nd_grid_doubles(L) + ((size_t)sl * P + ax) * nd_rec_doubles(L, DELJ);
+    AxisVecs v;
+    nd_vecs_at(rec + ND_HEAD, L, DELJ, v);
+    for (int i = threadIdx.x; i < L; i += blockDim.x)
+        build_axis_entry(i, L, g, Sh.s, Sh.vscale, DELJ, v);
+    if (threadIdx.x == 0) {
+        NDRecHead h;
+        h.s = Sh.s;
+        for (int k = 0; k < DGB_MAX_DIM; k++)
+            h.inj[k] = Sh.inj[k];
+        const double *hp = reinterpret_cast<const double *>(&h);
+        for (int k = 0; k < ND_HEAD; k++)
+            rec[k] = hp[k];
     }
+    if (sl == 0 && ax == first)
+        for (int i = threadIdx.x; i < nd_grid_doubles(L); i += blockDim.x)
+            coef[i] = smem[i];
+}
+
+// Sweep that reads its step's coefficients from the records of k_coef_nd:
+// one coalesced copy of O(L) doubles per CTA instead of the FP64 setup.
+template <bool DELJ>
+__global__ void k_sweep_nd_rec(NDArgs A, const double *coef, long step0)
+{
+    extern __shared__ __align__(16) double smem[];
+    __shared__ NDRecHead H;
+    const int nt = blockDim.x, L = A.L, P = A.ndim;
+    constexpr int NV = DELJ ? 10 : 5;
+    double *tile = smem;
+    double *gam = tile + (size_t)L * (nt + 1);
+    double *gx = gam + (size_t)L * nt; // x, xInt, dx
+    double *vv = gx + 3 * (size_t)L;
+    const double *rec =
+        coef + nd_grid_doubles(L) + ((size_t)(A.step - step0) * P + A.axis) * nd_rec_doubles(L, DELJ);
+    double *hp = reinterpret_cast<double *>(&H);
+    for (int i = threadIdx.x; i < ND_HEAD; i += nt)
+        hp[i] = rec[i];
+    for (int i = threadIdx.x; i < NV * L; i += nt)
+        vv[i] = rec[ND_HEAD + i];
+    for (int i = threadIdx.x; i < L; i += nt) {
+        gx[i] = coef[i];
+        if (DELJ) {
+            gx[L + i] = coef[3 * L + i];
+            gx[2 * L + i] = coef[5 * L + i];
+        }
+    }
+    GridVecs g = {};
+    g.x = gx;
+    g.xInt = gx + L;
+    g.dx = gx + 2 * L;
+    AxisVecs v;
+    nd_vecs_at(vv, L, DELJ, v);
+    const long l0 = (long)blockIdx.x * nt;
+    const int n = (int)min((long)nt, A.nlines - l0);
+    nd_tile_io(A, tile, nt, l0, n, false);
+    __syncthreads();
+    nd_solve_tile<DELJ>(A, tile, gam, nt, l0, n, g, v, H.s, H.inj);
     __syncthreads();
     nd_tile_io(A, tile, nt, l0, n, true);
 }
@@ -208,6 +318,42 @@ static int nd_launch_precalc(NDArgs &A, cudaStream_t st)
 
 int nd_sweep(NDArgs &A, bool delj, cudaStream_t st) { return nd_launch_sweep(A, delj, st); }
 
+int nd_coef_chunk(const NDArgs &A, bool delj, long step0, int n, int frozen_mask, int active,
+                  double *coef, cudaStream_t st)
+{
+    if (n < 1 || n > nd_chunk_steps(A.ndim, A.L) || !A.table)
+        return DGB_ERR_ARG;
+    const size_t smem = (size_t)nd_grid_doubles(A.L) * sizeof(double);
+    const unsigned grid = (unsigned)(n * A.ndim);
+    if (delj) {
+        if (raise_smem_limit(k_coef_nd<true>))
+            return DGB_ERR_CUDA;
+        k_coef_nd<true><<<grid, 128, smem, st>>>(A, step0, frozen_mask, active, coef);
+    } else {
+        if (raise_smem_limit(k_coef_nd<false>))
+            return DGB_ERR_CUDA;
+        k_coef_nd<false><<<grid, 128, smem, st>>>(A, step0, frozen_mask, active, coef);
+    }
+    return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
+}
+
+int nd_sweep_rec(NDArgs &A, bool delj, const double *coef, long step0, cudaStream_t st)
+{
+    const int nt = nd_threads(A.L, A.nlines);
+    const size_t smem = nd_rec_smem_doubles(A.L, nt, delj) * sizeof(double);
+    const long nblocks = (A.nlines + nt - 1) / nt;
+    if (delj) {
+        if (raise_smem_limit(k_sweep_nd_rec<true>))
+            return DGB_ERR_CUDA;
+        k_sweep_nd_rec<true><<<(unsigned)nblocks, nt, smem, st>>>(A, coef, step0);
+    } else {
+        if (raise_smem_limit(k_sweep_nd_rec<false>))
+            return DGB_ERR_CUDA;
+        k_sweep_nd_rec<false><<<(unsigned)nblocks, nt, smem, st>>>(A, coef, step0);
+    }
+    return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
+}
+
 } // namespace dgb
 
 using namespace dgb;
@@ -239,14 +385,22 @@ extern "C" const char *dgb_status_string(int status)
 
 extern "C" size_t dgb_workspace_bytes(int kind, int ndim, int L, long n)
 {
-    if (kind == 0)
-        return (ndim == 2) ? k2_table_ws_bytes(L) : 0;
+    if (kind == 0) {
+        // the shared-memory 2-D integrator's scratch, or the coefficient
+        // records of the per-axis sweeps
+        if (ndim == 2 && k2_smem_fits(L, false, true, nullptr))
+            return k2_table_ws_bytes(L);
+        return std::max(ndim == 2 ? k2_table_ws_bytes(L) : (size_t)0, nd_coef_bytes(ndim, L));
+    }
     if (kind == 1)
         return k2_batch_ws_bytes(L, n);
     if (kind == 2)
         return (size_t)n * L * sizeof(double);
     if (kind == 3) // any gam placement: a slice per work item
         return 256 + (size_t)n * L * L * sizeof(double);
+    if (kind == 4) // recomputed intermediate densities + coefficient records
+        return (size_t)std::max(ndim - 1, 1) * ipow(L, ndim) * sizeof(double) +
+               nd_coef_bytes(ndim, L);
     return 0;
 }
 
@@ -319,11 +473,24 @@ extern "C" int dgb_integrate_table(double *phi, int ndim, int L, const double *x
         return k2_integrate_table(phi, L, xx, table, nsteps, frozen_mask, nomut_mask,
                                   use_delj_trick, ws, ws_bytes, st);
     const int active = ((1 << ndim) - 1) & ~frozen_mask & ~nomut_mask;
+    const bool delj = use_delj_trick != 0;
     NDArgs A = {};
     nd_fill(A, phi, ndim, L, 0, xx);
     int rc = DGB_OK;
     A.table = table;
+    // with room for them in the workspace, each chunk of steps gets its
+    // coefficient records from one launch, and the sweeps only read them
+    double *coef = (ws && ws_bytes >= nd_coef_bytes(ndim, L)) ? (double *)ws : nullptr;
+    const int chunk = nd_chunk_steps(ndim, L);
+    long step0 = 0;
     for (long s = 0; s < nsteps; s++) {
+        if (coef && s % chunk == 0) {
+            step0 = s;
+            rc = nd_coef_chunk(A, delj, s, (int)std::min<long>(chunk, nsteps - s), frozen_mask,
+                               active, coef, st);
+            if (rc)
+                return rc;
+        }
         bool first = true;
         for (int ax = 0; ax < ndim; ax++) {
             if (frozen_mask >> ax & 1)
@@ -334,7 +501,7 @@ extern "C" int dgb_integrate_table(double *phi, int ndim, int L, const double *x
             A.step = s;
             A.inject_mask = first ? active : 0;
             first = false;
-            rc = nd_launch_sweep(A, use_delj_trick != 0, st);
+            rc = coef ? nd_sweep_rec(A, delj, coef, step0, st) : nd_launch_sweep(A, delj, st);
             if (rc)
                 return rc;
         }

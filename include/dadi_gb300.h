@@ -78,9 +78,12 @@ int dgb_abi_version(void);
 const char *dgb_status_string(int status);
 
 /* Scratch bytes needed by a call.  kind: 0 = dgb_integrate_table /
- * dgb_integrate_precalc / the single sweeps, 1 = dgb_batch2d_integrate and
- * dgb_items2d_integrate (with n = number of work items), 2 =
- * dgb_tridiag_batch, 3 = dgb_items2d_integrate with one_per_cta. */
+ * dgb_integrate_table_states / dgb_integrate_precalc / the single sweeps
+ * (for 3-5 populations and 2-D grids too large for shared memory: per-step
+ * coefficient records, see dgb_integrate_table), 1 = dgb_batch2d_integrate
+ * and dgb_items2d_integrate (with n = number of work items), 2 =
+ * dgb_tridiag_batch, 3 = dgb_items2d_integrate with one_per_cta, 4 =
+ * dgb_adjoint_table_nd. */
 size_t dgb_workspace_bytes(int kind, int ndim, int L, long n);
 
 /* Batched Numerical-Recipes tridiagonal solve of `batch` independent systems
@@ -271,7 +274,8 @@ int dgb_batch2d_count_steps(const dgb_inst2d *insts, int ninst,
  * dgb_integrate_table_states: dgb_integrate_table through the per-axis
  * sweeps that also records the density at the start of every step and at the
  * end: states (device) holds (nsteps + 1) x L^ndim doubles.  (The delj trick
- * is not differentiated.)
+ * is not differentiated.)  ws: as dgb_integrate_table (kind 0); a smaller
+ * workspace (or none) only costs speed.
  *
  * dgb_adjoint_table_nd: lam (device, L^ndim) holds dJ/dphi_final on entry
  * and dJ/dphi_initial on exit; gpart (device,
@@ -280,12 +284,15 @@ int dgb_batch2d_count_steps(const dgb_inst2d *insts, int ninst,
  * one DGB_ROW_STRIDE(ndim) row per CTA of that sweep, followed by two
  * doubles, the injection's dJ/d(dt) and dJ/d(theta0).  Summing a step's
  * rows (any fixed order) and adding those two to entries 0 and 1 gives
- * dJ/d(row) for that step.  ws: (active axes - 1) x L^ndim doubles.  The
+ * dJ/d(row) for that step.  ws: (active axes - 1) x L^ndim doubles, and
+ * with dgb_workspace_bytes(4, ...) bytes also the coefficient records of the
+ * recomputed sweeps (faster, same results).  The
  * reference has no adjoint; its gradients come from finite differences
  * (dadi/Godambe.py:131-185). */
 int dgb_integrate_table_states(double *phi, int ndim, int L, const double *xx,
                                const double *table, int nsteps, int frozen_mask,
-                               int nomut_mask, double *states, void *stream);
+                               int nomut_mask, double *states, void *ws, size_t ws_bytes,
+                               void *stream);
 size_t dgb_adjoint_table_nd_gpart_doubles(int ndim, int L);
 int dgb_adjoint_table_nd(double *lam, int ndim, int L, const double *xx, const double *table,
                          int nsteps, int frozen_mask, int nomut_mask, const double *states,

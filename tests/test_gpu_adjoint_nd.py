@@ -83,3 +83,49 @@ def test_many_sets_concurrently_equal_one_at_a_time(cuda_lib):
         ll1, g1, _ = model.loglik_and_grad(t, data, 10.0)
         assert float(ll) == float(ll1)
         assert np.array_equal(g.cpu().numpy(), g1.cpu().numpy())
+
+
+@pytest.mark.parametrize("P,L,frozen", [(3, 14, 0), (3, 12, 4), (4, 8, 0)])
+def test_adjoint_records_match_inline_setup(cuda_lib, P, L, frozen):
+    """dgb_integrate_table_states and dgb_adjoint_table_nd give bitwise the
+    same states, dJ/dphi_initial and per-step row gradients whether the
+    recomputed sweeps read coefficient records (workspace kind 4) or build
+    their coefficients in every CTA (the minimal workspace), over 300 steps
+    (more than one chunk of records, walked backwards)."""
+    import torch
+    from dadi_gb300 import _lib, integration as gi
+    import cases
+    from util import table_rows
+    lib = cuda_lib
+    xx = cases.grid("default", L)
+    N = L ** P
+    tab = table_rows(P, 300, seed=7 * P + L)
+    n = len(tab)
+    d_xx = torch.from_numpy(xx).cuda()
+    d_tab = torch.from_numpy(tab).cuda()
+    phi0 = np.abs(cases.initial_phi(5, (L,) * P)) + 1e-3
+    lam0 = cases.initial_phi(6, (L,) * P) - 0.5
+    na = P - bin(frozen).count("1")
+    per = lib.dgb_adjoint_table_nd_gpart_doubles(P, L)
+    sh = _lib.stream_handle(torch)
+    res = []
+    for fwd_ws, adj_ws in ((0, (na - 1) * N * 8), (lib.dgb_workspace_bytes(0, P, L, 0),
+                                                    lib.dgb_workspace_bytes(4, P, L, 0))):
+        d_phi = torch.from_numpy(phi0.copy()).cuda()
+        states = torch.empty((n + 1) * N, dtype=torch.float64, device="cuda")
+        ws, nws = _lib.workspace(torch, fwd_ws)
+        _lib.check(lib.dgb_integrate_table_states(
+            _lib.dptr(d_phi), P, L, _lib.dptr(d_xx), _lib.dptr(d_tab), n, frozen, 0,
+            _lib.dptr(states), _lib.dptr(ws) if fwd_ws else None, fwd_ws, sh),
+            "dgb_integrate_table_states")
+        lam = torch.from_numpy(lam0.copy()).cuda()
+        gpart = torch.empty(n * per, dtype=torch.float64, device="cuda")
+        ws2, nws2 = _lib.workspace(torch, adj_ws)
+        _lib.check(lib.dgb_adjoint_table_nd(
+            _lib.dptr(lam), P, L, _lib.dptr(d_xx), _lib.dptr(d_tab), n, frozen, 0,
+            _lib.dptr(states), _lib.dptr(gpart), _lib.dptr(ws2), nws2, sh),
+            "dgb_adjoint_table_nd")
+        res.append((states.cpu().numpy(), lam.cpu().numpy(), gpart.cpu().numpy()))
+    for a, b in zip(res[0], res[1]):
+        assert np.all(np.isfinite(a))
+        assert np.array_equal(a, b)

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 import cases
-from util import ALL_CASES, assert_fs_parity, case_inputs, fs_parity, max_rel
+from util import ALL_CASES, assert_fs_parity, case_inputs, fs_parity, max_rel, table_rows
 
 pytestmark = pytest.mark.gpu
 
@@ -290,3 +290,32 @@ def test_dadi_settings(cuda_lib, golden, name, kw):
     finally:
         for k, v in saved.items():
             setattr(gi, k, v)
+
+
+@pytest.mark.parametrize("P,L,delj,frozen", [(3, 20, 0, 0), (3, 20, 1, 0), (3, 16, 0, 1),
+                                             (4, 10, 0, 0), (4, 10, 1, 2), (1, 60, 0, 0),
+                                             (1, 60, 1, 0), (2, 180, 0, 0), (5, 7, 0, 0)])
+def test_coefficient_records_match_inline_setup(cuda_lib, P, L, delj, frozen):
+    """The per-axis sweeps that read per-step coefficient records (the
+    workspace holds them) give bitwise the densities of the sweeps that build
+    their coefficients in every CTA (no workspace), over 300 steps -- more
+    than one chunk of records -- with and without the delj trick and frozen
+    populations."""
+    import torch
+    from dadi_gb300 import _lib
+    lib = cuda_lib
+    xx = cases.grid("default", L)
+    phi0 = np.abs(cases.initial_phi(11, (L,) * P)) + 1e-3
+    tab = table_rows(P, 300, seed=P * 100 + L)
+    d_xx, d_tab = _dev(torch, xx), _dev(torch, tab)
+    outs = []
+    for ws_bytes in (0, lib.dgb_workspace_bytes(0, P, L, 0)):
+        d_phi = _dev(torch, phi0)
+        ws, nws = _lib.workspace(torch, ws_bytes)
+        _lib.check(lib.dgb_integrate_table(_lib.dptr(d_phi), P, L, _lib.dptr(d_xx),
+                                           _lib.dptr(d_tab), len(tab), frozen, 0, delj,
+                                           _lib.dptr(ws) if ws_bytes else None, ws_bytes,
+                                           _lib.stream_handle(torch)), "dgb_integrate_table")
+        outs.append(d_phi.cpu().numpy())
+    assert np.all(np.isfinite(outs[0]))
+    assert np.array_equal(outs[0], outs[1])

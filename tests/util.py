@@ -61,3 +61,20 @@ def assert_fs_parity(fs, ref):
     rel_big, abs_small, n_small = fs_parity(fs, ref)
     assert rel_big <= FS_REL, (rel_big, n_small)
     assert abs_small <= FS_REL * TINY_FRAC, (abs_small, n_small)
+
+
+def table_rows(P, nsteps, seed):
+    """A parameter table of nsteps rows for P populations: varying sizes,
+    migration, selection and dominance (row layout of build_table)."""
+    from dadi_gb300 import integration as gi
+    rng = np.random.default_rng(seed)
+    tab = np.empty((nsteps, gi.row_stride(P)))
+    tab[:, 0] = rng.uniform(2e-4, 1e-3, nsteps)          # dt
+    tab[:, 1] = rng.uniform(0.5, 2.0, nsteps)            # theta0
+    tab[:, 2:2 + P] = rng.uniform(0.2, 5.0, (nsteps, P))  # nu
+    tab[:, 2 + P:2 + 2 * P] = rng.uniform(-5, 5, (nsteps, P))  # gamma
+    tab[:, 2 + 2 * P:2 + 3 * P] = rng.uniform(0.1, 0.9, (nsteps, P))  # h
+    tab[:, 2 + 3 * P] = 1.0 if P > 1 else rng.uniform(0.5, 2.0, nsteps)  # beta
+    tab[:, 3 + 3 * P:] = rng.uniform(0, 3, (nsteps, P * (P - 1)))  # migration
+    return tab
+
