@@ -35,6 +35,8 @@ struct ADNArgs {
     const double *out;  // this sweep's forward output s_j
     const double *rhs;  // this sweep's forward input s_{j-1} (psi without injection)
     double *gpart;      // per CTA: row_stride(P) doubles
+    const double *coef; // coefficient records of the chunk from step0 (null: build inline)
+    long step0;
 };
 
 __host__ __device__ inline size_t adn_smem_doubles(int L, int nt)
@@ -60,12 +62,30 @@ __global__ void k_adjoint_sweep_nd(ADNArgs A)
     vt.C1 = p; p += L;
     vt.C0 = p; p += L;
     vt.B0 = p;
-    nd_grid_consts(N, g);
-    if (tid == 0)
-        nd_load_params(N, Sh, g);
-    __syncthreads();
-    for (int i = tid; i < L; i += nt)
-        build_axis_entry(i, L, g, Sh.s, Sh.vscale, false, v);
+    if (A.coef) {
+        // the grid constants and this step's record, in the carve order
+        const double *rec = A.coef + nd_grid_doubles(L) +
+                            ((size_t)(N.step - A.step0) * P + ax) * nd_rec_doubles(L, false);
+        constexpr int NS = (int)(sizeof(AxisScalars) / sizeof(double));
+        double *sp = reinterpret_cast<double *>(&Sh.s);
+        for (int i = tid; i < nd_grid_doubles(L); i += nt)
+            g.x[i] = A.coef[i];
+        for (int i = tid; i < 5 * L; i += nt)
+            v.A1[i] = rec[ND_HEAD + i];
+        for (int i = tid; i < ND_HEAD; i += nt) {
+            if (i < NS)
+                sp[i] = rec[i];
+            else
+                Sh.inj[i - NS] = rec[i];
+        }
+    } else {
+        nd_grid_consts(N, g);
+        if (tid == 0)
+            nd_load_params(N, Sh, g);
+        __syncthreads();
+        for (int i = tid; i < L; i += nt)
+            build_axis_entry(i, L, g, Sh.s, Sh.vscale, false, v);
+    }
     __syncthreads();
     for (int i = tid; i < L; i += nt) {
         vt.A1[i] = (i > 0) ? v.C1[i - 1] : 0.0;
@@ -317,12 +337,12 @@ extern "C" int dgb_adjoint_table_nd(double *lam, int ndim, int L, const double *
     NDArgs F = {};
     nd_fill(F, nullptr, ndim, L, 0, xx);
     F.table = table;
-    // coefficient records of the recomputed sweeps, after the intermediate
-    // densities when the workspace holds them; chunks walk backwards
+    // coefficient records of the step's sweeps (recomputed forward and
+    // adjoint), after the intermediate densities when the workspace holds
+    // them; chunks walk backwards
     const size_t inter = (size_t)(na - 1) * N * sizeof(double);
-    double *coef = (na > 1 && ws_bytes >= inter + nd_coef_bytes(ndim, L))
-                       ? ws + (size_t)(na - 1) * N
-                       : nullptr;
+    double *coef =
+        (ws_bytes >= inter + nd_coef_bytes(ndim, L)) ? ws + (size_t)(na - 1) * N : nullptr;
     const int chunk = nd_chunk_steps(ndim, L);
     long lo = -1;
     for (long k = nsteps - 1; k >= 0; k--) {
@@ -359,6 +379,8 @@ extern "C" int dgb_adjoint_table_nd(double *lam, int ndim, int L, const double *
             A.out = (j == na - 1) ? phin : ws + (size_t)j * N;
             A.rhs = j ? ws + (size_t)(j - 1) * N : phik;
             A.gpart = gk + (size_t)j * nb * stride;
+            A.coef = coef;
+            A.step0 = lo;
             int rc = adn_launch(A, st);
             if (rc)
                 return rc;

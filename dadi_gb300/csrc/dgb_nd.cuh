@@ -209,7 +209,9 @@ __device__ __forceinline__ void nd_carve(double *smem, int L, int nt, bool delj,
     }
 }
 
-// Load (dir=0) or store (dir=1) the CTA's tile of lines [l0, l0+n).
+// Load (dir=0) or store (dir=1) the CTA's tile of lines [l0, l0+n).  (Moving
+// each thread's elements in batches of 8 loads in flight measured no faster
+// on 3-D grids of L = 70-90: the sweep's time is its solve.)
 __device__ __forceinline__ void nd_tile_io(const NDArgs &A, double *tile, int nt, long l0, int n,
                                            bool store)
 {
