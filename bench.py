@@ -161,6 +161,13 @@ def replica_draws(rank):
     return im_draws(NINST, rank)
 
 
+def _cand_name(c):
+    """Autotuner candidate (mode, gam placement, threads) as a JSON key."""
+    mode, gam, threads = c
+    return "%s/%s/%s" % (mode, "shared" if gam == 1 else "workspace",
+                         "auto" if threads == 0 else "%d threads" % threads)
+
+
 def job_value(world, ms_per_step):
     """Whole-job spectra/s: every rank's instances over the slowest rank's
     step time."""
@@ -415,11 +422,13 @@ def run_ours(a, world, rank, local):
                    "global_batch": NINST * world, "pts_l": list(PTS_L), "ns": list(NS),
                    "point_sweeps_per_step": ps, "parallelism": "replicas x%d" % world,
                    "l2": "flushed between iterations (256 MB write); phi outputs 803 MB > L2",
-                   "gam_placement": eng.gam_placement, "launch_mode": eng.launch_mode},
+                   "gam_placement": eng.gam_placement, "launch_mode": eng.launch_mode,
+                   "threads_per_cta": eng.threads or "auto"},
         "autotune": None if tuned is None else {
             "choice": list(tuned["choice"]), "sample_instances": tuned["sample"],
-            "ms": {"%s/%s" % (m, "shared" if g == 1 else "workspace"): v
-                   for (m, g), v in tuned["ms"].items()}},
+            "ms": {_cand_name(c): v for c, v in tuned["ms"].items()},
+            "large_sample_instances": tuned["large_sample"],
+            "ms_large": {_cand_name(c): v for c, v in tuned["ms_large"].items()}},
         "e2e": {"value": e2e_value, "unit": "spectra/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -439,7 +448,9 @@ def run_ours(a, world, rank, local):
         "kernel_ms_per_step": kmean * 1e3,
         "warmup_ms": warm_ms,
         "clocks": clk,
-        "gpu_launches": 5 * a.steps,  # per step: 2 schedule passes, the integration, 2 epilogue
+        # per step: 2 schedule passes, the integration (one launch per grid
+        # with per_grid), 2 epilogue
+        "gpu_launches": (eng.launches_per_integrate() + 2) * a.steps,
         "failed_instances": bad,
         "scores": scores,
         "plain": plain,

@@ -11,21 +11,30 @@ The knobs, each a real alternative the kernels implement:
   that one launch's tail overlaps the next;
 * gam placement — the Thomas recurrence's scratch in shared memory (fewer
   CTAs per SM when the density already fills it) or in a per-CTA slice of
-  the workspace (more CTAs per SM, L2 traffic on the back substitution).
+  the workspace (more CTAs per SM, L2 traffic on the back substitution);
+* threads per CTA — 0 lets the engine choose the fewest warps that hold
+  every line of the launch's largest grid (fuller warps: the FP64 pipe
+  charges a warp instruction whatever its active lanes), so per_grid runs
+  grids of up to 96 points on three warps; 128 forces four warps, the check
+  on that rule.
 
 `tune_batch2d` times every candidate on a sample of the batch — instances
 spread over the batch's cost distribution, so the sample has the batch's mix
-of long and short integrations — with CUDA events, keeps the fastest on the
-engine, and caches the choice per (device, grids, sample size).  Every
-candidate computes bitwise the same densities (tested): only the launch
-differs.
+of long and short integrations — with CUDA events.  A small sample
+overstates the tails of launches that run one after another (per_grid's
+three launches each end on their longest item), so for a batch much larger
+than the sample the best candidate and the best per_grid candidate are timed
+again on a larger slice, which decides.  The choice is kept on the engine
+and cached per (device, grids, batch size class).  Every candidate computes
+bitwise the same densities (tested): only the launch differs.
 """
 import numpy as np
 
 from . import _lib, batch
 
-CANDIDATES = [("persistent", 1), ("persistent", 2), ("one_per_cta", 1), ("one_per_cta", 2),
-              ("per_grid", 1), ("per_grid", 2)]
+CANDIDATES = [("persistent", 1, 0), ("persistent", 2, 0), ("one_per_cta", 1, 0),
+              ("one_per_cta", 2, 0), ("per_grid", 1, 0), ("per_grid", 2, 0),
+              ("per_grid", 2, 128)]
 
 _cache = {}
 
@@ -44,41 +53,67 @@ def _sample(rec, size, settings=None):
     return rec[np.sort(pick)]
 
 
-def tune_batch2d(eng, rec, sample_size=None, repeats=1, candidates=None):
+def _apply(eng, cand):
+    eng.launch_mode, eng.gam_placement, eng.threads = cand
+
+
+def _time(eng, rec, cand, warm=True):
+    """ms of one integration of rec under candidate cand (None: it does not
+    apply, e.g. gam does not fit shared memory)."""
+    torch = eng.torch
+    _apply(eng, cand)
+    try:
+        if warm:
+            eng.integrate(rec[:min(len(rec), 64)])
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        eng.integrate(rec, timer=(e0, e1))
+        torch.cuda.synchronize()
+    except _lib.DgbError as e:
+        if e.status == _lib.DGB_ERR_UNSUPPORTED:
+            return None
+        raise
+    return e0.elapsed_time(e1)
+
+
+def tune_batch2d(eng, rec, sample_size=None, candidates=None, large_size=2048):
     """Time the candidates on a sample of `rec` (dgb_inst2d records) with
     engine `eng` (a batch.Batch2D), set the fastest on the engine and return
-    {"choice": (mode, gam), "ms": {candidate: ms}}."""
+    {"choice": (mode, gam, threads), "ms": {candidate: ms}, "ms_large":
+    {finalist: ms} (empty when the batch is not much larger than the
+    sample), "sample": n, "large_sample": n}."""
     torch = eng.torch
     props = torch.cuda.get_device_properties(torch.cuda.current_device())
     size = sample_size or 4 * props.multi_processor_count
-    key = (props.name, tuple(eng.pts_l), int(size))
+    big = min(large_size, len(rec) // 2) if len(rec) >= 4 * size else 0
+    key = (props.name, tuple(eng.pts_l), int(size), int(big))
     if key in _cache:
-        eng.launch_mode, eng.gam_placement = _cache[key]["choice"]
+        _apply(eng, _cache[key]["choice"])
         return _cache[key]
-    sample = _sample(np.ascontiguousarray(rec), size)
+    saved = (eng.launch_mode, eng.gam_placement, eng.threads)
+    rec = np.ascontiguousarray(rec)
+    sample = _sample(rec, size)
     times = {}
-    saved = (eng.launch_mode, eng.gam_placement)
-    for mode, gam in (candidates or CANDIDATES):
-        eng.launch_mode, eng.gam_placement = mode, gam
-        try:
-            eng.integrate(sample)  # warm-up
-        except _lib.DgbError as e:
-            if e.status == _lib.DGB_ERR_UNSUPPORTED:  # gam does not fit shared memory
-                continue
-            raise
-        best = None
-        for _ in range(repeats):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            eng.integrate(sample, timer=(e0, e1))
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1)
-            best = ms if best is None else min(best, ms)
-        times[(mode, gam)] = best
+    for cand in (candidates or CANDIDATES):
+        ms = _time(eng, sample, cand)
+        if ms is not None:
+            times[cand] = ms
     if not times:
-        eng.launch_mode, eng.gam_placement = saved
+        _apply(eng, saved)
         raise RuntimeError("no launch configuration applies")
     choice = min(times, key=times.get)
-    eng.launch_mode, eng.gam_placement = choice
-    _cache[key] = {"choice": choice, "ms": times, "sample": int(len(sample))}
+    large = {}
+    if big:
+        finalists = {choice}
+        per_grid = [c for c in times if c[0] == "per_grid"]
+        if per_grid:
+            finalists.add(min(per_grid, key=times.get))
+        if len(finalists) > 1:
+            slice_ = _sample(rec, big)
+            for cand in sorted(finalists):
+                large[cand] = _time(eng, slice_, cand, warm=False)
+            choice = min(large, key=large.get)
+    _apply(eng, choice)
+    _cache[key] = {"choice": choice, "ms": times, "ms_large": large,
+                   "sample": int(len(sample)), "large_sample": int(big)}
     return _cache[key]

@@ -92,9 +92,9 @@ def im_seeds(n):
     return sd
 
 
-def settings_from_globals(gam_placement=0):
+def settings_from_globals(gam_placement=0, threads=0):
     tsf, otsf, old, delj = integration.current_settings()
-    return _lib.settings_struct(tsf, otsf, old, delj, gam_placement)
+    return _lib.settings_struct(tsf, otsf, old, delj, gam_placement, threads)
 
 
 #: dgb_item2d (dadi_gb300.h): one (integration, grid) work item.
@@ -130,6 +130,7 @@ class Batch2D:
         self.ns = tuple(ns)
         self.max_steps = int(max_steps)
         self.gam_placement = gam_placement
+        self.threads = 0  # threads per CTA: 0 auto, 96 or 128 (dgb_settings.threads)
         self.launch_mode = "persistent"
         self.adjoint_ctas_per_sm = None  # None: sized to L2 (see adjoint)
         self.xxs = [numerics.default_grid(p) for p in self.pts_l]
@@ -142,12 +143,20 @@ class Batch2D:
         self.mask = np.zeros((ns[0] + 1, ns[1] + 1), dtype=bool)
         self.mask.flat[0] = self.mask.flat[-1] = True
 
+    def launches_per_integrate(self):
+        """Kernel launches of ours in one integrate(): two schedule passes
+        (count, fill) and the integration, one launch per grid size with
+        launch_mode "per_grid"."""
+        per_grid = self.launch_mode == "per_grid" and len(set(self.pts_l)) > 1 \
+            and not integration.current_settings()[2]
+        return 2 + (len(self.pts_l) if per_grid else 1)
+
     def schedule(self, d_rec, n):
         """Device schedules of n dgb_inst2d records already on the device:
         (table, row_off, row_cnt, status)."""
         torch = self.torch
         lib = _lib.lib()
-        st = settings_from_globals(self.gam_placement)
+        st = settings_from_globals(self.gam_placement, self.threads)
         ng = len(self.pts_l)
         nsched = n * ng if st.use_old_timestep else n
         sh = _lib.stream_handle(torch)
@@ -187,7 +196,7 @@ class Batch2D:
             return self.integrate_from(rec, phi0s, one_per_cta=True, timer=timer)
         n = len(rec)
         ng = len(self.pts_l)
-        st = settings_from_globals(self.gam_placement)
+        st = settings_from_globals(self.gam_placement, self.threads)
         rec = np.ascontiguousarray(rec)
         d_rec = _lib.to_device(torch, rec.view(np.uint8), np.uint8)
         table, off, cnt, status = self.schedule(d_rec, n)
@@ -226,7 +235,7 @@ class Batch2D:
         when schedules are per grid (use_old_timestep)."""
         torch = self.torch
         lib = _lib.lib()
-        st = settings_from_globals(self.gam_placement)
+        st = settings_from_globals(self.gam_placement, self.threads)
         if st.use_old_timestep:
             return None
         n = len(rec)
@@ -241,6 +250,8 @@ class Batch2D:
         cur = torch.cuda.current_stream()
         if not hasattr(self, "_side"):
             self._side = [torch.cuda.Stream() for _ in self.pts_l]
+        # workspaces first, so that allocation stays outside the timed launches
+        wss = [_lib.workspace(torch, lib.dgb_workspace_bytes(1, 2, L, n)) for L in self.pts_l]
         fork = torch.cuda.Event()
         if timer is not None:
             timer[0].record()
@@ -255,7 +266,7 @@ class Batch2D:
             side = self._side[g]
             with torch.cuda.stream(side):
                 side.wait_event(fork)
-                ws, nws = _lib.workspace(torch, lib.dgb_workspace_bytes(1, 2, L, n))
+                ws, nws = wss[g]
                 Ls = (ctypes.c_int * 1)(L)
                 _lib.check(lib.dgb_batch2d_integrate(
                     _lib.dptr(d_masks), n, Ls, 1, _lib.dptr(self.d_xx[xo:xo + L]),
@@ -283,7 +294,7 @@ class Batch2D:
         lib = _lib.lib()
         n = len(rec)
         ng = len(self.pts_l)
-        st = settings_from_globals(self.gam_placement)
+        st = settings_from_globals(self.gam_placement, self.threads)
         rec = np.ascontiguousarray(rec)
         d_rec = _lib.to_device(torch, rec.view(np.uint8), np.uint8)
         table, off, cnt, status = self.schedule(d_rec, n)
@@ -356,7 +367,7 @@ class Batch2D:
         rec = np.ascontiguousarray(rec)
         n = len(rec)
         ng = len(self.pts_l)
-        st = settings_from_globals(self.gam_placement)
+        st = settings_from_globals(self.gam_placement, self.threads)
         if st.use_delj_trick:
             raise NotImplementedError("the adjoint does not support the delj trick")
         sh = _lib.stream_handle(torch)

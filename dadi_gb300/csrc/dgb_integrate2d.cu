@@ -445,15 +445,6 @@ static int k2_occupancy(bool delj, size_t smem, int threads = K2_THREADS)
     return nb > 0 ? nb : 1;
 }
 
-// Threads per CTA for a launch whose grids are at most Lmax: 96 (three warps)
-// when that packs more lines per SMSP instruction stream than 128.  A sweep
-// of one line is one lane's chain, and the FP64 pipe charges a warp
-// instruction whatever its active lanes, so an SM's time per step is set by
-// the most warps any SMSP holds: with occ CTAs of w warps per SM, lines per
-// SMSP-stream = occ * Lmax / ceil(occ * w / 4).  At Lmax = 80 (four CTAs per
-// SM): 96 threads 106.7, 128 threads 80.  occ returns the chosen CTAs per SM.
-static int k2_threads(bool delj, size_t smem, int Lmax, int &occ);
-
 static int k2_num_sms()
 {
     int dev = 0, nsm = 0;
@@ -462,20 +453,28 @@ static int k2_num_sms()
     return nsm > 0 ? nsm : 1;
 }
 
-static int k2_threads(bool delj, size_t smem, int Lmax, int &occ)
+// Threads per CTA of a batched launch whose grids are at most Lmax points:
+// the fewest warps (two to four) that give every line of the largest grid
+// its own lane.  A sweep of one line is one lane's dependency chain and the
+// FP64 pipe charges a warp instruction whatever its active lanes, so lines
+// packed into fewer warps cost fewer pipe cycles per step.  Measured on the
+// 4096-instance IM batch at pts 80/90/100, one launch per grid: three warps
+// at L = 80 and 90 (27 and 30 of 32 lanes busy, instead of 20 and 23 with
+// four) 11.72 s, four warps for every grid 13.39 s, bitwise the same
+// densities.  settings->threads = 64, 96 or 128 asks for that size where it
+// holds the lines (else the automatic choice applies); 0 is automatic.
+// occ gets the CTAs per SM.  Returns 0 for an unsupported setting.
+static int k2_pick_threads(const dgb_settings *settings, bool delj, size_t smem, int Lmax,
+                           int &occ)
 {
-    int best_t = K2_THREADS;
-    occ = k2_occupancy(delj, smem + sizeof(K2Shared), K2_THREADS);
-    if (Lmax > 96)
-        return best_t;
-    double best = (double)occ * Lmax / ((occ * 4 + 3) / 4);
-    int o3 = k2_occupancy(delj, smem + sizeof(K2Shared), 96);
-    double t3 = (double)o3 * Lmax / ((o3 * 3 + 3) / 4);
-    if (t3 > best) {
-        best_t = 96;
-        occ = o3;
-    }
-    return best_t;
+    const int want = settings->threads;
+    if (want != 0 && want != 64 && want != 96 && want != 128)
+        return 0;
+    int warps = std::min(4, std::max(2, (Lmax + 31) / 32));
+    if (want != 0 && Lmax <= want)
+        warps = want / 32;
+    occ = k2_occupancy(delj, smem + sizeof(K2Shared), 32 * warps);
+    return 32 * warps;
 }
 
 int k2_integrate_table(double *phi, int L, const double *xx, const double *table, int nsteps,
@@ -582,18 +581,21 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     }
     int nblocks;
     size_t smem;
-    int threads = K2_THREADS;
+    int threads;
     if (use_s) {
         A.gam_smem = 1;
-        nblocks = nsm * occ_s;
         smem = bytes_s;
+        threads = k2_pick_threads(settings, A.use_delj, smem, A.Lmax, occ_s);
+        nblocks = nsm * occ_s;
     } else {
         A.gam_smem = 0;
         A.gam_glob = (double *)((char *)ws + 256);
         smem = bytes_g;
-        threads = k2_threads(A.use_delj, smem, A.Lmax, occ_g);
+        threads = k2_pick_threads(settings, A.use_delj, smem, A.Lmax, occ_g);
         nblocks = (int)std::min<size_t>((ws_bytes - 256) / slice, (size_t)nsm * occ_g);
     }
+    if (threads == 0)
+        return DGB_ERR_ARG;
     if (nblocks < 1)
         return DGB_ERR_WORKSPACE;
     nblocks = std::min(nblocks, A.nwork);
@@ -768,38 +770,38 @@ extern "C" int dgb_items2d_integrate(const dgb_item2d *items, int nitems, int Lm
         fit_s = false; // as in k2_batch: shared memory only if it costs no CTAs per SM
     int nsm = k2_num_sms();
     int nblocks;
-    size_t smem;
+    size_t smem = fit_s ? bytes_s : bytes_g;
     size_t slice = (size_t)Lmax * Lmax * sizeof(double);
+    int occ = 1;
+    const int threads = k2_pick_threads(settings, A.use_delj, smem, Lmax, occ);
+    if (threads == 0)
+        return DGB_ERR_ARG;
     if (one_per_cta) {
         // CTA b integrates item order[b] (or b) and retires: no queue
         A.counter = nullptr;
         nblocks = nitems;
         A.gam_smem = fit_s ? 1 : 0;
-        smem = fit_s ? bytes_s : bytes_g;
         if (!fit_s) {
             if ((ws_bytes - 256) / slice < (size_t)nitems)
                 return DGB_ERR_WORKSPACE;
             A.gam_glob = (double *)((char *)ws + 256);
         }
-        return k2_launch(A, nblocks, smem, (cudaStream_t)stream);
+        return k2_launch(A, nblocks, smem, (cudaStream_t)stream, threads);
     }
     if (fit_s) {
         A.gam_smem = 1;
-        nblocks = nsm * k2_occupancy(A.use_delj, bytes_s + sizeof(K2Shared));
-        smem = bytes_s;
+        nblocks = nsm * occ;
     } else {
         A.gam_smem = 0;
-        nblocks = (int)std::min<size_t>((ws_bytes - 256) / slice,
-                                        (size_t)nsm * k2_occupancy(A.use_delj, bytes_g + 256));
+        nblocks = (int)std::min<size_t>((ws_bytes - 256) / slice, (size_t)nsm * occ);
         A.gam_glob = (double *)((char *)ws + 256);
-        smem = bytes_g;
     }
     if (nblocks < 1)
         return DGB_ERR_WORKSPACE;
     nblocks = std::min(nblocks, nitems);
     if (cudaMemsetAsync(A.counter, 0, sizeof(int), (cudaStream_t)stream) != cudaSuccess)
         return DGB_ERR_CUDA;
-    return k2_launch(A, nblocks, smem, (cudaStream_t)stream);
+    return k2_launch(A, nblocks, smem, (cudaStream_t)stream, threads);
 }
 
 extern "C" int dgb_sched2d_host(const dgb_inst2d *insts, int ninst,

@@ -71,7 +71,10 @@ typedef struct {
     int use_old_timestep;        /* default 0 */
     int use_delj_trick;          /* default 0 */
     int gam_placement;           /* batched engine: 0 auto, 1 shared memory, 2 workspace */
-    int pad_;
+    int threads;                 /* batched engine: threads per CTA, 0 auto (the fewest
+                                    warps, 2-4, that give every line of the largest grid a
+                                    lane), or 64 / 96 / 128 where that many threads hold
+                                    every line (else auto) */
 } dgb_settings;
 
 int dgb_abi_version(void);
