@@ -59,6 +59,6 @@ def test_threads_setting_is_checked(cuda_lib):
         eng.threads = t
         out = [p.cpu().numpy() for p in eng.integrate(rec)[0]]
         assert all(np.array_equal(a, b) for a, b in zip(out, ref))
-    eng.threads = 64
+    eng.threads = 80
     with pytest.raises(_lib.DgbError):
         eng.integrate(rec)
