@@ -46,7 +46,11 @@ NINST = 4096
 BYTES_PER_PS = 16      # algorithmic HBM bytes per point-sweep (phi read + write)
 FLOPS_PER_PS = 30      # algorithmic FP64 flops per point-sweep (reference formulation)
 FP64_INSTR_PER_PS = 10  # FP64 pipe instructions per point-sweep in k_integrate2d
-K2_TRAFFIC_BYTES = 2.89e9 + 0.886e9  # ncu dram__bytes_read.sum + dram__bytes_write.sum
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of the integration of one
+# full step of this workload, by launch mode: one mixed launch, or the three
+# launches of per_grid (1.09 + 0.329, 1.04 + 0.244, 1.03 + 0.191 GB)
+K2_TRAFFIC_BYTES = {"persistent": 2.89e9 + 0.886e9,
+                    "per_grid": (1.09 + 1.04 + 1.03) * 1e9 + (328.68 + 243.90 + 190.98) * 1e6}
 
 
 def im_draws(n, seed):
@@ -404,10 +408,10 @@ def run_ours(a, world, rank, local):
     peak, src = load_peaks()
     kmean = float(np.mean(kern_ms)) / 1e3
     achieved = ps * BYTES_PER_PS / kmean / 1e9
-    # DRAM bytes (read + write) of one k_integrate2d launch on this workload,
-    # from one ncu capture of the timed launch (1-pass metrics)
-    traffic = K2_TRAFFIC_BYTES if (NINST, PTS_L, NS) == (4096, (80, 90, 100), (40, 40)) \
-        else None
+    # DRAM bytes (read + write) of the integration of one step on this
+    # workload, from one ncu capture of the timed launches (1-pass metrics)
+    traffic = K2_TRAFFIC_BYTES.get(eng.launch_mode) \
+        if (NINST, PTS_L, NS) == (4096, (80, 90, 100), (40, 40)) else None
     fp64_achieved = ps * FLOPS_PER_PS / kmean / 1e12
     fp64_instr = ps * FP64_INSTR_PER_PS * 2 / kmean / 1e12
     fp64_peak = fp64_peak_measured
@@ -571,13 +575,15 @@ def run_profile_case(a):
     steps = batch.count_steps(rec)
     sel = np.where((steps >= 200) & (steps <= 800))[0][:a.profile_items]
     eng = batch.Batch2D(PTS_L, NS, gam_placement=a.gam)
+    eng.launch_mode = a.launch or "persistent"
     for _ in range(2):
         t = time.perf_counter()
         phis, st = eng.integrate(rec[sel])
         torch.cuda.synchronize()
         dt = time.perf_counter() - t
     ps = point_sweeps(steps[sel], PTS_L)
-    print(json.dumps({"mode": "profile", "instances": int(len(sel)), "point_sweeps": ps,
+    print(json.dumps({"mode": "profile", "launch_mode": eng.launch_mode,
+                      "instances": int(len(sel)), "point_sweeps": ps,
                       "seconds": dt, "status_nonzero": int((st != 0).sum())}))
     return 0
 
