@@ -279,8 +279,14 @@ def test_dadi_settings(cuda_lib, golden, name, kw):
         assert _rel(p3, g["set_%s_3d" % name]) < tol
         ref = g["set_%s_im" % name]
         fs = numerics.make_extrap_func(models.IM)(d["params"], d["ns"], d["pts_l"])
-        fsb, _, st = batch.Batch2D(d["pts_l"], d["ns"]).run(np.array([d["params"]]))
+        eng = batch.Batch2D(d["pts_l"], d["ns"])
+        fsb, _, st = eng.run(np.array([d["params"]]))
         assert int(st.abs().sum()) == 0
+        # one launch per grid size (CTA size per grid) gives the same bits
+        eng.launch_mode = "per_grid"
+        fsp, _, stp = eng.run(np.array([d["params"]]))
+        assert int(stp.abs().sum()) == 0
+        assert np.array_equal(fsp.cpu().numpy(), fsb.cpu().numpy())
         for f in (np.asarray(fs.data), fsb.cpu().numpy()[0]):
             if name == "delj":
                 rel, _, _ = fs_parity(f, ref)
