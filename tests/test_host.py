@@ -192,3 +192,53 @@ def test_dfe_pdf_and_integrate_match_reference(golden):
     fs = c.integrate(d["sel_params"], None, dfe.biv_lognormal, d["theta"], None,
                      exterior_int=False)
     assert np.allclose(np.asarray(fs.data), g["dfe_fs_interior"], rtol=1e-12, atol=0)
+
+
+def _phi1d_direct(xx, gamma, h, prec=None):
+    """The stationary density with selection and dominance evaluated straight
+    from its integral form, phi(x) = e^{S(x)} int_x^1 e^{-S} / int_0^1 e^{-S}
+    / (x (1 - x)) with S(x) = 4 gamma h x + 2 gamma (1 - 2h) x^2 (end points
+    as phi_1D sets them), by scipy quadrature or, with prec, by mpmath at
+    that many digits.  The check the reference's test_phi1D.py makes."""
+    S = lambda x: 4 * gamma * h * x + 2 * gamma * (1 - 2 * h) * x * x
+    if prec:
+        import mpmath
+        mpmath.mp.dps = prec
+        f = lambda x: mpmath.exp(-S(x))
+        int0 = mpmath.quad(f, [0, 1])
+        ints = [mpmath.quad(f, [q, 1]) for q in xx]
+        phi = np.array([float(mpmath.exp(S(q)) * v / int0) for q, v in zip(xx, ints)])
+        int0 = float(int0)
+    else:
+        import warnings
+        import scipy.integrate
+        f = lambda x: np.exp(-S(x))
+        with np.errstate(all="ignore"), warnings.catch_warnings():
+            warnings.simplefilter("ignore")  # the overflow this form is known for
+            int0 = scipy.integrate.quad(f, 0, 1)[0]
+            ints = np.array([scipy.integrate.quad(f, q, 1)[0] for q in xx])
+            phi = np.exp(S(xx)) * ints / int0
+    phi[1:-1] /= xx[1:-1] * (1 - xx[1:-1])
+    phi[0] = phi[1]
+    phi[-1] = 1. / int0
+    return phi
+
+
+def test_phi_1D_dominance_matches_integral_form():
+    """phi_1D with dominance (dadi/PhiManip.py:12-108) against the integral
+    form: close to direct quadrature where that converges (gamma = 50),
+    finite where direct quadrature overflows (gamma = 500), and within
+    5e-3 of arbitrary-precision quadrature for strongly negative gammas
+    (the reference's tests/test_phi1D.py cases)."""
+    xx = numerics.default_grid(20)
+    for gamma, h in ([50, 0.14], [50, 0.84]):
+        assert np.allclose(phimanip.phi_1D(xx, gamma=gamma, h=h), _phi1d_direct(xx, gamma, h))
+    for gamma, h in ([500, 0.14], [500, 0.84]):
+        assert np.any(np.isnan(_phi1d_direct(xx, gamma, h)))
+        assert not np.any(np.isnan(phimanip.phi_1D(xx, gamma=gamma, h=h)))
+    pytest.importorskip("mpmath")
+    for gamma, h in [(-500, 0.14), (-500, 0.94), (-2000, 0.34), (-1429, 0.51), (-1e4, 0),
+                     (-1e5, 0), (-1e6, 0)]:
+        ours = phimanip.phi_1D(xx, gamma=gamma, h=h)
+        ref = _phi1d_direct(xx, gamma, h, prec=5)
+        assert np.max(2 * np.abs(ours - ref) / (ours + ref + 1e-12)) < 5e-3, (gamma, h)
