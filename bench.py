@@ -439,6 +439,9 @@ def run_ours(a, world, rank, local):
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": src,
                      "kernel": "k_integrate2d",
+                     "launches_per_step": eng.launches_per_integrate() - 2,
+                     "per": "step: achieved and traffic cover every integration launch of "
+                            "one step (one per grid size with per_grid)",
                      "note": "FP64-pipe bound: phi stays in shared memory, so HBM carries "
                              "little; see fp64"},
         "fp64": {"algorithmic_tflops": fp64_achieved,
