@@ -299,6 +299,219 @@ __global__ void __launch_bounds__(K2_THREADS) k_integrate2d(K2Args A)
     }
 }
 
+// ------------------------------------------------ two items per CTA
+
+// k_integrate2d for a launch over one grid of L points with two work items
+// per CTA, stepped together: the 2L lines of a sweep (L of each item) are
+// spread over ceil(2L/32) warps, so a grid whose L lines would leave a
+// fourth warp mostly empty (L = 100: 25 of 32 lanes busy on four warps)
+// fills its warps better (200 lines on seven warps: 29 of 32).  Each item
+// keeps its own density, schedule, masks and coefficient vectors; the grid
+// constants are shared.  The two items are neighbours in the longest-first
+// order, so their step counts are close; the shorter one's lanes idle for
+// the difference.  Per line the arithmetic is k_integrate2d's, so the
+// results are bitwise the same.  Thomas scratch: a 2L x L slice of the
+// workspace per CTA (element p of line q at gam[p*2L + q]).
+constexpr int K2P_MAXTHREADS = 256;
+
+struct K2PairShared {
+    AxisScalars ax[2][2]; // [item slot][axis]
+    double inj[2];
+    int item[2];
+};
+
+__host__ __device__ inline size_t k2_pair_doubles(int L, bool delj)
+{
+    return 2 * (size_t)L * odd_pitch(L) + 6 * (size_t)L + 4 * (size_t)(delj ? 10 : 5) * L;
+}
+
+// Coefficient vectors of (slot, axis) index sa = 2*slot + axis.
+__device__ __forceinline__ AxisVecs k2p_vecs(double *vbase, int sa, int L, bool delj)
+{
+    const int nv = delj ? 10 : 5;
+    double *p = vbase + (size_t)sa * nv * L;
+    AxisVecs v;
+    v.A1 = p;
+    v.A0 = p + L;
+    v.C1 = p + 2 * L;
+    v.C0 = p + 3 * L;
+    v.B0 = p + 4 * L;
+    v.G = v.Pv = v.Qv = v.VI = v.DF = nullptr;
+    if (delj) {
+        v.G = p + 5 * L;
+        v.Pv = p + 6 * L;
+        v.Qv = p + 7 * L;
+        v.VI = p + 8 * L;
+        v.DF = p + 9 * L;
+    }
+    return v;
+}
+
+template <bool DELJ>
+__global__ void __launch_bounds__(K2P_MAXTHREADS, 1) k_integrate2d_pair(K2Args A)
+{
+    extern __shared__ __align__(16) double smem[];
+    __shared__ K2PairShared S;
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int nwarps = blockDim.x >> 5;
+    const int L = A.L[0];
+    const int pitch = odd_pitch(L);
+    const size_t psz = (size_t)L * pitch;
+    double *phi0 = smem; // slot s at phi0 + s * psz
+    GridVecs g;
+    double *p = smem + 2 * psz;
+    g.x = p; p += L;
+    g.xv = p; p += L;
+    g.dfac = p; p += L;
+    g.xInt = p; p += L;
+    g.ih = p; p += L;
+    g.dx = p; p += L;
+    double *vbase = p; // 4 x (5 or 10) x L doubles
+    double *gam = A.gam_glob + (size_t)blockIdx.x * 2 * L * L;
+    const double *xx = A.xx_all + A.xx_off[0];
+
+    // grid constants, once for every item of the launch
+    for (int i = tid; i < L; i += blockDim.x) {
+        double x = xx[i];
+        g.x[i] = x;
+        g.xv[i] = x * (1. - x);
+        if (i < L - 1) {
+            double d = xx[i + 1] - x;
+            g.dx[i] = d;
+            g.ih[i] = 1.0 / (2 * d);
+            g.xInt[i] = 0.5 * (xx[i + 1] + x);
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < L; i += blockDim.x) {
+        if (i == 0)
+            g.dfac[i] = 2. / g.dx[0];
+        else if (i == L - 1)
+            g.dfac[i] = 2. / g.dx[L - 2];
+        else
+            g.dfac[i] = 2. / (g.dx[i] + g.dx[i - 1]);
+    }
+    __syncthreads();
+    const int j0 = (g.x[0] == 0.0) ? 0 : -1;
+    const int j1 = (g.x[L - 1] == 1.0) ? L - 1 : -1;
+
+    // S.item is written by thread 0 and read by all between the barrier that
+    // follows the write and the next barrier thread 0 must pass to write again.
+    for (int iter = 0;; iter++) {
+        if (tid == 0) {
+            const int base =
+                A.counter ? atomicAdd(A.counter, 2) : (iter == 0 ? 2 * (int)blockIdx.x : A.nwork);
+            S.item[0] = base;
+            S.item[1] = base + 1;
+        }
+        __syncthreads();
+        if (S.item[0] >= A.nwork)
+            break;
+        const int ns = (S.item[1] < A.nwork) ? 2 : 1; // item slots in use
+        int nst0 = 0, nst1 = 0, fr0 = 0, fr1 = 0, nm0 = 0, nm1 = 0;
+        const double *rows0 = nullptr, *rows1 = nullptr;
+        double *out0 = nullptr, *out1 = nullptr;
+        for (int s = 0; s < ns; s++) {
+            const int wid = A.order ? A.order[S.item[s]] : S.item[s];
+            double *out = A.phi_out + A.out_off[0] + (size_t)wid * L * L;
+            const double *src = A.phi0_all ? A.phi0_all + A.phi0_off[0] : out;
+            const int fr = A.masks ? (A.masks[wid] & 0xff) : A.frozen_mask;
+            const int nm = A.masks ? (A.masks[wid] >> 8 & 0xff) : A.nomut_mask;
+            const double *rows = A.row_off ? A.table + A.row_off[wid] * K2_ROW : A.table;
+            const int nst = A.row_off ? A.row_cnt[wid] : A.fixed_cnt;
+            if (s == 0) {
+                out0 = out; fr0 = fr; nm0 = nm; rows0 = rows; nst0 = nst;
+            } else {
+                out1 = out; fr1 = fr; nm1 = nm; rows1 = rows; nst1 = nst;
+            }
+            double *ph = phi0 + s * psz;
+            for (int idx = tid; idx < L * L; idx += blockDim.x) {
+                int r = idx / L, c = idx - r * L;
+                ph[r * pitch + c] = src[idx];
+            }
+        }
+        __syncthreads();
+        const int nmax = max(nst0, nst1);
+        const int nl = ns * L; // lines of one sweep over the slots in use
+        const int lpw = (nl + nwarps - 1) / nwarps;
+
+        for (int step = 0; step < nmax; step++) {
+            const bool act0 = step < nst0, act1 = step < nst1;
+            // ---- step scalars: lane 2s+a of warp 0 for (slot s, axis a),
+            // lane 4+s the injection of slot s
+            if (warp == 0 && lane < 6) {
+                const int s = (lane < 4) ? (lane >> 1) : lane - 4;
+                if (s ? act1 : act0) {
+                    const double *row = (s ? rows1 : rows0) + (size_t)step * K2_ROW;
+                    if (lane < 4)
+                        k2_axis_scalars(S.ax[s][lane & 1], lane & 1, row, g, L);
+                    else
+                        S.inj[s] = inject_value(2, row[0], row[1], g.x[0], g.x[1], g.x[2]);
+                }
+            }
+            __syncthreads();
+            // ---- per-axis vectors of both slots and mutation injection
+            for (int t = tid; t < ns * 2 * L; t += blockDim.x) {
+                const int sa = t / L, i = t - sa * L; // sa = 2*slot + axis
+                if ((sa >> 1) ? act1 : act0) {
+                    AxisVecs v = k2p_vecs(vbase, sa, L, DELJ);
+                    build_axis_entry(i, L, g, S.ax[sa >> 1][sa & 1], 1.0, DELJ, v);
+                }
+            }
+            if (tid == 0) {
+                for (int s = 0; s < ns; s++) {
+                    if (!(s ? act1 : act0))
+                        continue;
+                    const int fr = s ? fr1 : fr0, nm = s ? nm1 : nm0;
+                    double *ph = phi0 + s * psz;
+                    if (!(fr & 1) && !(nm & 1))
+                        ph[1 * pitch + 0] += S.inj[s];
+                    if (!(fr & 2) && !(nm & 2))
+                        ph[0 * pitch + 1] += S.inj[s];
+                }
+            }
+            __syncthreads();
+            // ---- x sweep (axis 0) then y sweep (axis 1) over both slots' lines
+            for (int a = 0; a < 2; a++) {
+                const int sp = (a == 0) ? pitch : 1;
+                const int sl = (a == 0) ? 1 : pitch;
+                for (int k = lane; k < lpw; k += 32) {
+                    const int q = warp * lpw + k;
+                    if (q >= nl)
+                        break;
+                    const int s = (q >= L) ? 1 : 0;
+                    const int line = q - s * L;
+                    if (!(s ? act1 : act0) || ((s ? fr1 : fr0) & (1 << a)))
+                        continue;
+                    const AxisScalars &sc = S.ax[s][a];
+                    const AxisVecs v = k2p_vecs(vbase, 2 * s + a, L, DELJ);
+                    const double W = sc.mig[1 - a] * g.x[line];
+                    const double bs = (line == j0) ? sc.bcs : 0.0;
+                    const double be = (line == j1) ? sc.bce : 0.0;
+                    double *ph = phi0 + s * psz + (size_t)line * sl;
+                    double *gm = gam + q;
+                    if (DELJ)
+                        solve_line_delj(ph, sp, gm, 2 * L, L, &sc.mig[1 - a], &g.x[line], 1, bs,
+                                        be, g, v);
+                    else
+                        solve_line(ph, sp, gm, 2 * L, L, W, bs, be, v, sc);
+                }
+                __syncthreads();
+            }
+        }
+        for (int s = 0; s < ns; s++) {
+            const double *ph = phi0 + s * psz;
+            double *out = s ? out1 : out0;
+            for (int idx = tid; idx < L * L; idx += blockDim.x) {
+                int r = idx / L, c = idx - r * L;
+                out[idx] = ph[r * pitch + c];
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------- schedule pass
 
 // Walk the reference time loop of two_pops (dadi/Integration.py:346-386) for
@@ -443,6 +656,39 @@ static int k2_occupancy(bool delj, size_t smem, int threads = K2_THREADS)
         return 1;
     }
     return nb > 0 ? nb : 1;
+}
+
+// Resident two-item CTAs per SM (k_integrate2d_pair), as k2_occupancy.
+static int k2_pair_occupancy(bool delj, size_t smem, int threads)
+{
+    int nb = 0;
+    cudaError_t e;
+    if (delj) {
+        raise_smem_limit(k_integrate2d_pair<true>);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate2d_pair<true>, threads,
+                                                          smem);
+    } else {
+        raise_smem_limit(k_integrate2d_pair<false>);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate2d_pair<false>,
+                                                          threads, smem);
+    }
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return nb;
+}
+
+// Threads of a two-item CTA for grids of L points when pairing pays: one
+// grid of 97-128 points (a single item needs four warps there) whose 2L
+// lines fill their warps at least 5 % better than L lines fill four; else 0.
+static int k2_pair_threads(int L)
+{
+    if (L <= 96 || L > K2P_MAXTHREADS / 2)
+        return 0;
+    const int w1 = (L + 31) / 32, w2 = (2 * L + 31) / 32;
+    const double f1 = (double)L / (32 * w1), f2 = (double)(2 * L) / (32 * w2);
+    return (f2 >= f1 + 0.05) ? 32 * w2 : 0;
 }
 
 static int k2_num_sms()
@@ -596,6 +842,35 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     }
     if (threads == 0)
         return DGB_ERR_ARG;
+    // two work items per CTA where that fills the warps better (one grid,
+    // automatic thread count, no checkpoints, scratch in the workspace)
+    const int pthreads = (ngrids == 1 && !ckpt && !use_s && settings->threads == 0)
+                             ? k2_pair_threads(Lmax)
+                             : 0;
+    if (pthreads) {
+        const size_t pbytes = k2_pair_doubles(Lmax, A.use_delj) * sizeof(double);
+        int dev = 0, optin = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+                cudaSuccess)
+            return DGB_ERR_CUDA;
+        const int pocc = (pbytes + sizeof(K2PairShared) + 1024 <= (size_t)optin)
+                             ? k2_pair_occupancy(A.use_delj, pbytes, pthreads)
+                             : 0;
+        long pblocks = std::min<long>((long)((ws_bytes - 256) / (2 * slice)), (long)nsm * pocc);
+        pblocks = std::min<long>(pblocks, (A.nwork + 1) / 2);
+        if (pblocks >= 1) {
+            A.gam_smem = 0;
+            A.gam_glob = (double *)((char *)ws + 256);
+            if (cudaMemsetAsync(A.counter, 0, sizeof(int), st) != cudaSuccess)
+                return DGB_ERR_CUDA;
+            if (A.use_delj)
+                k_integrate2d_pair<true><<<(unsigned)pblocks, pthreads, pbytes, st>>>(A);
+            else
+                k_integrate2d_pair<false><<<(unsigned)pblocks, pthreads, pbytes, st>>>(A);
+            return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
+        }
+    }
     if (nblocks < 1)
         return DGB_ERR_WORKSPACE;
     nblocks = std::min(nblocks, A.nwork);

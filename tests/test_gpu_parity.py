@@ -325,3 +325,29 @@ def test_coefficient_records_match_inline_setup(cuda_lib, P, L, delj, frozen):
         outs.append(d_phi.cpu().numpy())
     assert np.all(np.isfinite(outs[0]))
     assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("pts_l,delj", [((100,), False), ((100, 110), False), ((100,), True)])
+def test_two_items_per_cta_bitwise(cuda_lib, pts_l, delj):
+    """A launch over one grid of 97-128 points runs two work items per CTA
+    when the thread count is automatic; its densities are bitwise those of
+    one item per CTA (threads forced to 128), with an odd number of
+    instances (the last CTA holds one item) and with the delj trick."""
+    from dadi_gb300 import batch, integration as gi
+    saved = gi.use_delj_trick
+    try:
+        gi.use_delj_trick = bool(delj)
+        eng = batch.Batch2D(pts_l, (10, 10))
+        rec = batch.im_instances(cases.im_draws(5))  # 133-2744 steps
+        for mode in ("persistent", "per_grid"):
+            eng.launch_mode = mode
+            out = []
+            for threads in (0, 128):
+                eng.threads = threads
+                phis, st = eng.integrate(rec)
+                assert int(st.abs().sum()) == 0
+                out.append([p.cpu().numpy() for p in phis])
+            assert all(np.array_equal(a, b) for a, b in zip(out[0], out[1])), mode
+            assert all(np.all(np.isfinite(a)) for a in out[0])
+    finally:
+        gi.use_delj_trick = saved
