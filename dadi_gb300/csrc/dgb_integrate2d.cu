@@ -309,8 +309,8 @@ __global__ void __launch_bounds__(K2_THREADS) k_integrate2d(K2Args A)
 // keeps its own density, schedule, masks and coefficient vectors; the grid
 // constants are shared.  The two items are neighbours in the longest-first
 // order, so their step counts are close; the shorter one's lanes idle for
-// the difference.  Per line the arithmetic is k_integrate2d's, so the
-// results are bitwise the same.  Thomas scratch: a 2L x L slice of the
+// the difference.  Per line the arithmetic is k_integrate2d's (default
+// delta_j only), so the results are bitwise the same.  Thomas scratch: a 2L x L slice of the
 // workspace per CTA (element p of line q at gam[p*2L + q]).
 constexpr int K2P_MAXTHREADS = 256;
 
@@ -320,16 +320,15 @@ struct K2PairShared {
     int item[2];
 };
 
-__host__ __device__ inline size_t k2_pair_doubles(int L, bool delj)
+__host__ __device__ inline size_t k2_pair_doubles(int L)
 {
-    return 2 * (size_t)L * odd_pitch(L) + 6 * (size_t)L + 4 * (size_t)(delj ? 10 : 5) * L;
+    return 2 * (size_t)L * odd_pitch(L) + 6 * (size_t)L + 4 * 5 * (size_t)L;
 }
 
 // Coefficient vectors of (slot, axis) index sa = 2*slot + axis.
-__device__ __forceinline__ AxisVecs k2p_vecs(double *vbase, int sa, int L, bool delj)
+__device__ __forceinline__ AxisVecs k2p_vecs(double *vbase, int sa, int L)
 {
-    const int nv = delj ? 10 : 5;
-    double *p = vbase + (size_t)sa * nv * L;
+    double *p = vbase + (size_t)sa * 5 * L;
     AxisVecs v;
     v.A1 = p;
     v.A0 = p + L;
@@ -337,17 +336,9 @@ __device__ __forceinline__ AxisVecs k2p_vecs(double *vbase, int sa, int L, bool 
     v.C0 = p + 3 * L;
     v.B0 = p + 4 * L;
     v.G = v.Pv = v.Qv = v.VI = v.DF = nullptr;
-    if (delj) {
-        v.G = p + 5 * L;
-        v.Pv = p + 6 * L;
-        v.Qv = p + 7 * L;
-        v.VI = p + 8 * L;
-        v.DF = p + 9 * L;
-    }
     return v;
 }
 
-template <bool DELJ>
 __global__ void __launch_bounds__(K2P_MAXTHREADS, 1) k_integrate2d_pair(K2Args A)
 {
     extern __shared__ __align__(16) double smem[];
@@ -367,7 +358,7 @@ __global__ void __launch_bounds__(K2P_MAXTHREADS, 1) k_integrate2d_pair(K2Args A
     g.xInt = p; p += L;
     g.ih = p; p += L;
     g.dx = p; p += L;
-    double *vbase = p; // 4 x (5 or 10) x L doubles
+    double *vbase = p; // 4 x 5 x L doubles
     double *gam = A.gam_glob + (size_t)blockIdx.x * 2 * L * L;
     const double *xx = A.xx_all + A.xx_off[0];
 
@@ -455,8 +446,8 @@ __global__ void __launch_bounds__(K2P_MAXTHREADS, 1) k_integrate2d_pair(K2Args A
             for (int t = tid; t < ns * 2 * L; t += blockDim.x) {
                 const int sa = t / L, i = t - sa * L; // sa = 2*slot + axis
                 if ((sa >> 1) ? act1 : act0) {
-                    AxisVecs v = k2p_vecs(vbase, sa, L, DELJ);
-                    build_axis_entry(i, L, g, S.ax[sa >> 1][sa & 1], 1.0, DELJ, v);
+                    AxisVecs v = k2p_vecs(vbase, sa, L);
+                    build_axis_entry(i, L, g, S.ax[sa >> 1][sa & 1], 1.0, false, v);
                 }
             }
             if (tid == 0) {
@@ -485,17 +476,12 @@ __global__ void __launch_bounds__(K2P_MAXTHREADS, 1) k_integrate2d_pair(K2Args A
                     if (!(s ? act1 : act0) || ((s ? fr1 : fr0) & (1 << a)))
                         continue;
                     const AxisScalars &sc = S.ax[s][a];
-                    const AxisVecs v = k2p_vecs(vbase, 2 * s + a, L, DELJ);
+                    const AxisVecs v = k2p_vecs(vbase, 2 * s + a, L);
                     const double W = sc.mig[1 - a] * g.x[line];
                     const double bs = (line == j0) ? sc.bcs : 0.0;
                     const double be = (line == j1) ? sc.bce : 0.0;
                     double *ph = phi0 + s * psz + (size_t)line * sl;
-                    double *gm = gam + q;
-                    if (DELJ)
-                        solve_line_delj(ph, sp, gm, 2 * L, L, &sc.mig[1 - a], &g.x[line], 1, bs,
-                                        be, g, v);
-                    else
-                        solve_line(ph, sp, gm, 2 * L, L, W, bs, be, v, sc);
+                    solve_line(ph, sp, gam + q, 2 * L, L, W, bs, be, v, sc);
                 }
                 __syncthreads();
             }
@@ -659,19 +645,12 @@ static int k2_occupancy(bool delj, size_t smem, int threads = K2_THREADS)
 }
 
 // Resident two-item CTAs per SM (k_integrate2d_pair), as k2_occupancy.
-static int k2_pair_occupancy(bool delj, size_t smem, int threads)
+static int k2_pair_occupancy(size_t smem, int threads)
 {
     int nb = 0;
-    cudaError_t e;
-    if (delj) {
-        raise_smem_limit(k_integrate2d_pair<true>);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate2d_pair<true>, threads,
-                                                          smem);
-    } else {
-        raise_smem_limit(k_integrate2d_pair<false>);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate2d_pair<false>,
-                                                          threads, smem);
-    }
+    raise_smem_limit(k_integrate2d_pair);
+    cudaError_t e =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate2d_pair, threads, smem);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return 0;
@@ -843,19 +822,23 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     if (threads == 0)
         return DGB_ERR_ARG;
     // two work items per CTA where that fills the warps better (one grid,
-    // automatic thread count, no checkpoints, scratch in the workspace)
-    const int pthreads = (ngrids == 1 && !ckpt && !use_s && settings->threads == 0)
-                             ? k2_pair_threads(Lmax)
-                             : 0;
+    // automatic thread count, no checkpoints, scratch in the workspace, the
+    // default delta_j: the delj trick's per-interval arithmetic leaves the
+    // compiler choices of contraction that differ between the two kernels,
+    // so it keeps one item per CTA and its bits)
+    const int pthreads =
+        (ngrids == 1 && !ckpt && !use_s && settings->threads == 0 && !A.use_delj)
+            ? k2_pair_threads(Lmax)
+            : 0;
     if (pthreads) {
-        const size_t pbytes = k2_pair_doubles(Lmax, A.use_delj) * sizeof(double);
+        const size_t pbytes = k2_pair_doubles(Lmax) * sizeof(double);
         int dev = 0, optin = 0;
         if (cudaGetDevice(&dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
                 cudaSuccess)
             return DGB_ERR_CUDA;
         const int pocc = (pbytes + sizeof(K2PairShared) + 1024 <= (size_t)optin)
-                             ? k2_pair_occupancy(A.use_delj, pbytes, pthreads)
+                             ? k2_pair_occupancy(pbytes, pthreads)
                              : 0;
         long pblocks = std::min<long>((long)((ws_bytes - 256) / (2 * slice)), (long)nsm * pocc);
         pblocks = std::min<long>(pblocks, (A.nwork + 1) / 2);
@@ -864,10 +847,7 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
             A.gam_glob = (double *)((char *)ws + 256);
             if (cudaMemsetAsync(A.counter, 0, sizeof(int), st) != cudaSuccess)
                 return DGB_ERR_CUDA;
-            if (A.use_delj)
-                k_integrate2d_pair<true><<<(unsigned)pblocks, pthreads, pbytes, st>>>(A);
-            else
-                k_integrate2d_pair<false><<<(unsigned)pblocks, pthreads, pbytes, st>>>(A);
+            k_integrate2d_pair<<<(unsigned)pblocks, pthreads, pbytes, st>>>(A);
             return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
         }
     }

@@ -332,7 +332,8 @@ def test_two_items_per_cta_bitwise(cuda_lib, pts_l, delj):
     """A launch over one grid of 97-128 points runs two work items per CTA
     when the thread count is automatic; its densities are bitwise those of
     one item per CTA (threads forced to 128), with an odd number of
-    instances (the last CTA holds one item) and with the delj trick."""
+    instances (the last CTA holds one item).  With the delj trick the
+    engine keeps one item per CTA, so the two settings agree as well."""
     from dadi_gb300 import batch, integration as gi
     saved = gi.use_delj_trick
     try:
