@@ -822,10 +822,9 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     if (threads == 0)
         return DGB_ERR_ARG;
     // two work items per CTA where that fills the warps better (one grid,
-    // automatic thread count, no checkpoints, scratch in the workspace, the
-    // default delta_j: the delj trick's per-interval arithmetic leaves the
-    // compiler choices of contraction that differ between the two kernels,
-    // so it keeps one item per CTA and its bits)
+    // automatic thread count, no checkpoints, scratch in the workspace; the
+    // two-item kernel implements the default delta_j only, so the delj
+    // trick keeps one item per CTA)
     const int pthreads =
         (ngrids == 1 && !ckpt && !use_s && settings->threads == 0 && !A.use_delj)
             ? k2_pair_threads(Lmax)
