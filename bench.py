@@ -48,9 +48,10 @@ FLOPS_PER_PS = 30      # algorithmic FP64 flops per point-sweep (reference formu
 FP64_INSTR_PER_PS = 10  # FP64 pipe instructions per point-sweep in k_integrate2d
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the integration of one
 # full step of this workload, by launch mode: one mixed launch, or the three
-# launches of per_grid (1.09 + 0.329, 1.04 + 0.244, 1.03 + 0.191 GB)
+# launches of per_grid (L = 100 with two items per CTA 1.06 + 0.318 GB,
+# L = 90 1.04 + 0.244, L = 80 1.02 + 0.191)
 K2_TRAFFIC_BYTES = {"persistent": 2.89e9 + 0.886e9,
-                    "per_grid": (1.09 + 1.04 + 1.03) * 1e9 + (328.68 + 243.90 + 190.98) * 1e6}
+                    "per_grid": (1.06 + 1.04 + 1.02) * 1e9 + (318.36 + 243.98 + 191.32) * 1e6}
 
 
 def im_draws(n, seed):
