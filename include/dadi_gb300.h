@@ -73,8 +73,10 @@ typedef struct {
     int gam_placement;           /* batched engine: 0 auto, 1 shared memory, 2 workspace */
     int threads;                 /* batched engine: threads per CTA, 0 auto (the fewest
                                     warps, 2-4, that give every line of the largest grid a
-                                    lane), or 64 / 96 / 128 where that many threads hold
-                                    every line (else auto) */
+                                    lane; for a launch over one grid of 97-128 points, two
+                                    work items per CTA on ceil(2L/32) warps), or 64 / 96 /
+                                    128 where that many threads hold every line (else
+                                    auto), one item per CTA */
 } dgb_settings;
 
 int dgb_abi_version(void);
