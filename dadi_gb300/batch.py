@@ -5,7 +5,10 @@ Each (instance, grid) pair is one work item of a persistent kernel
 with the reference's operation order (dadi/Integration.py:147-176, 355-386),
 phi stays in shared memory for the whole loop, and CTAs pull items
 longest-first from an atomic counter, so instances with 11 or 20,000 steps
-balance across the SMs.  The spectra, their Richardson extrapolation and the
+balance across the SMs.  The launch shape — one launch over all grids or one
+per grid size (CTA size fitted to each L, two items per CTA where that fills
+the warps better), the Thomas scratch placement — is what
+autotune.tune_batch2d chooses; every shape gives the same bits.  The spectra, their Richardson extrapolation and the
 Poisson likelihood are computed on the device afterwards, so only parameters
 go in and spectra / likelihoods come out.
 
