@@ -82,6 +82,33 @@ def test_record_dtypes_match_header(tmp_path, struct, dtype, cfields):
     assert [dt.fields[n][1] for n in dt.names] == offs
 
 
+@pytest.mark.parametrize("struct,ctype", [("dgb_settings", "Settings"), ("dgb_pform", "PForm")])
+def test_ctypes_structs_match_header(tmp_path, struct, ctype):
+    """The ctypes structures passed by reference match the C structs (size
+    and every field offset)."""
+    if shutil.which("gcc") is None:
+        pytest.skip("no host C compiler")
+    cls = getattr(_lib, ctype)
+    names = [f[0] for f in cls._fields_]
+    size, offs = _c_layout(tmp_path, struct, names)
+    assert ctypes.sizeof(cls) == size
+    assert [getattr(cls, n).offset for n in names] == offs
+
+
+def test_inst2d_dtype_matches_header(tmp_path):
+    """batch.INST_DTYPE (the dgb_inst2d records the host fills) matches the C
+    struct."""
+    if shutil.which("gcc") is None:
+        pytest.skip("no host C compiler")
+    from dadi_gb300 import batch
+    cf = ["T", "initial_t", "nu", "m12", "m21", "gamma", "h", "theta0", "frozen_mask",
+          "nomut_mask"]
+    size, offs = _c_layout(tmp_path, "dgb_inst2d", cf)
+    dt = batch.INST_DTYPE
+    assert dt.itemsize == size
+    assert [dt.fields[n][1] for n in dt.names] == offs
+
+
 def test_count_steps_matches_python_schedule(lib):
     from dadi_gb300 import batch
     draws = cases.im_draws(16)
