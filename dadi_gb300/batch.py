@@ -100,6 +100,75 @@ def settings_from_globals(gam_placement=0, threads=0):
     return _lib.settings_struct(tsf, otsf, old, delj, gam_placement, threads)
 
 
+def _pform_at(f, t):
+    """Values of dgb_pform records f ((n, 4) float64, the kind in the first
+    int) at times t (n,), as pform_eval computes them."""
+    kind = np.ascontiguousarray(f).view(np.int32)[:, 0]
+    a, b, c = f[:, 1], f[:, 2], f[:, 3]
+    with np.errstate(all="ignore"):
+        return np.where(kind == _lib.PF_EXPGROW, a * (b / a) ** (t / c),
+                        np.where(kind == _lib.PF_EXPLOG, a * np.exp(np.log(b / a) * t / c),
+                                 np.where(kind == _lib.PF_LINEAR, a + b * t, a)))
+
+
+#: Reserve at most this many schedule rows from host bounds (else count them).
+ROW_BOUND_LIMIT = 2 * 10 ** 8
+
+
+def row_bounds(rec, settings, dx0s, max_steps):
+    """Upper bounds on the rows of each schedule of dgb_inst2d records (one
+    per instance, or per (instance, grid) under use_old_timestep), so that
+    dgb_sched2d can fill them in one pass; None when no useful bound exists
+    (non-finite or nonpositive sizes at an end of the interval, or more than
+    ROW_BOUND_LIMIT rows in all).
+
+    Every parametric form is monotone in t (constant, exponential, linear),
+    so over [initial_t, T] a size is at least its smaller end value, a
+    migration rate at most its larger one, and |gamma| and the dominance
+    factor of _compute_dt (dadi/Integration.py:147-176) at most their larger
+    ends.  Each step is then at least dt_min = timescale_factor / max(0.25 /
+    nu_min, m_max, 2 |gamma|_max tm_max) over both populations (division and
+    max are monotone in floating point), so a schedule has at most
+    (T - initial_t) / dt_min rows; the reserve adds 1e-9 relative and two
+    rows for the rounding of the sums of steps."""
+    rec = np.ascontiguousarray(rec)
+    t0, T = rec["initial_t"], rec["T"]
+    span = T - t0
+    if settings.use_old_timestep:
+        # one schedule per (instance, grid): dt = old_timescale_factor * dx0
+        dts = settings.old_timescale_factor * np.asarray(dx0s, dtype=np.float64)
+        span = np.repeat(span[:, None], len(dts), axis=1)
+        per = span / dts[None, :]
+    else:
+        live = span > 0  # the others take no step (NaN included)
+
+        def ends(f):
+            return _pform_at(f, t0), _pform_at(f, T)
+        vm = []
+        for k, mig in ((0, rec["m12"]), (1, rec["m21"])):
+            nu = np.minimum(*ends(rec["nu"][:, k]))
+            m = np.maximum(*ends(mig))
+            g = np.maximum(*[np.abs(v) for v in ends(rec["gamma"][:, k])])
+            tm = np.maximum(*[np.maximum(np.abs(h + (1 - 2 * h) * 0.5) * 0.5 * (1 - 0.5),
+                                         np.abs(h + (1 - 2 * h) * 0.25) * 0.25 * (1 - 0.25))
+                              for h in ends(rec["h"][:, k])])
+            if not np.all((np.isfinite(nu) & (nu > 0))[live]):
+                return None
+            with np.errstate(all="ignore"):
+                vm.append(np.maximum(np.maximum(0.25 / nu, m), g * 2 * tm))
+        with np.errstate(all="ignore"):
+            per = np.where(live, span * np.maximum(vm[0], vm[1]) / settings.timescale_factor,
+                           0.0)
+    per = np.where(span > 0, per, 0.0)
+    if not np.all(np.isfinite(per)):
+        return None
+    caps = np.where(per > 0, np.floor(per * (1 + 1e-9)) + 2, 0.0)
+    caps = np.minimum(caps, float(max_steps)).reshape(-1)
+    if caps.sum() > ROW_BOUND_LIMIT:
+        return None
+    return caps.astype(np.int64)
+
+
 #: dgb_item2d (dadi_gb300.h): one (integration, grid) work item.
 ITEM2D_DTYPE = np.dtype([("L", "i4"), ("masks", "i4"), ("xx_off", "i8"), ("out_off", "i8"),
                          ("sched", "i8")])
@@ -133,36 +202,56 @@ class Batch2D:
         self.ns = tuple(ns)
         self.max_steps = int(max_steps)
         self.gam_placement = gam_placement
-        self.threads = 0  # threads per CTA: 0 auto, 96 or 128 (dgb_settings.threads)
+        self.threads = 0  # threads per CTA: 0 auto, 64, 96 or 128 (dgb_settings.threads)
+        self.schedule_passes = 2
         self.launch_mode = "persistent"
         self.adjoint_ctas_per_sm = None  # None: sized to L2 (see adjoint)
         self.xxs = [numerics.default_grid(p) for p in self.pts_l]
         phi0 = [phimanip.phi_1D_to_2D(xx, phimanip.phi_1D(xx)) for xx in self.xxs]
         self.d_xx = _lib.to_device(torch, np.concatenate(self.xxs))
         self.d_phi0 = _lib.to_device(torch, np.concatenate([p.ravel() for p in phi0]))
-        self.d_dx0 = _lib.to_device(torch, np.array([xx[1] - xx[0] for xx in self.xxs]))
+        self.dx0s = np.array([xx[1] - xx[0] for xx in self.xxs])
+        self.d_dx0 = _lib.to_device(torch, self.dx0s)
         self.Ls = (ctypes.c_int * len(self.pts_l))(*self.pts_l)
         self.x_l = [xx[1] for xx in self.xxs]
         self.mask = np.zeros((ns[0] + 1, ns[1] + 1), dtype=bool)
         self.mask.flat[0] = self.mask.flat[-1] = True
 
     def launches_per_integrate(self):
-        """Kernel launches of ours in one integrate(): two schedule passes
-        (count, fill) and the integration, one launch per grid size with
-        launch_mode "per_grid"."""
+        """Kernel launches of ours in the last integrate(): the schedule
+        passes (one within host bounds, or count and fill) and the
+        integration, one launch per grid size with launch_mode "per_grid"."""
         per_grid = self.launch_mode == "per_grid" and len(set(self.pts_l)) > 1 \
             and not integration.current_settings()[2]
-        return 2 + (len(self.pts_l) if per_grid else 1)
+        return self.schedule_passes + (len(self.pts_l) if per_grid else 1)
 
-    def schedule(self, d_rec, n):
+    def schedule(self, d_rec, n, rec=None):
         """Device schedules of n dgb_inst2d records already on the device:
-        (table, row_off, row_cnt, status)."""
+        (table, row_off, row_cnt, status).  With the host records `rec`, one
+        fill pass into room reserved from host-side upper bounds on each
+        schedule's rows (row_bounds); else (or when no useful bound exists)
+        a count pass, a scan and a fill pass."""
         torch = self.torch
         lib = _lib.lib()
         st = settings_from_globals(self.gam_placement, self.threads)
         ng = len(self.pts_l)
         nsched = n * ng if st.use_old_timestep else n
         sh = _lib.stream_handle(torch)
+        caps = row_bounds(rec, st, self.dx0s, self.max_steps) if rec is not None else None
+        if caps is not None:
+            self.schedule_passes = 1
+            off_h = np.zeros(nsched, dtype=np.int64)
+            np.cumsum(caps[:-1], out=off_h[1:])
+            cnt = _lib.to_device(torch, caps.astype(np.int32), np.int32)
+            off = _lib.to_device(torch, off_h, np.int64)
+            table = torch.empty(max(int(caps.sum()), 1) * 11, dtype=torch.float64, device="cuda")
+            status = torch.zeros(n, dtype=torch.int32, device="cuda")
+            _lib.check(lib.dgb_sched2d(_lib.dptr(d_rec), n, ng, _lib.dptr(self.d_dx0),
+                                       ctypes.byref(st), self.max_steps, 2, _lib.dptr(cnt),
+                                       _lib.dptr(off), _lib.dptr(table), _lib.dptr(status), sh),
+                       "dgb_sched2d(fill within bounds)")
+            return table, off, cnt, status
+        self.schedule_passes = 2
         cnt = torch.zeros(nsched, dtype=torch.int32, device="cuda")
         _lib.check(lib.dgb_sched2d(_lib.dptr(d_rec), n, ng, _lib.dptr(self.d_dx0), ctypes.byref(st),
                                    self.max_steps, 0, _lib.dptr(cnt), None, None, None, sh),
@@ -202,7 +291,7 @@ class Batch2D:
         st = settings_from_globals(self.gam_placement, self.threads)
         rec = np.ascontiguousarray(rec)
         d_rec = _lib.to_device(torch, rec.view(np.uint8), np.uint8)
-        table, off, cnt, status = self.schedule(d_rec, n)
+        table, off, cnt, status = self.schedule(d_rec, n, rec)
         Lsq = torch.tensor([L * L for L in self.pts_l], dtype=torch.int64, device="cuda")
         if order is None:
             steps = cnt.to(torch.int64).view(n, -1)
@@ -244,7 +333,7 @@ class Batch2D:
         n = len(rec)
         rec = np.ascontiguousarray(rec)
         d_rec = _lib.to_device(torch, rec.view(np.uint8), np.uint8)
-        table, off, cnt, status = self.schedule(d_rec, n)
+        table, off, cnt, status = self.schedule(d_rec, n, rec)
         d_order = torch.argsort(-cnt.to(torch.int64), stable=True).to(torch.int32)
         masks = (rec["frozen"].astype(np.int32) & 0xff) | ((rec["nomut"].astype(np.int32) & 0xff) << 8)
         d_masks = _lib.to_device(torch, masks, np.int32)
@@ -300,7 +389,7 @@ class Batch2D:
         st = settings_from_globals(self.gam_placement, self.threads)
         rec = np.ascontiguousarray(rec)
         d_rec = _lib.to_device(torch, rec.view(np.uint8), np.uint8)
-        table, off, cnt, status = self.schedule(d_rec, n)
+        table, off, cnt, status = self.schedule(d_rec, n, rec)
         blocks, o = [], 0
         for L in self.pts_l:
             blocks.append(o)
@@ -375,7 +464,7 @@ class Batch2D:
             raise NotImplementedError("the adjoint does not support the delj trick")
         sh = _lib.stream_handle(torch)
         d_rec = _lib.to_device(torch, rec.view(np.uint8), np.uint8)
-        table, off, cnt, status = self.schedule(d_rec, n)
+        table, off, cnt, status = self.schedule(d_rec, n, rec)
         seeds = im_seeds(n) if seeds is None else np.ascontiguousarray(seeds)
         d_seed = _lib.to_device(torch, seeds.view(np.uint8), np.uint8)
         drows = torch.empty(max(int(table.numel() // 11), 1) * 60, dtype=torch.float64,

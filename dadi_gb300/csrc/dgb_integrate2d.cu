@@ -582,11 +582,14 @@ __global__ void k_sched2d(const dgb_inst2d *insts, int nsched, int ngrids, int p
     int inst = per_grid ? s / ngrids : s;
     double dx0 = dx0s[per_grid ? s % ngrids : 0];
     int err = 0;
-    long n = sched2d_walk(insts[inst], st, dx0, max_steps,
+    // fill == 2: row_cnt holds the room reserved at row_off (an upper bound
+    // on the rows); a walk that would exceed it stops with DGB_ST_STEPCAP
+    const long cap = (fill == 2) ? std::min<long>(max_steps, row_cnt[s]) : max_steps;
+    long n = sched2d_walk(insts[inst], st, dx0, cap,
                           fill ? table + row_off[s] * K2_ROW : nullptr, &err);
-    if (!fill)
+    if (fill != 1)
         row_cnt[s] = (int)n;
-    else if (err)
+    if (fill && err)
         atomicOr(status + inst, err);
 }
 
@@ -895,7 +898,8 @@ extern "C" int dgb_sched2d(const dgb_inst2d *insts, int ninst, int ngrids, const
                            const long *row_off, double *table, int *status, void *stream)
 {
     if (!insts || ninst < 1 || ngrids < 1 || !dx0s || !settings || max_steps < 1 ||
-        (!fill && !row_cnt) || (fill && (!row_off || !table || !status)))
+        fill < 0 || fill > 2 || (fill != 1 && !row_cnt) ||
+        (fill && (!row_off || !table || !status)))
         return DGB_ERR_ARG;
     int per_grid = settings->use_old_timestep ? 1 : 0;
     int nsched = per_grid ? ninst * ngrids : ninst;

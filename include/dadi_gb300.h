@@ -152,7 +152,11 @@ int dgb_integrate_precalc(double *phi, int ndim, int L, const double *xx,
  * Run it twice: fill == 0 writes row_cnt[s]; after the caller's exclusive
  * scan of row_cnt into row_off, fill == 1 writes the rows (DGB_ROW_STRIDE(2)
  * doubles each) at table + row_off[s]*11 and ORs DGB_ST_* bits into
- * status[instance] (caller zeroes it).  There is one schedule per instance,
+ * status[instance] (caller zeroes it).  Or once: with row_cnt[s] holding an
+ * upper bound on the rows of schedule s and row_off its exclusive scan,
+ * fill == 2 writes the rows there and replaces row_cnt[s] by their number
+ * (a walk that would pass the bound stops with DGB_ST_STEPCAP).  There is
+ * one schedule per instance,
  * or per (instance, grid) when settings->use_old_timestep makes dt depend on
  * the grid; dx0s (device) holds each grid's first spacing.
  *   insts  device, ninst dgb_inst2d */

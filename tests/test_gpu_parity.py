@@ -359,3 +359,34 @@ def test_two_items_per_cta_bitwise(cuda_lib, pts_l, delj):
             assert all(np.all(np.isfinite(a)) for a in out[0])
     finally:
         gi.use_delj_trick = saved
+
+
+@pytest.mark.parametrize("old_timestep", [False, True])
+def test_schedule_single_pass_matches_two_passes(cuda_lib, old_timestep):
+    """Filling the device schedules in one pass, into room reserved from the
+    host bounds, writes exactly the rows and counts of the count-scan-fill
+    passes (IM draws and records with every parametric form)."""
+    import torch
+    from dadi_gb300 import _lib, batch, integration as gi
+    from test_host import _random_records
+    saved = gi.use_old_timestep
+    try:
+        gi.use_old_timestep = old_timestep
+        eng = batch.Batch2D((20, 25, 30), (8, 8))
+        rec = np.concatenate([batch.im_instances(cases.im_draws(200)),
+                              _random_records(100, seed=9)])
+        n = len(rec)
+        d_rec = _lib.to_device(torch, rec.view(np.uint8), np.uint8)
+        one = eng.schedule(d_rec, n, rec)
+        assert eng.schedule_passes == 1
+        two = eng.schedule(d_rec, n)
+        assert eng.schedule_passes == 2
+        (t1, o1, c1, s1), (t2, o2, c2, s2) = [[x.cpu().numpy() for x in r] for r in (one, two)]
+        assert np.array_equal(c1, c2) and np.array_equal(s1, s2)
+        t1, t2 = t1.reshape(-1, 11), t2.reshape(-1, 11)
+        for s in range(len(c1)):
+            a = t1[o1[s]:o1[s] + c1[s]]
+            b = t2[o2[s]:o2[s] + c2[s]]
+            assert np.array_equal(a, b), s
+    finally:
+        gi.use_old_timestep = saved

@@ -242,3 +242,72 @@ def test_phi_1D_dominance_matches_integral_form():
         ours = phimanip.phi_1D(xx, gamma=gamma, h=h)
         ref = _phi1d_direct(xx, gamma, h, prec=5)
         assert np.max(2 * np.abs(ours - ref) / (ours + ref + 1e-12)) < 5e-3, (gamma, h)
+
+
+def _random_records(n, seed):
+    """dgb_inst2d records with every parametric form: exponential growth and
+    decline, exp-log, linear and constant sizes, migration, selection and
+    dominance that change over time."""
+    from dadi_gb300 import _lib, batch
+    rng = np.random.default_rng(seed)
+    rec = np.zeros(n, dtype=batch.INST_DTYPE)
+    rec["initial_t"] = rng.uniform(0, 0.05, n)
+    rec["T"] = rec["initial_t"] + rng.uniform(0.001, 0.5, n)
+    T = rec["T"]
+
+    def forms(lo, hi, kinds=(0, 1, 2, 3)):
+        a = rng.uniform(lo, hi, n)
+        b = rng.uniform(lo, hi, n)
+        kind = rng.choice(np.array(kinds), n)
+        out = np.zeros((n, 4))
+        out.view(np.int32)[:, 0] = kind
+        out[:, 1] = a
+        lin = kind == _lib.PF_LINEAR
+        # linear: from a at t = 0 to b at T
+        out[:, 2] = np.where(lin, (b - a) / T, b)
+        out[:, 3] = np.where(lin, 0.0, T)
+        return out
+
+    for k in (0, 1):
+        rec["nu"][:, k] = forms(0.01, 20)
+        # exponential forms need ends of one sign
+        rec["gamma"][:, k] = forms(-20, 20, kinds=(_lib.PF_CONST, _lib.PF_LINEAR))
+        rec["h"][:, k] = forms(0.0, 1.0, kinds=(_lib.PF_CONST, _lib.PF_LINEAR))
+    rec["m12"] = forms(0, 8)
+    rec["m21"] = forms(0, 8)
+    rec["theta0"] = forms(0.5, 2)
+    return rec
+
+
+def test_row_bounds_cover_the_schedules():
+    """The host bounds that let the device schedule be filled in one pass
+    are never below the rows the reference's time loop takes (the same walk
+    in C on the host), for the 4096-draw IM workload, records with every
+    parametric form, the old timestep and degenerate intervals; and they
+    stay close (the workload reserves 1.26x its rows)."""
+    from dadi_gb300 import batch
+    st = batch.settings_from_globals()
+    rec = batch.im_instances(cases.im_draws(4096))
+    steps = batch.count_steps(rec, st)
+    caps = batch.row_bounds(rec, st, [1e-3], 10 ** 8)
+    assert np.all(caps >= steps)
+    assert caps.sum() < 1.3 * steps.sum()
+    mixed = _random_records(3000, seed=5)
+    steps = batch.count_steps(mixed, st)
+    caps = batch.row_bounds(mixed, st, [1e-3], 10 ** 8)
+    assert caps is not None and np.all(caps >= steps)
+    capped = batch.row_bounds(mixed, st, [1e-3], 50)
+    assert np.all(capped <= 50) and np.all(capped >= np.minimum(steps, 50))
+    old = batch.settings_from_globals()
+    old.use_old_timestep = 1
+    steps = batch.count_steps(mixed, old)
+    caps = batch.row_bounds(mixed, old, [1e-3], 10 ** 8)
+    assert np.all(caps >= steps)
+    edge = mixed[:4].copy()
+    edge["T"][0] = edge["initial_t"][0]        # no time to integrate
+    edge["T"][1] = np.nan
+    caps = batch.row_bounds(edge, st, [1e-3], 10 ** 8)
+    assert caps[0] == 0 and caps[1] == 0
+    bad = mixed[:2].copy()
+    bad["nu"][0, 0] = batch._pf(0, 0.0)        # a zero size: no bound
+    assert batch.row_bounds(bad, st, [1e-3], 10 ** 8) is None
