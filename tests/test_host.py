@@ -311,3 +311,39 @@ def test_row_bounds_cover_the_schedules():
     bad = mixed[:2].copy()
     bad["nu"][0, 0] = batch._pf(0, 0.0)        # a zero size: no bound
     assert batch.row_bounds(bad, st, [1e-3], 10 ** 8) is None
+
+
+def test_serving_stream_and_summary():
+    """The serving workload's request stream (host side): seeded and
+    reproducible, Poisson arrivals at the stated rate, the 70/20/8/2 class
+    mix, gradients only on (40,40) IM requests with data, DFE entries on the
+    50-point gamma grid; and the latency summary over finished requests."""
+    from dadi_gb300 import serving
+    obs = np.ones((41, 41))
+    a = serving.config5_stream(2000, seed=3, rate=2000.0, obs=obs)
+    b = serving.config5_stream(2000, seed=3, rate=2000.0, obs=obs)
+    assert [(r.kind, r.params, r.pts_l, r.ns, r.arrival) for r in a] == \
+        [(r.kind, r.params, r.pts_l, r.ns, r.arrival) for r in b]
+    kinds = np.array([r.kind for r in a])
+    frac = {k: float(np.mean(kinds == k)) for k in ("im", "im_sel", "growth3", "four")}
+    for k, want in (("im", 0.70), ("im_sel", 0.20), ("growth3", 0.08), ("four", 0.02)):
+        assert abs(frac[k] - want) < 0.03, frac
+    arr = np.array([r.arrival for r in a])
+    assert np.all(np.diff(arr) > 0) and abs(arr[-1] - 1.0) < 0.1  # 2000 at 2000/s
+    gammas = -np.logspace(np.log10(2000), np.log10(1e-4), 50)
+    for r in a:
+        assert max(r.pts_l) <= 120
+        if r.want_grad:
+            assert r.kind == "im" and r.ns == (40, 40) and r.data is obs
+        if r.kind == "im_sel":
+            assert r.params[-2] in gammas and r.params[-1] in gammas
+    assert any(r.want_grad for r in a)
+    done = a[:10]
+    for i, r in enumerate(done):
+        r.t_done = r.arrival + 0.1 * (i + 1)
+    done[3].error = "failed"
+    summ = serving.latency_summary(done)
+    lat = np.array([0.1 * (i + 1) for i in range(10) if i != 3])
+    assert summ["completed"] == 9 and summ["errors"] == 1
+    assert summ["p50_s"] == pytest.approx(np.percentile(lat, 50))
+    assert summ["p99_s"] == pytest.approx(np.percentile(lat, 99))
