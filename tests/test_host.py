@@ -347,3 +347,21 @@ def test_serving_stream_and_summary():
     assert summ["completed"] == 9 and summ["errors"] == 1
     assert summ["p50_s"] == pytest.approx(np.percentile(lat, 50))
     assert summ["p99_s"] == pytest.approx(np.percentile(lat, 99))
+
+
+def test_autotune_sample_spans_the_cost_quantiles():
+    """The autotuner's sample: the requested number of instances, spread
+    evenly over the 5-85 % quantiles of the batch's step counts, in batch
+    order; the whole batch when it is smaller than the sample."""
+    from dadi_gb300 import autotune, batch
+    rec = batch.im_instances(cases.im_draws(1000))
+    steps = batch.count_steps(rec)
+    smp = autotune._sample(rec, 100)
+    assert len(smp) == 100
+    s = batch.count_steps(smp)
+    lo, hi = np.sort(steps)[[int(0.05 * 999), int(0.85 * 999)]]
+    assert s.min() >= lo and s.max() <= hi
+    assert np.median(s) == pytest.approx(np.quantile(steps, 0.45), rel=0.25)
+    idx = [int(np.nonzero(rec["T"] == t)[0][0]) for t in smp["T"]]
+    assert idx == sorted(idx)
+    assert len(autotune._sample(rec[:50], 100)) == 50
