@@ -14,9 +14,12 @@
 // batched engine a separate pass (k_sched2d, one thread per instance, so the
 // scalar pow/exp/divide chain of the schedule runs on full warps instead of
 // serialising inside every integrating CTA) evaluates the parametric forms
-// with the reference's operation order: count rows, scan, fill rows.
+// with the reference's operation order: one fill pass into room reserved
+// from host bounds on the rows, or count rows, scan, fill rows.
 // The batched integration is a persistent launch whose CTAs pull work items
-// longest-first from an atomic counter.
+// longest-first from an atomic counter (one launch over all grids, or one
+// per grid size with a CTA shaped for it, two items per CTA where that fills
+// the warps better: k_integrate2d_pair), or one CTA per item.
 //
 // Reference: the time loop of Integration.two_pops (dadi/Integration.py:
 // 340-386) with implicit_2Dx / implicit_2Dy (dadi/integration2D.c:19-160).
