@@ -20,7 +20,6 @@ one, each growing exponentially from nu0_i to nuF_i over T, symmetric
 migration): parameters (nu0_1, nu0_2, nu0_3, nuF_1, nuF_2, nuF_3, m12, m13,
 m23, T) with fixed selection gammas.
 """
-import ctypes
 
 import numpy as np
 

@@ -5,7 +5,6 @@ import os
 import re
 import shutil
 
-import numpy as np
 import pytest
 
 import cases

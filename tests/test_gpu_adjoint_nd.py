@@ -93,7 +93,7 @@ def test_adjoint_records_match_inline_setup(cuda_lib, P, L, frozen):
     their coefficients in every CTA (the minimal workspace), over 300 steps
     (more than one chunk of records, walked backwards)."""
     import torch
-    from dadi_gb300 import _lib, integration as gi
+    from dadi_gb300 import _lib
     import cases
     from util import table_rows
     lib = cuda_lib
