@@ -10,15 +10,19 @@ engine over the whole 4096-instance batch.  Synthetic data stands in for an
 observed spectrum (none is used by the reference's benchmark).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--serve R] [--adjoint]
+                  [--serve R] [--no-adjoint] [--no-config2]
 
 `value` times the engine with the parameters already on the device; `e2e`
 times the public API call (host parameter and data arrays in, host spectra and
 likelihoods out).  --impl reference times the CPU integrator restatement
 (the reference's algorithm: Python time loop over C sweeps) on all host
-cores over a bounded sample and scales it to the workload by point-sweeps.
-`serving` reports p50/p99 latency and spectra/s of a served mixed request
-stream; `adjoint` (with --adjoint) the time of 256 likelihood gradients.
+cores over a bounded stratified sample and scales it to the workload by
+point-sweeps; it imports nothing of the GPU package.  `parity` compares the
+GPU batch's spectra with the oracle's on the stratified 64-instance sample
+that the CPU baseline integrates.  `serving` reports p50/p99 latency and
+spectra/s of a served mixed request stream; `adjoint` the time of 256 IM and
+32 three-population likelihood gradients; `config2` the three-population
+growth model at pts [70,80,90].
 """
 import argparse
 import json
@@ -185,81 +189,142 @@ def point_sweeps(steps, pts_l):
 
 # ------------------------------------------------------------------ CPU arm
 
+WORKLOAD = ("batched 2-D IM, 4096 instances, pts [80,90,100], ns (40,40), "
+            "extrapolated + Poisson and multinomial ll")
+
+
+def workload_config(world, ps):
+    """The `config` of both arms' lines (identical, so the two are the same
+    workload)."""
+    return {"workload": WORKLOAD, "global_batch": NINST * world, "pts_l": list(PTS_L),
+            "ns": list(NS), "point_sweeps_per_step": int(ps),
+            "parallelism": "replicas x%d" % world,
+            "l2": "flushed between iterations (256 MB write); phi outputs 803 MB > L2"}
+
+
 def _cpu_one(args):
     """One extrapolated IM spectrum and its Poisson and multinomial
     log-likelihoods on the CPU restatement (Python time loop over the C
-    sweeps, as the reference runs)."""
-    p, pts_l, ns, obs = args
+    sweeps, as the reference runs).  Returns (index, seconds, spectrum)."""
+    i, p, pts_l, ns, obs = args
     from oracle import numerics as onum
     t = time.perf_counter()
     fs = onum.extrap_model(onum.IM, p, ns, pts_l)
     mask = onum.corner_mask(fs.shape)
     onum.ll(5e4 * fs, obs, mask)
     onum.ll_multinom(fs, obs, mask)
-    return time.perf_counter() - t
+    return i, time.perf_counter() - t, np.asarray(fs)
 
 
-def cpu_rate(draws, steps_all, budget_s, cores):
-    """Spectra/s of the CPU restatement on `cores` processes, measured on a
-    sample of instances and scaled to the workload by point-sweeps."""
-    import multiprocessing as mp
+def oracle_steps(draws):
+    """Steps of each instance's schedule, walked by the oracle (the
+    reference's loop restated in C)."""
     from oracle import clib
     clib.build()
-    ps_per_inst = steps_all * sum(2 * L * L for L in PTS_L)
-    total_ps = float(np.sum(ps_per_inst))
-    # a sample spread over the cost distribution, sized to the budget
-    rng = np.random.default_rng(123)
-    idx = rng.permutation(len(draws))
-    ns_per_ps = 25e-9  # rough single-core cost, only to size the sample
-    chosen, work = [], 0.0
-    for i in idx:
-        c = ps_per_inst[i] * ns_per_ps
-        if c > budget_s * cores / 4:
-            continue
-        chosen.append(i)
-        work += c
-        if work > budget_s * cores * 0.8:
-            break
-    # the observed spectrum as the GPU arm makes it: Poisson(5e4 * model(set 0))
+    return clib.im_steps(draws)
+
+
+def oracle_obs(draws):
+    """The observed spectrum as both arms make it: Poisson(5e4 * model(set 0))."""
     from oracle import numerics as onum
     fs0 = onum.extrap_model(onum.IM, draws[0], NS, PTS_L)
-    obs = np.random.default_rng(0).poisson(5e4 * fs0).astype(np.float64)
-    ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
-    with ctx.Pool(cores) as pool:
-        pool.map(_cpu_one, [(draws[i], PTS_L, NS, obs) for i in chosen], chunksize=1)
-    wall = time.perf_counter() - t0
-    sample_ps = float(np.sum(ps_per_inst[chosen]))
-    ps_rate = sample_ps / wall
-    value = len(draws) * ps_rate / total_ps
-    return value, len(chosen), wall, sample_ps
+    return np.random.default_rng(0).poisson(5e4 * fs0).astype(np.float64)
+
+
+def parity_sample(draws, steps):
+    """The stratified 64-instance sample (draws 0-5, the longest and shortest
+    schedules, each parameter's extremes, step-count quantiles)."""
+    import cases
+    return cases.im_parity_sample(draws, steps, 64)
+
+
+def cpu_rate(draws, steps, idx, cores, obs, pool=None):
+    """Spectra/s of the CPU restatement on `cores` processes for the sample
+    idx, scaled to the workload by point-sweeps: cores x (sample point-sweeps
+    / summed per-instance seconds) -- the throughput of the cores kept busy,
+    as the whole workload would keep them.  Returns (value, info, spectra by
+    instance)."""
+    import multiprocessing as mp
+    ps_per_inst = steps * sum(2 * L * L for L in PTS_L)
+    total_ps = float(np.sum(ps_per_inst))
+    order = sorted(idx, key=lambda i: -steps[i])  # longest first packs best
+    own = pool is None
+    if own:
+        pool = mp.get_context("spawn").Pool(cores)
+    try:
+        t0 = time.perf_counter()
+        res = list(pool.imap_unordered(_cpu_one, [(int(i), draws[i], PTS_L, NS, obs)
+                                                  for i in order], chunksize=1))
+        wall = time.perf_counter() - t0
+    finally:
+        if own:
+            pool.close()
+            pool.join()
+    task_s = float(sum(r[1] for r in res))
+    sample_ps = float(np.sum(ps_per_inst[list(idx)]))
+    value = len(draws) * (cores * sample_ps / task_s) / total_ps
+    info = {"instances": len(idx), "point_sweeps": sample_ps, "task_s": task_s, "wall_s": wall}
+    return value, info, {r[0]: r[2] for r in res}
+
+
+def parity_of(fs_gpu, fs_cpu):
+    """Spectrum parity of the GPU batch's spectra against the oracle's over
+    the instances in fs_cpu: entries >= 1e-12 of a spectrum's largest
+    compared relatively, smaller ones absolutely relative to the largest
+    (the tests' spectrum bar)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import util
+    worst, worst_small, n_small, worst_i = 0.0, 0.0, 0, None
+    for i, ref in fs_cpu.items():
+        rel, ab, ns = util.fs_parity(fs_gpu[i], ref)
+        if rel > worst:
+            worst, worst_i = rel, int(i)
+        worst_small = max(worst_small, ab)
+        n_small += ns
+    return {"n_checked": len(fs_cpu), "max_rel": worst, "worst_instance": worst_i,
+            "n_small": n_small, "max_abs_small_over_max": worst_small,
+            "bar": "max_rel <= 1e-9 over entries >= 1e-12 x max; smaller entries <= 1e-21 x max",
+            "against": "the oracle (the reference's algorithm, bit-identical to dadi's "
+                       "golden vectors) on the stratified 64-instance sample"}
 
 
 def run_reference(a, world, rank):
+    """The reference's algorithm (the oracle port: Python time loop over the
+    C sweeps, as dadi runs) on all host cores.  Each step integrates one
+    quarter of the stratified 64-instance sample (16 instances spread over the
+    step-count quantiles), scaled to the workload by point-sweeps.  Nothing
+    of the GPU package is imported."""
     if rank != 0:
         return 0
-    from dadi_gb300 import batch
+    import multiprocessing as mp
     draws = im_draws(NINST, 0)
-    steps = batch.count_steps(batch.im_instances(draws))
+    steps = oracle_steps(draws)
+    ps = point_sweeps(steps, PTS_L)
+    obs = oracle_obs(draws)
+    idx = parity_sample(draws, steps)
+    by_cost = sorted(idx, key=lambda i: steps[i])
+    slices = [by_cost[r::4] for r in range(4)]
     cores = os.cpu_count() or 1
     vals = []
-    for it in range(a.warmup + a.steps):
-        v, n, wall, sps = cpu_rate(draws, steps, a.cpu_budget, cores)
-        if it >= a.warmup:
-            vals.append((v, n, wall, sps))
+    with mp.get_context("spawn").Pool(cores) as pool:
+        for it in range(a.warmup + a.steps):
+            v, info, _ = cpu_rate(draws, steps, slices[it % 4], cores, obs, pool)
+            if it >= a.warmup:
+                vals.append((v, info))
     v = float(np.mean([x[0] for x in vals]))
+    info = vals[-1][1]
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "spectra/s", "n_gpus": a.gpus,
-        "steps": a.steps, "warmup": a.warmup, "ms_per_step": float(np.mean([x[2] for x in vals])) * 1e3,
+        "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": float(np.mean([x[1]["wall_s"] for x in vals])) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seed-0 IM parameter draws)",
-        "config": {"workload": "batched 2-D IM, 4096 instances, pts [80,90,100], ns (40,40), "
-                               "extrapolated + Poisson and multinomial ll", "global_batch": NINST,
-                   "pts_l": list(PTS_L), "ns": list(NS)},
+        "data": "synthetic (seed-0 IM parameter draws; observed spectrum Poisson(5e4*model))",
+        "config": workload_config(world, ps),
         "cpu_baseline": {"value": v, "unit": "spectra/s", "cores": cores, "kind": "port",
-                         "sample": "%d seed-0 instances per step (%.3g point-sweeps, %.1f s on "
-                                   "%d processes), scaled to the 4096-instance workload by "
-                                   "point-sweeps" % (vals[-1][1], vals[-1][3], vals[-1][2], cores)},
+                         "sample": "per step 16 of the stratified 64 seed-0 instances "
+                                   "(%.3g point-sweeps, %.1f s of CPU on %d processes), "
+                                   "scaled to the 4096-instance workload by point-sweeps"
+                                   % (info["point_sweeps"], info["task_s"], cores)},
         "e2e": {"value": v, "unit": "spectra/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -342,6 +407,7 @@ def run_ours(a, world, rank, local):
     # the scores of the workload: Poisson ll of 5e4 * model and the
     # multinomial ll (optimal scaling) against the observed spectrum
     ll_h, llm_h = ll.cpu().numpy(), llm.cpu().numpy()
+    fs_last = fs.cpu().numpy()
     scores = {"ll_set0": float(ll_h[0]), "ll_multinom_set0": float(llm_h[0]),
               "ll_best": float(np.nanmax(ll_h)), "ll_multinom_best": float(np.nanmax(llm_h))}
 
@@ -389,18 +455,24 @@ def run_ours(a, world, rank, local):
                            "concurrent_grids_value: the three grids on three streams), "
                            "scaled by point-sweeps" % len(sample)}
 
-    # CPU baseline (oracle restatement, bounded sample), rank 0 only
-    cpu = None
-    if rank == 0 and not a.no_cpu:
+    # CPU baseline (oracle restatement, bounded sample) on rank 0 at N=1, and
+    # the parity of the GPU batch's spectra against it on that sample
+    cpu = parity = None
+    if rank == 0 and world == 1 and not a.no_cpu:
         cores = os.cpu_count() or 1
-        v, n, wall, sps = cpu_rate(draws, steps, a.cpu_budget, cores)
+        idx = parity_sample(draws, steps)
+        v, info, fs_cpu = cpu_rate(draws, steps, idx, cores, obs)
         cpu = {"value": v, "unit": "spectra/s", "cores": cores, "kind": "port",
-               "sample": "%d seed-0 instances (%.3g point-sweeps) on %d processes in %.1f s, "
-                         "scaled to the 4096-instance workload by point-sweeps"
-                         % (n, sps, cores, wall)}
+               "sample": "the stratified 64 seed-0 instances (draws 0-5, longest and shortest "
+                         "schedules, each parameter's extremes, step-count quantiles; %.3g "
+                         "point-sweeps, %.1f s of CPU on %d processes, %.1f s wall), scaled "
+                         "to the 4096-instance workload by point-sweeps"
+                         % (info["point_sweeps"], info["task_s"], cores, info["wall_s"])}
+        parity = parity_of(fs_last, fs_cpu)
 
     serve = run_serving(a, obs) if (rank == 0 and a.serve > 0) else None
-    adjoint = run_adjoint(a, obs) if (rank == 0 and a.adjoint) else None
+    adjoint = run_adjoint(a, obs) if (rank == 0 and not a.no_adjoint) else None
+    config2 = run_config2(a) if (rank == 0 and not a.no_config2) else None
 
     if rank != 0:
         return 0
@@ -422,12 +494,8 @@ def run_ours(a, world, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seed-%d IM parameter draws; observed spectrum Poisson(5e4*model))"
                 % rank,
-        "config": {"workload": "batched 2-D IM, 4096 instances, pts [80,90,100], ns (40,40), "
-                               "extrapolated + Poisson and multinomial ll",
-                   "global_batch": NINST * world, "pts_l": list(PTS_L), "ns": list(NS),
-                   "point_sweeps_per_step": ps, "parallelism": "replicas x%d" % world,
-                   "l2": "flushed between iterations (256 MB write); phi outputs 803 MB > L2",
-                   "gam_placement": eng.gam_placement, "launch_mode": eng.launch_mode,
+        "config": workload_config(world, ps),
+        "engine": {"gam_placement": eng.gam_placement, "launch_mode": eng.launch_mode,
                    "threads_per_cta": eng.threads or "auto"},
         "autotune": None if tuned is None else {
             "choice": list(tuned["choice"]), "sample_instances": tuned["sample"],
@@ -464,8 +532,10 @@ def run_ours(a, world, rank, local):
         "plain": plain,
         "batched_over_plain": (value / plain["value"]) if plain else None,
         "cpu_baseline": cpu,
+        "parity": parity,
         "serving": serve,
         "adjoint": adjoint,
+        "config2": config2,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -568,6 +638,31 @@ def run_adjoint(a, obs):
     return out
 
 
+def run_config2(a):
+    """The three-population growth model at pts [70,80,90], ns (20,20,20),
+    extrapolated (T = 0.15, 675 steps per grid), through the drop-in public
+    call (make_extrap_func: the three grids on their own streams; host
+    parameters in, host spectrum out): host wall clock, median of 3 after a
+    warm-up."""
+    import torch
+    from dadi_gb300 import models, numerics
+    f = numerics.make_extrap_func(models.growth3)
+    args = (models.GROWTH3_DEFAULT, (20, 20, 20), [70, 80, 90])
+    f(*args)
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fs = f(*args)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    ps = 675 * 3 * (70 ** 3 + 80 ** 3 + 90 ** 3)
+    t = float(np.median(times))
+    return {"model": "three populations, exponential growth, pts [70,80,90], ns (20,20,20)",
+            "seconds": t, "times_s": times, "point_sweeps": ps,
+            "point_sweeps_per_s": ps / t, "finite": bool(np.all(np.isfinite(np.asarray(fs))))}
+
+
 def run_profile_case(a):
     """A small batch for ncu captures: each launch of the integration kernel
     lasts ~0.1 s and holds ~100 MB on the device."""
@@ -654,8 +749,11 @@ def main():
     ap.add_argument("--serve-sustained", type=int, default=200,
                     help="requests of a second, below-capacity stream (0: skip)")
     ap.add_argument("--serve-sustained-rate", type=float, default=20.0)
-    ap.add_argument("--adjoint", action="store_true",
-                    help="also time 256 IM gradients at pts [100,110,120]")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip timing 256 IM gradients at pts [100,110,120] and 32 "
+                         "three-population gradients at pts 80")
+    ap.add_argument("--no-config2", action="store_true",
+                    help="skip timing the three-population growth model at pts [70,80,90]")
     ap.add_argument("--profile-items", type=int, default=0,
                     help="run only a small batch (this many seed-0 instances with 200-800 "
                          "steps, twice) for profiler captures, then exit")

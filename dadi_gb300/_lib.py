@@ -211,25 +211,33 @@ def settings_struct(timescale_factor=1e-3, old_timescale_factor=0.1, use_old_tim
                     int(threads))
 
 
-def fp64_fma_peak_tflops(torch, iters=4096, active_lanes=32):
-    """Measured FP64 FMA rate of this GPU in TFLOP/s (2 flops per FMA):
-    4 warps per SM on every SM, 8 independent chains per thread, counting
-    only the FMAs of the active lanes."""
+def fp64_fma_peak_tflops(torch, active_lanes=32, target_s=0.1, repeats=5):
+    """Measured FP64 FMA rate of this GPU in TFLOP/s (2 flops per FMA): 4 and
+    8 warps per SM on every SM, 8 independent chains per thread, counting only
+    the FMAs of the active lanes; each launch sized to last about target_s,
+    the best of `repeats` launches per shape."""
     nsm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
-    blocks, threads = nsm, 128
-    out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
     sh = stream_handle(torch)
-    check(lib().dgb_probe_fp64_fma(dptr(out), blocks, threads, 16, active_lanes, sh),
-          "dgb_probe_fp64_fma")
     best = 0.0
-    for _ in range(3):
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        check(lib().dgb_probe_fp64_fma(dptr(out), blocks, threads, iters, active_lanes, sh),
-              "dgb_probe_fp64_fma")
-        e1.record()
-        torch.cuda.synchronize()
-        fmas = blocks * (threads // 32) * active_lanes * iters * 8
-        best = max(best, 2.0 * fmas / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    for threads in (128, 256):
+        blocks = nsm
+        out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
+
+        def timed(iters):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            check(lib().dgb_probe_fp64_fma(dptr(out), blocks, threads, iters, active_lanes, sh),
+                  "dgb_probe_fp64_fma")
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1) * 1e-3
+        timed(16)
+        iters = 4096
+        t = timed(iters)
+        iters = int(min(2 ** 30 // 8, max(iters, iters * target_s / max(t, 1e-6))))
+        for _ in range(repeats):
+            t = timed(iters)
+            fmas = blocks * (threads // 32) * active_lanes * iters * 8
+            best = max(best, 2.0 * fmas / t / 1e12)
     return best

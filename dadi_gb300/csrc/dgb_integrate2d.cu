@@ -870,26 +870,32 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
 // DGB_NOALLOC_MAX_L (128 KB), resident on every GPU that loads the library.
 static __device__ __align__(256) double g_noalloc_gam[DGB_NOALLOC_MAX_L * DGB_NOALLOC_MAX_L];
 
-// Device address of g_noalloc_gam per device, looked up once per device with
-// that device current (host code must not use the symbol itself).
+// Device address of g_noalloc_gam per device, looked up with that device
+// current (host code must not use the symbol itself).  Only a successful
+// lookup is kept: a failed one (e.g. made during stream capture) is retried
+// by the next call.
 constexpr int NOALLOC_MAXDEV = 64;
-static std::once_flag g_noalloc_once[NOALLOC_MAXDEV];
+static std::mutex g_noalloc_mu;
 static double *g_noalloc_ptr[NOALLOC_MAXDEV];
-static int g_noalloc_rc[NOALLOC_MAXDEV];
 
 static int noalloc_scratch(double **ptr)
 {
     int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAXDEV)
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0)
         return DGB_ERR_CUDA;
-    std::call_once(g_noalloc_once[dev], [dev]() {
+    if (dev >= NOALLOC_MAXDEV)
+        return DGB_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
         void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_gam);
+        if (cudaGetSymbolAddress(&p, g_noalloc_gam) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return DGB_ERR_CUDA;
+        }
         g_noalloc_ptr[dev] = (double *)p;
-        g_noalloc_rc[dev] = (e == cudaSuccess && p) ? DGB_OK : DGB_ERR_CUDA;
-    });
+    }
     *ptr = g_noalloc_ptr[dev];
-    return g_noalloc_rc[dev];
+    return DGB_OK;
 }
 
 } // namespace dgb
@@ -949,14 +955,18 @@ extern "C" int dgb_integrate2d_noalloc(double *phi, int L, const double *xx, con
         return DGB_ERR_TOO_LARGE;
     if (nsteps == 0)
         return DGB_OK;
-    double *scratch = nullptr;
-    int rc = dgb::noalloc_scratch(&scratch);
-    if (rc)
-        return rc;
-    size_t bytes = 0;
-    if (!dgb::k2_smem_fits(L, false, use_delj_trick != 0, &bytes))
-        return DGB_ERR_UNSUPPORTED;
     dgb::K2Args A = {};
+    size_t bytes = 0;
+    // the Thomas scratch in shared memory where it fits beside phi (as
+    // dgb_integrate_table does); only larger grids use the static array
+    A.gam_smem = dgb::k2_smem_fits(L, true, use_delj_trick != 0, &bytes);
+    if (!A.gam_smem) {
+        if (!dgb::k2_smem_fits(L, false, use_delj_trick != 0, &bytes))
+            return DGB_ERR_UNSUPPORTED;
+        int rc = dgb::noalloc_scratch(&A.gam_glob);
+        if (rc)
+            return rc;
+    }
     A.ngrids = 1;
     A.L[0] = L;
     A.xx_all = xx;
@@ -968,8 +978,6 @@ extern "C" int dgb_integrate2d_noalloc(double *phi, int L, const double *xx, con
     A.nwork = 1;
     A.Lmax = L;
     A.use_delj = use_delj_trick;
-    A.gam_smem = 0;
-    A.gam_glob = scratch;
     return dgb::k2_launch(A, 1, bytes, (cudaStream_t)stream);
 }
 

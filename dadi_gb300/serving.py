@@ -509,11 +509,13 @@ def _item_schedules(recs, req_of_item, L_of_item, st, dx0_of_L):
 
 def config5_stream(n, seed=0, rate=2000.0, grad_frac=0.1, obs=None):
     """The mixed request stream of the serving workload: Poisson arrivals at
-    `rate` per second; 70% 2-D IM (pts base uniform in 40..120, pts_l = base,
-    base+10, base+20, ns (20,20) or (40,40)), 20% DFE cache entries (IM with
+    `rate` per second; 70% 2-D IM (pts_l = base, base+10, base+20 with the
+    base uniform in 40..100, so every grid lies in 40..120; ns (20,20) or
+    (40,40)), 20% DFE cache entries (IM with
     selection, gamma1 and gamma2 from the 50-point log grid on
-    [-2000, -1e-4]), 8% 3-D growth model (pts 60..90), 2% four populations
-    (pts 30..40, ns (10,10,10,10)); grad_frac of the IM requests also ask for
+    [-2000, -1e-4]), 8% 3-D growth model (grids in 60..90: base 60..70),
+    2% four populations (grids in 30..40: base 30..36, ns (10,10,10,10));
+    grad_frac of the IM requests also ask for
     gradients (they need `obs`, an observed 41x41 spectrum)."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate, n)

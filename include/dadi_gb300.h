@@ -356,15 +356,20 @@ int dgb_extrap_ll(const dgb_extrap_item *items, int nitems, double fail_mag, voi
  * allocate device memory or pass a workspace -- e.g. code that runs where
  * cudaMalloc is not allowed or a caching allocator must not be entered, or
  * a host that embeds the library without a device allocator of its own.
- * Its Thomas scratch is a file-scope device array of DGB_NOALLOC_MAX_L^2
+ * Grids small enough for the Thomas scratch to sit in shared memory beside
+ * the density (on GB300 up to L = 116, or 113 with the delj trick) keep it
+ * there.  Larger grids use a file-scope device array of DGB_NOALLOC_MAX_L^2
  * doubles (128 KB) that every GPU which loads the library holds until the
  * process exits; grids with L > DGB_NOALLOC_MAX_L return DGB_ERR_TOO_LARGE.
- * The first call on each device looks up the array's address
+ * The first such call on each device looks up the array's address
  * (cudaGetSymbolAddress) with that device current, so make that first call
- * before any stream capture.  Every call shares the one array, which keeps
- * the previous call's contents (nothing in it needs to start at zero): calls
- * that overlap on the GPU -- on different streams or from different host
- * threads -- race on it, so serialise them.  The call allocates nothing. */
+ * before any stream capture; a failed lookup returns DGB_ERR_CUDA and is
+ * retried by the next call.  Device ordinals 64 and up return
+ * DGB_ERR_UNSUPPORTED.  Every call that uses the array shares it, and it
+ * keeps the previous call's contents (nothing in it needs to start at
+ * zero): such calls that overlap on the GPU -- on different streams or from
+ * different host threads -- race on it, so serialise them.  The call
+ * allocates nothing. */
 #define DGB_NOALLOC_MAX_L 128
 int dgb_integrate2d_noalloc(double *phi, int L, const double *xx, const double *table,
                             int nsteps, int frozen_mask, int nomut_mask, int use_delj_trick,

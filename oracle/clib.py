@@ -15,7 +15,7 @@ _ref = None
 
 def build():
     """Compile oracle/sweeps.c (and the reference C if its tree is present)."""
-    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    subprocess.run(["make", "-s", "-C", _HERE, "oracle"], check=True)
 
 
 def _ptr(a):
@@ -41,6 +41,9 @@ def lib():
         L.orc_sweep_precalc.restype = ctypes.c_int
         L.orc_tridiag_solve.argtypes = [_dp, _dp, _dp, _dp, _dp, ctypes.c_int]
         L.orc_tridiag_solve.restype = ctypes.c_int
+        L.orc_im_steps.argtypes = [_dp, ctypes.c_long, ctypes.c_double, ctypes.c_long,
+                                   ctypes.POINTER(ctypes.c_long)]
+        L.orc_im_steps.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -83,6 +86,16 @@ def sweep_precalc(phi, axis, a, b, c, dt):
     if rc != 0:
         raise RuntimeError("orc_sweep_precalc failed: %d" % rc)
     return phi
+
+
+def im_steps(params, timescale_factor=1e-3, max_steps=10 ** 8):
+    """Steps of the reference two_pops loop of Demographics2D.IM for each row
+    (s, nu1, nu2, T, m12, m21) of params (see orc_im_steps in sweeps.c)."""
+    p = np.ascontiguousarray(np.asarray(params, dtype=np.float64).reshape(-1, 6))
+    out = np.zeros(len(p), dtype=np.int64)
+    lib().orc_im_steps(_ptr(p), len(p), float(timescale_factor), int(max_steps),
+                       out.ctypes.data_as(ctypes.POINTER(ctypes.c_long)))
+    return out
 
 
 def tridiag(a, b, c, r):

@@ -262,6 +262,36 @@ def growth3(params, ns, pts):
     return from_phi(phi, ns, xx), xx
 
 
+def IM_sel(params, ns, pts):
+    """DFE.DemogSelModels.IM_sel (dadi/DFE/DemogSelModels.py:162-197): IM_pre_sel
+    (:64-121) with nuPre = 1 and TPre = 0, so the ancestral density is
+    phi_1D with gamma1 (one_pop over T = 0 returns it unchanged)."""
+    s, nu1, nu2, T, m12, m21, gamma1, gamma2 = params
+    xx = default_grid(pts)
+    phi = phi_1D_to_2D(xx, phi_1D(xx, gamma=gamma1))
+    nu1_0, nu2_0 = 1 * s, 1 * (1 - s)
+    nu1_func = lambda t: nu1_0 * (nu1 / nu1_0) ** (t / T)
+    nu2_func = lambda t: nu2_0 * (nu2 / nu2_0) ** (t / T)
+    phi = oint.two_pops(phi, xx, T, nu1_func, nu2_func, m12=m12, m21=m21,
+                        gamma1=gamma1, gamma2=gamma2)
+    return from_phi(phi, ns, xx), xx
+
+
+def four_split(params, ns, pts):
+    """Four populations split successively from one (dadi/PhiManip.py:
+    214-250, 412-450), then four_pops for T with constant sizes and symmetric
+    migration m."""
+    nu1, nu2, nu3, nu4, m, T = params
+    xx = default_grid(pts)
+    phi = phi_1D_to_2D(xx, phi_1D(xx))
+    phi = phi_2D_to_3D_admix(phi, 0, xx, xx, xx)
+    phi = phi_3D_to_4D(phi, 0.0, 0.0, xx, xx, xx, xx)
+    phi = oint.four_pops(phi, xx, T, nu1, nu2, nu3, nu4,
+                         m12=m, m13=m, m14=m, m21=m, m23=m, m24=m,
+                         m31=m, m32=m, m34=m, m41=m, m42=m, m43=m)
+    return from_phi(phi, ns, xx), xx
+
+
 def extrap_model(model, params, ns, pts_l):
     """make_extrap_func(model)(params, ns, pts_l) with extrap_x = xx[1]."""
     res, xs = [], []

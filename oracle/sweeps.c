@@ -282,3 +282,44 @@ int orc_tridiag_solve(const double *a, const double *b, const double *c,
     free(gam);
     return 0;
 }
+
+/* Steps taken by the two_pops time loop (dadi/Integration.py:346-386, dt by
+ * _compute_dt, :147-176) of Demographics2D.IM (dadi/Demographics2D.py:
+ * 297-307) for each parameter row (s, nu1, nu2, T, m12, m21):
+ * nu1(t) = s (nu1/s)^(t/T), nu2(t) = (1-s) (nu2/(1-s))^(t/T), constant
+ * migration, no selection.  The walk uses the reference's operations in
+ * its order (libm pow, Python's max/min keeping the first extreme), so the
+ * counts equal the reference loop's.  A walk that passes max_steps stops
+ * there and reports max_steps + 1. */
+static double orc_im_dt(double nu, double m, double tsf)
+{
+    double mx = 0.25 / nu;
+    if (m > mx)
+        mx = m;
+    if (0.0 > mx) /* |gamma| * 2 * ... with gamma = 0 */
+        mx = 0.0;
+    return mx > 0 ? tsf / mx : INFINITY;
+}
+
+int orc_im_steps(const double *params, long n, double tsf, long max_steps, long *steps)
+{
+    for (long i = 0; i < n; i++) {
+        const double *p = params + 6 * i;
+        const double s = p[0], nu1 = p[1], nu2 = p[2], T = p[3], m12 = p[4], m21 = p[5];
+        double t = 0.0;
+        double n1 = s * pow(nu1 / s, t / T), n2 = (1 - s) * pow(nu2 / (1 - s), t / T);
+        long k = 0;
+        while (t < T && k <= max_steps) {
+            double d1 = orc_im_dt(n1, m12, tsf), d2 = orc_im_dt(n2, m21, tsf);
+            double dt = (d2 < d1) ? d2 : d1;
+            double rest = T - t;
+            double this_dt = (rest < dt) ? rest : dt;
+            t = t + this_dt;
+            n1 = s * pow(nu1 / s, t / T);
+            n2 = (1 - s) * pow(nu2 / (1 - s), t / T);
+            k++;
+        }
+        steps[i] = k;
+    }
+    return 0;
+}

@@ -163,6 +163,40 @@ def im_draws(n=4096, seed=0):
     return np.stack([s, nu1, nu2, T, m12, m21], axis=1)
 
 
+def im_parity_sample(draws, steps, n=64):
+    """Indices (sorted) of a stratified sample of the 4096-draw IM workload for
+    parity at scale: draws 0-5; the longest and shortest schedules; the
+    extremes of each parameter (smallest and largest nu1, nu2, T, m12, m21 and
+    s); then instances at evenly spaced quantiles of the step counts until
+    there are n.  steps[i] is instance i's step count."""
+    steps = np.asarray(steps)
+    picks = list(range(6))
+    picks += [int(np.argmax(steps)), int(np.argmin(steps))]
+    for col in range(6):
+        picks += [int(np.argmin(draws[:, col])), int(np.argmax(draws[:, col]))]
+    chosen = []
+    for i in picks:
+        if i not in chosen:
+            chosen.append(i)
+    order = np.argsort(steps, kind="stable")
+    q = 0
+    nq = n - len(chosen)
+    while len(chosen) < n:
+        # quantile ranks in (0, 1): skip the extremes already taken
+        r = order[int(round((q + 0.5) / max(nq, 1) * (len(order) - 1)))]
+        q += 1
+        if int(r) not in chosen:
+            chosen.append(int(r))
+        if q > 4 * len(order):
+            break
+    return np.array(sorted(chosen[:n]), dtype=np.int64)
+
+
+#: Dadi golden spectra at the batched workload's grids: this many of the
+#: parity sample, the longest schedules first.
+IM_SCALE_GOLDEN = 16
+
+
 #: Config-2 workload: 3 populations with exponential growth (see oracle growth3).
 GROWTH3 = dict(params=((0.5, 1.0, 2.0), (5.0, 0.2, 10.0), (0.5, 1.5, 3.0), (-2.0, 0.0, 5.0),
                        0.15),

@@ -3,7 +3,8 @@
 Run once in a container that holds the reference tree (it cannot run on a GPU
 host, which has no reference):
 
-    python tests/golden/make_golden.py [--ref /root/reference] [--build /tmp/dadi_ref]
+    python tests/golden/make_golden.py --ref <reference tree> [--build <scratch dir>]
+                                       [--only im_scale]
 
 The reference is copied to the build directory, its pyproject.toml moved aside
 (its licence field trips the installed setuptools), its Cython extensions built
@@ -16,6 +17,7 @@ import os
 import shutil
 import subprocess
 import sys
+import tempfile
 import time
 import types
 
@@ -209,6 +211,40 @@ def gen_models(dadi, out, big):
                                                data) for i in sel])
 
 
+_DADI = None
+
+
+def _im_extrap(p):
+    fim = _DADI.Numerics.make_extrap_func(_DADI.Demographics2D.IM)
+    return np.asarray(fim(p, (40, 40), [80, 90, 100]).data)
+
+
+def gen_im_scale(dadi, out, procs):
+    """Dadi spectra of the batched workload (seed-0 IM draws, pts [80,90,100],
+    ns (40,40)) for the cases.IM_SCALE_GOLDEN longest schedules of the
+    stratified parity sample (cases.im_parity_sample), computed by worker
+    processes forked from this one (dadi's C integrator is single-threaded)."""
+    global _DADI
+    import multiprocessing as mp
+    sys.path.insert(0, os.path.join(HERE, "..", ".."))
+    from oracle import clib
+    clib.build()
+    draws = cases.im_draws()
+    steps = clib.im_steps(draws)
+    idx = cases.im_parity_sample(draws, steps)
+    gold = idx[np.argsort(-steps[idx], kind="stable")][:cases.IM_SCALE_GOLDEN]
+    _DADI = dadi
+    t = time.time()
+    with mp.get_context("fork").Pool(procs) as pool:
+        fs = pool.map(_im_extrap, [draws[i] for i in gold], chunksize=1)
+    print("im_scale: %d spectra in %.1fs" % (len(gold), time.time() - t), flush=True)
+    out["sample_idx"] = idx
+    out["sample_steps"] = steps[idx]
+    out["golden_idx"] = gold
+    out["golden_params"] = draws[gold]
+    out["golden_fs"] = np.stack(fs)
+
+
 def gen_grad(dadi, out):
     fim = dadi.Numerics.make_extrap_func(dadi.Demographics2D.IM)
     draws = cases.im_draws()
@@ -275,11 +311,21 @@ def gen_dfe(dadi, out):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--build", default="/tmp/dadi_ref")
+    ap.add_argument("--ref", required=True, help="the reference dadi source tree")
+    ap.add_argument("--build", default=os.path.join(tempfile.gettempdir(), "dadi_ref"),
+                    help="scratch directory for the reference build")
     ap.add_argument("--no-big", action="store_true", help="skip the 3-D model (~1 min)")
+    ap.add_argument("--only", choices=["im_scale"], default=None,
+                    help="write only this fixture")
+    ap.add_argument("--procs", type=int, default=os.cpu_count() or 1)
     a = ap.parse_args()
     dadi = load_dadi(a.ref, a.build)
+    if a.only == "im_scale":
+        out = {}
+        gen_im_scale(dadi, out, a.procs)
+        np.savez_compressed(os.path.join(HERE, "im_scale.npz"), **out)
+        print("wrote im_scale", len(out))
+        return
     for name, gen in [("integrate", gen_integrations), ("sweeps", gen_sweeps),
                       ("host", gen_host), ("grad", gen_grad), ("dfe", gen_dfe),
                       ("settings", gen_settings)]:

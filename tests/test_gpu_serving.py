@@ -2,9 +2,12 @@
 sample sizes, DFE-style IM with selection, 3-D growth, four populations,
 gradient requests) arriving over time is served with continuous batching;
 every result equals the same request served alone (bitwise: each request's
-work is the same kernels on the same data, only its neighbours differ) and
-matches the one-at-a-time model functions within the spectrum bar."""
+work is the same kernels on the same data, only its neighbours differ); the
+2-D results match the oracle (the reference's algorithm on the CPU) and the
+3-D / 4-D ones the one-at-a-time drop-in, within the spectrum bar."""
 import copy
+import multiprocessing as mp
+import os
 
 import numpy as np
 import pytest
@@ -20,6 +23,13 @@ def _obs():
     eng = batch.Batch2D((80, 90, 100), (40, 40))
     fs0, _, _ = eng.run(cases.im_draws(1))
     return np.random.default_rng(0).poisson(5e4 * fs0.cpu().numpy()[0]).astype(np.float64)
+
+
+def _oracle_fs(args):
+    kind, params, ns, pts_l = args
+    from oracle import numerics as onum
+    model = {"im": onum.IM, "im_sel": onum.IM_sel}[kind]
+    return np.asarray(onum.extrap_model(model, params, ns, list(pts_l)))
 
 
 def test_serving_mix_equals_alone_and_reference(cuda_lib):
@@ -41,12 +51,20 @@ def test_serving_mix_equals_alone_and_reference(cuda_lib):
         assert np.array_equal(alone.fs, by_id[r.rid].fs), r.kind
         if r.want_grad:
             assert np.array_equal(alone.grad, by_id[r.rid].grad)
-    # against the one-at-a-time model functions
-    fns = {"im": models.IM, "im_sel": models.IM_sel, "growth3": models.growth3,
-           "four": models.four_split}
-    for r in mix[:12]:
-        ref = numerics.make_extrap_func(fns[r.kind])(r.params, r.ns, list(r.pts_l))
-        assert_fs_parity(r.fs, np.asarray(ref.data))
+    # 2-D results against the oracle (a spawn pool: this process uses CUDA)
+    two = [r for r in mix[:12] if r.kind in ("im", "im_sel")]
+    assert len(two) == 12
+    with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
+        refs = pool.map(_oracle_fs, [(r.kind, r.params, r.ns, r.pts_l) for r in two],
+                        chunksize=1)
+    for r, ref in zip(two, refs):
+        assert_fs_parity(r.fs, ref)
+    # 3-D and 4-D results against the one-at-a-time drop-in
+    fns = {"growth3": models.growth3, "four": models.four_split}
+    for r in mix:
+        if r.kind in fns:
+            ref = numerics.make_extrap_func(fns[r.kind])(r.params, r.ns, list(r.pts_l))
+            assert_fs_parity(r.fs, np.asarray(ref.data))
 
 
 def test_serving_admits_by_footprint(cuda_lib):

@@ -164,3 +164,71 @@ def test_oracle_under_dadi_settings(golden, name, kw):
     finally:
         for k, v in saved.items():
             setattr(oint, k, v)
+
+
+# ---------------------------------------------- the batched workload at scale
+
+def _reference_loop_steps(p, tsf=1e-3):
+    """Steps of dadi's two_pops loop for Demographics2D.IM, walked in Python
+    with the reference's expressions (dadi/Integration.py:346-386,
+    dadi/Demographics2D.py:297-307)."""
+    s, nu1, nu2, T, m12, m21 = p
+    f1 = oint.ensure_1arg_func(lambda t: s * (nu1 / s) ** (t / T))
+    f2 = oint.ensure_1arg_func(lambda t: (1 - s) * (nu2 / (1 - s)) ** (t / T))
+    t, n = 0, 0
+    a, b = f1(t), f2(t)
+    dx = np.diff(onum.default_grid(10))
+    while t < T:
+        dt = min(oint.compute_dt(dx, a, [m12], 0, 0.5), oint.compute_dt(dx, b, [m21], 0, 0.5))
+        t = t + min(dt, T - t)
+        a, b = f1(t), f2(t)
+        n += 1
+    return n
+
+
+def test_im_step_counter_matches_reference_loop():
+    """The oracle's C walk of the IM schedule (used to pick and scale the CPU
+    sample and by the reference arm of the benchmark) counts exactly the
+    steps of the reference loop."""
+    draws = cases.im_draws()
+    steps = clib.im_steps(draws)
+    sel = [i for i in range(200) if steps[i] < 2500][:40]
+    for i in sel:
+        assert _reference_loop_steps(draws[i]) == steps[i]
+    assert steps.sum() == 10784487 and steps.max() == 19546
+
+
+def test_im_step_counter_matches_library_host_walk():
+    """... and the GPU package's host walk of the same schedules agrees on all
+    4096 draws (the batched engine's device walk is tested against it on the
+    GPU)."""
+    from dadi_gb300 import batch
+    draws = cases.im_draws()
+    assert np.array_equal(clib.im_steps(draws), batch.count_steps(batch.im_instances(draws)))
+
+
+def test_parity_sample_is_stratified(golden):
+    import os
+    g = np.load(os.path.join(os.path.dirname(cases.__file__), "im_scale.npz"))
+    draws = cases.im_draws()
+    steps = clib.im_steps(draws)
+    idx = cases.im_parity_sample(draws, steps)
+    assert np.array_equal(idx, g["sample_idx"])
+    assert np.array_equal(steps[idx], g["sample_steps"])
+    assert len(idx) == 64 and 4 in idx and steps[idx].max() == 19546
+    for col in range(6):
+        assert int(np.argmin(draws[:, col])) in idx and int(np.argmax(draws[:, col])) in idx
+    # the goldens are the 16 longest schedules of the sample
+    order = idx[np.argsort(-steps[idx], kind="stable")]
+    assert np.array_equal(g["golden_idx"], order[:cases.IM_SCALE_GOLDEN])
+    assert np.array_equal(g["golden_params"], draws[g["golden_idx"]])
+
+
+def test_oracle_matches_dadi_at_scale():
+    """The oracle equals dadi bit for bit on the cheapest at-scale golden
+    spectrum (pts [80,90,100], ns (40,40), 3285 steps)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(cases.__file__), "im_scale.npz"))
+    k = len(g["golden_idx"]) - 1
+    fs = onum.extrap_model(onum.IM, g["golden_params"][k], (40, 40), [80, 90, 100])
+    assert np.array_equal(fs, g["golden_fs"][k])
