@@ -33,7 +33,9 @@ EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
            "dgb_batch2d_integrate_ckpt", "dgb_adjoint2d_scratch_bytes", "dgb_adjoint2d",
            "dgb_items2d_integrate", "dgb_sched2d_host", "dgb_from_phi2d_smem_bytes",
            "dgb_from_phi2d", "dgb_extrap_ll", "dgb_integrate_table_states",
-           "dgb_adjoint_table_nd_gpart_doubles", "dgb_adjoint_table_nd"]
+           "dgb_adjoint_table_nd_gpart_doubles", "dgb_adjoint_table_nd",
+           "dgb_batchnd_workspace_bytes", "dgb_batchnd_integrate", "dgb_schednd_host",
+           "dgb_from_phi_nd_workspace_bytes", "dgb_from_phi_nd"]
 
 
 class PForm(ctypes.Structure):
@@ -46,6 +48,18 @@ class Inst2D(ctypes.Structure):
                 ("nu", PForm * 2), ("m12", PForm), ("m21", PForm), ("gamma", PForm * 2),
                 ("h", PForm * 2), ("theta0", PForm),
                 ("frozen_mask", ctypes.c_int), ("nomut_mask", ctypes.c_int)]
+
+
+class InstND(ctypes.Structure):
+    _fields_ = [("T", ctypes.c_double), ("initial_t", ctypes.c_double),
+                ("nu", PForm * 5), ("gamma", PForm * 5), ("h", PForm * 5),
+                ("mig", (PForm * 5) * 5), ("theta0", PForm),
+                ("ndim", ctypes.c_int), ("pad_", ctypes.c_int)]
+
+
+class ItemND(ctypes.Structure):
+    _fields_ = [("phi_off", ctypes.c_long), ("row_off", ctypes.c_long),
+                ("nsteps", ctypes.c_int), ("masks", ctypes.c_int)]
 
 
 class Settings(ctypes.Structure):
@@ -102,6 +116,12 @@ def _declare(L):
         "dgb_integrate_table_states": (i, [_vp, i, i, _vp, _vp, i, i, i, _vp, _vp, sz, _vp]),
         "dgb_adjoint_table_nd_gpart_doubles": (sz, [i, i]),
         "dgb_adjoint_table_nd": (i, [_vp, i, i, _vp, _vp, i, i, i, _vp, _vp, _vp, sz, _vp]),
+        "dgb_batchnd_workspace_bytes": (sz, [i, i, i, ctypes.POINTER(Settings)]),
+        "dgb_batchnd_integrate": (i, [_vp, _vp, i, i, i, _vp, _vp, _vp,
+                                      ctypes.POINTER(Settings), _vp, sz, _vp]),
+        "dgb_schednd_host": (i, [_vp, i, ctypes.POINTER(Settings), lg, d, _vp, _vp, _vp, _vp]),
+        "dgb_from_phi_nd_workspace_bytes": (sz, [i, i, _vp, i]),
+        "dgb_from_phi_nd": (i, [_vp, i, i, i, _vp, _vp, _vp, _vp, _vp, _vp, sz, _vp]),
         "dgb_adjoint2d": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp, _vp,
                               _vp, _vp, i, _vp, _vp, _vp, ctypes.POINTER(Settings), _vp, sz,
                               _vp]),

@@ -1,0 +1,427 @@
+// Batched N-dimensional engine: many integrations of the same number of
+// populations on the same grid advance together, so that a 3-D or 4-D sweep
+// launch carries the lines of every integration instead of one (a single
+// 3-D grid of 70-90 points has 4,900-8,100 lines: 150-250 warps, a quarter
+// of the warps the FP64 pipe of 152 SMs needs).
+//
+// Per chunk of steps one launch writes the coefficient records of every
+// (integration, step, swept axis) -- the grid constants, the parameter row,
+// the per-axis vectors, as k_coef_nd does for one integration -- and then
+// per step and axis one launch sweeps the lines of every integration still
+// running (integrations are ordered longest first, so the running ones are a
+// prefix).  Each CTA stages its lines in shared memory as k_sweep_nd_rec
+// does; the Thomas gam scratch sits in shared memory or in a per-CTA slice
+// of the workspace (L2), which leaves room for twice the CTAs per SM.
+// Per line the arithmetic is that of k_sweep_nd_rec, so every integration's
+// density is bitwise the one dgb_integrate_table computes alone.
+//
+// Replaces many calls of Integration.three_pops / four_pops / five_pops
+// (dadi/Integration.py:389-554, 556-727, 729-937), which the reference runs
+// one at a time, or as host processes (dadi/DFE/Cache2D_mod.py:117-167).
+#include <algorithm>
+#include <cmath>
+
+#include "dgb_nd.cuh"
+
+namespace dgb {
+
+struct NDBatch {
+    NDArgs A; // shared shape: ndim, L, axis, nlines, S, LS, xx
+    const dgb_itemnd *items;
+    double *phi_all;
+    const double *table;
+    double *coef;      // grid constants, then one block of records per integration
+    long item_coef;    // doubles of one integration's block (chunk x ndim records)
+    long step0;        // first step of the current chunk
+    int chunk;         // steps per chunk
+    int bpi;           // CTAs per integration in a sweep launch
+    double *gam_glob;  // per-CTA gam slices (null: shared memory)
+};
+
+__device__ __forceinline__ int first_swept(int frozen)
+{
+    int f = 0;
+    while (f < DGB_MAX_DIM && (frozen >> f & 1))
+        f++;
+    return f;
+}
+
+// One CTA per (integration, step of the chunk, axis): the record of
+// k_coef_nd for that integration's table row.
+template <bool DELJ>
+__global__ void k_coef_batch(NDBatch B, int nsl)
+{
+    extern __shared__ __align__(16) double smem[];
+    __shared__ NDShared Sh;
+    const int P = B.A.ndim, L = B.A.L;
+    const long b = blockIdx.x;
+    const int ax = (int)(b % P);
+    const long sl = (b / P) % nsl;
+    const long it = b / ((long)P * nsl);
+    const dgb_itemnd I = B.items[it];
+    const int frozen = I.masks & 0xff, nomut = (I.masks >> 8) & 0xff;
+    GridVecs g;
+    g.x = smem;
+    g.xv = smem + L;
+    g.dfac = smem + 2 * L;
+    g.xInt = smem + 3 * L;
+    g.ih = smem + 4 * L;
+    g.dx = smem + 5 * L;
+    NDArgs A = B.A;
+    A.axis = ax;
+    A.table = B.table + I.row_off * row_stride(P);
+    A.step = B.step0 + sl;
+    A.inject_mask = (ax == first_swept(frozen)) ? (((1 << P) - 1) & ~frozen & ~nomut) : 0;
+    nd_grid_consts(A, g);
+    if (b == 0)
+        for (int i = threadIdx.x; i < nd_grid_doubles(L); i += blockDim.x)
+            B.coef[i] = smem[i];
+    if (A.step >= I.nsteps || (frozen >> ax & 1))
+        return; // the whole CTA: no barrier is skipped by part of it
+    if (threadIdx.x == 0)
+        nd_load_params(A, Sh, g);
+    __syncthreads();
+    double *rec = B.coef + nd_grid_doubles(L) + it * B.item_coef +
+                  ((size_t)sl * P + ax) * nd_rec_doubles(L, DELJ);
+    AxisVecs v;
+    nd_vecs_at(rec + ND_HEAD, L, DELJ, v);
+    for (int i = threadIdx.x; i < L; i += blockDim.x)
+        build_axis_entry(i, L, g, Sh.s, Sh.vscale, DELJ, v);
+    if (threadIdx.x == 0) {
+        NDRecHead h;
+        h.s = Sh.s;
+        for (int k = 0; k < DGB_MAX_DIM; k++)
+            h.inj[k] = Sh.inj[k];
+        const double *hp = reinterpret_cast<const double *>(&h);
+        for (int k = 0; k < ND_HEAD; k++)
+            rec[k] = hp[k];
+    }
+}
+
+// One sweep along B.A.axis at `step` over the lines of every running
+// integration: CTA b handles tile b % bpi of integration b / bpi.
+template <bool DELJ, bool GSMEM>
+__global__ void k_sweep_batch(NDBatch B, long step)
+{
+    extern __shared__ __align__(16) double smem[];
+    __shared__ NDRecHead H;
+    const int nt = blockDim.x, L = B.A.L, P = B.A.ndim;
+    constexpr int NV = DELJ ? 10 : 5;
+    const long it = blockIdx.x / B.bpi;
+    const long tl = blockIdx.x - it * B.bpi;
+    const dgb_itemnd I = B.items[it];
+    const int frozen = I.masks & 0xff, nomut = (I.masks >> 8) & 0xff;
+    if (step >= I.nsteps || (frozen >> B.A.axis & 1))
+        return;
+    NDArgs A = B.A;
+    A.phi = B.phi_all + I.phi_off;
+    A.inject_mask =
+        (A.axis == first_swept(frozen)) ? (((1 << P) - 1) & ~frozen & ~nomut) : 0;
+    double *tile = smem;
+    double *gam, *gx;
+    if (GSMEM) {
+        gam = tile + (size_t)L * (nt + 1);
+        gx = gam + (size_t)L * nt;
+    } else {
+        gam = B.gam_glob + (size_t)blockIdx.x * L * nt;
+        gx = tile + (size_t)L * (nt + 1);
+    }
+    double *vv = gx + 3 * (size_t)L;
+    const double *rec = B.coef + nd_grid_doubles(L) + it * B.item_coef +
+                        ((size_t)(step - B.step0) * P + A.axis) * nd_rec_doubles(L, DELJ);
+    double *hp = reinterpret_cast<double *>(&H);
+    for (int i = threadIdx.x; i < ND_HEAD; i += nt)
+        hp[i] = rec[i];
+    for (int i = threadIdx.x; i < NV * L; i += nt)
+        vv[i] = rec[ND_HEAD + i];
+    for (int i = threadIdx.x; i < L; i += nt) {
+        gx[i] = B.coef[i];
+        if (DELJ) {
+            gx[L + i] = B.coef[3 * L + i];
+            gx[2 * L + i] = B.coef[5 * L + i];
+        }
+    }
+    GridVecs g = {};
+    g.x = gx;
+    g.xInt = gx + L;
+    g.dx = gx + 2 * L;
+    AxisVecs v;
+    nd_vecs_at(vv, L, DELJ, v);
+    const long l0 = tl * nt;
+    const int n = (int)min((long)nt, A.nlines - l0);
+    nd_tile_io(A, tile, nt, l0, n, false);
+    __syncthreads();
+    nd_solve_tile<DELJ>(A, tile, gam, nt, l0, n, g, v, H.s, H.inj);
+    __syncthreads();
+    nd_tile_io(A, tile, nt, l0, n, true);
+}
+
+// ------------------------------------------------------------ host side
+
+struct BatchPlan {
+    int nt;        // lines per CTA
+    int gsmem;     // gam in shared memory
+    int chunk;     // steps per record chunk
+    int bpi;       // CTAs per integration
+    size_t smem;   // dynamic shared memory of a sweep CTA
+    size_t coef_doubles;
+    size_t gam_doubles;
+};
+
+static size_t batch_sweep_smem(int L, int nt, bool delj, bool gsmem)
+{
+    return ((size_t)L * (nt + 1) + (gsmem ? (size_t)L * nt : 0) + 3 * (size_t)L +
+            (size_t)(delj ? 10 : 5) * L) *
+           sizeof(double);
+}
+
+// Records of at most ~64 MB per chunk, 1..64 steps.
+static int batch_chunk(int ndim, int L, int nitems)
+{
+    const size_t per = (size_t)nitems * ndim * nd_rec_doubles(L, true) * sizeof(double);
+    size_t c = ((size_t)64 << 20) / std::max<size_t>(per, 1);
+    return (int)std::max<size_t>(1, std::min<size_t>(64, c));
+}
+
+static int batch_plan(int ndim, int L, int nitems, const dgb_settings *st, BatchPlan &p)
+{
+    const long nlines = ipow(L, ndim - 1);
+    int nt = st ? st->threads : 0;
+    if (nt != 32 && nt != 64 && nt != 128)
+        nt = (L <= 48) ? 128 : 64;
+    if (nlines < nt)
+        nt = (int)std::max<long>(32, (nlines + 31) / 32 * 32);
+    const bool delj = st && st->use_delj_trick;
+    int gp = st ? st->gam_placement : 0;
+    int optin = 0, dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        return DGB_ERR_CUDA;
+    const size_t need_s = batch_sweep_smem(L, nt, delj, true) + sizeof(NDRecHead) + 1024;
+    const size_t need_g = batch_sweep_smem(L, nt, delj, false) + sizeof(NDRecHead) + 1024;
+    if (need_g > (size_t)optin)
+        return DGB_ERR_UNSUPPORTED;
+    if (gp == 1 && need_s > (size_t)optin)
+        return DGB_ERR_UNSUPPORTED;
+    p.gsmem = (gp == 1) ? 1 : 0; // auto: the workspace (twice the CTAs per SM)
+    p.nt = nt;
+    p.bpi = (int)((nlines + nt - 1) / nt);
+    p.chunk = batch_chunk(ndim, L, nitems);
+    p.smem = batch_sweep_smem(L, nt, delj, p.gsmem);
+    p.coef_doubles = (size_t)nd_grid_doubles(L) +
+                     (size_t)nitems * p.chunk * ndim * nd_rec_doubles(L, delj);
+    p.gam_doubles = p.gsmem ? 0 : (size_t)nitems * p.bpi * nt * L;
+    return DGB_OK;
+}
+
+template <bool DELJ, bool GSMEM>
+static int batch_sweep_launch(NDBatch &B, long nact, size_t smem, int nt, long step,
+                              cudaStream_t st)
+{
+    if (raise_smem_limit(k_sweep_batch<DELJ, GSMEM>))
+        return DGB_ERR_CUDA;
+    k_sweep_batch<DELJ, GSMEM><<<(unsigned)(nact * B.bpi), nt, smem, st>>>(B, step);
+    return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
+}
+
+} // namespace dgb
+
+using namespace dgb;
+
+extern "C" size_t dgb_batchnd_workspace_bytes(int ndim, int L, int nitems,
+                                              const dgb_settings *settings)
+{
+    if (!shape_ok(ndim, L) || nitems < 1)
+        return 0;
+    BatchPlan p;
+    if (batch_plan(ndim, L, nitems, settings, p))
+        return 0;
+    return (p.coef_doubles + p.gam_doubles) * sizeof(double) + 256;
+}
+
+extern "C" int dgb_batchnd_integrate(const dgb_itemnd *items, const int *nsteps, int nitems,
+                                     int ndim, int L, const double *xx, double *phi_all,
+                                     const double *table, const dgb_settings *settings,
+                                     void *ws, size_t ws_bytes, void *stream)
+{
+    if (!items || !nsteps || nitems < 1 || !xx || !phi_all || !table || !settings ||
+        !shape_ok(ndim, L))
+        return DGB_ERR_ARG;
+    for (int i = 0; i < nitems; i++)
+        if (nsteps[i] < 0 || (i > 0 && nsteps[i] > nsteps[i - 1]))
+            return DGB_ERR_ARG; // longest first
+    if (nsteps[0] == 0)
+        return DGB_OK;
+    BatchPlan p;
+    int rc = batch_plan(ndim, L, nitems, settings, p);
+    if (rc)
+        return rc;
+    if (!ws || ws_bytes < (p.coef_doubles + p.gam_doubles) * sizeof(double))
+        return DGB_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool delj = settings->use_delj_trick != 0;
+    NDBatch B = {};
+    nd_fill(B.A, phi_all, ndim, L, 0, xx);
+    B.items = items;
+    B.phi_all = phi_all;
+    B.table = table;
+    B.coef = (double *)ws;
+    B.chunk = p.chunk;
+    B.item_coef = (long)p.chunk * ndim * (long)nd_rec_doubles(L, delj);
+    B.bpi = p.bpi;
+    B.gam_glob = p.gsmem ? nullptr : (double *)ws + p.coef_doubles;
+    const size_t csmem = (size_t)nd_grid_doubles(L) * sizeof(double);
+    if (delj ? raise_smem_limit(k_coef_batch<true>) : raise_smem_limit(k_coef_batch<false>))
+        return DGB_ERR_CUDA;
+    long nact = nitems;
+    const long total = nsteps[0];
+    for (long s = 0; s < total; s++) {
+        while (nact > 0 && nsteps[nact - 1] <= s)
+            nact--;
+        if (s % p.chunk == 0) {
+            B.step0 = s;
+            const int nsl = (int)std::min<long>(p.chunk, total - s);
+            const unsigned grid = (unsigned)(nact * nsl * ndim);
+            if (delj)
+                k_coef_batch<true><<<grid, 128, csmem, st>>>(B, nsl);
+            else
+                k_coef_batch<false><<<grid, 128, csmem, st>>>(B, nsl);
+            if (cudaGetLastError() != cudaSuccess)
+                return DGB_ERR_CUDA;
+        }
+        for (int ax = 0; ax < ndim; ax++) {
+            B.A.axis = ax;
+            B.A.S = ipow(L, ndim - 1 - ax);
+            B.A.LS = B.A.S * L;
+            if (delj)
+                rc = p.gsmem ? batch_sweep_launch<true, true>(B, nact, p.smem, p.nt, s, st)
+                             : batch_sweep_launch<true, false>(B, nact, p.smem, p.nt, s, st);
+            else
+                rc = p.gsmem ? batch_sweep_launch<false, true>(B, nact, p.smem, p.nt, s, st)
+                             : batch_sweep_launch<false, false>(B, nact, p.smem, p.nt, s, st);
+            if (rc)
+                return rc;
+        }
+    }
+    return DGB_OK;
+}
+
+// ------------------------------------------- parametric schedules (host)
+
+// Value of a parametric form at t (dgb_pform; the same evaluation as the
+// device's pform_eval).
+static double pf_host(const dgb_pform &f, double t) { return pform_eval(f, t); }
+
+// The table rows of one parametric P-population integration: the loop of
+// Integration.three_pops / four_pops / five_pops (dadi/Integration.py:
+// 504-553, 672-726, 884-935): dt from the current parameters (the minimum
+// over populations of _compute_dt, :147-176, with each population's
+// migration rates into it summed in increasing order), the parameters at
+// the next time, the reference's validation.  rows == null counts; rows
+// are written while fewer than `room` have been.
+static long schednd_walk(const dgb_instnd &I, const dgb_settings &st, double dx0,
+                         long max_steps, double *rows, long room, int *status)
+{
+    const int P = I.ndim;
+    double nu[DGB_MAX_DIM], g[DGB_MAX_DIM], h[DGB_MAX_DIM], m[DGB_MAX_DIM][DGB_MAX_DIM];
+    auto eval = [&](double t) {
+        for (int k = 0; k < P; k++) {
+            nu[k] = pf_host(I.nu[k], t);
+            g[k] = pf_host(I.gamma[k], t);
+            h[k] = pf_host(I.h[k], t);
+            for (int j = 0; j < P; j++)
+                m[k][j] = (j == k) ? 0.0 : pf_host(I.mig[k][j], t);
+        }
+    };
+    double cur = I.initial_t;
+    eval(cur);
+    long n = 0;
+    int err = 0;
+    const int stride = row_stride(P);
+    while (cur < I.T) {
+        if (n >= max_steps) {
+            err |= DGB_ST_STEPCAP;
+            break;
+        }
+        double dtm = 0;
+        for (int k = 0; k < P; k++) {
+            double msum = 0;
+            for (int j = 0; j < P; j++)
+                if (j != k)
+                    msum = msum + m[k][j];
+            double d = compute_dt(nu[k], (P == 1) ? 0.0 : msum, g[k], h[k], st, dx0);
+            dtm = (k == 0) ? d : pymin(dtm, d);
+        }
+        if (dtm == 0) {
+            err |= DGB_ST_ZERODT;
+            break;
+        }
+        double dt = pymin(dtm, I.T - cur);
+        double next = cur + dt;
+        if (!(dt > 0) || !std::isfinite(next)) {
+            err |= DGB_ST_NONFINITE;
+            break;
+        }
+        eval(next);
+        double theta0 = pf_host(I.theta0, next);
+        bool bad = I.T < 0 || theta0 < 0;
+        for (int k = 0; k < P; k++) {
+            bad = bad || nu[k] < 0 || nu[k] == 0;
+            for (int j = 0; j < P; j++)
+                bad = bad || (j != k && m[k][j] < 0);
+        }
+        if (bad) {
+            err |= DGB_ST_BADPARAM;
+            break;
+        }
+        if (rows && n >= room) {
+            err |= DGB_ST_STEPCAP;
+            break;
+        }
+        if (rows) {
+            double *r = rows + n * stride;
+            r[0] = dt;
+            r[1] = theta0;
+            for (int k = 0; k < P; k++) {
+                r[row_nu(P, k)] = nu[k];
+                r[row_gamma(P, k)] = g[k];
+                r[row_h(P, k)] = h[k];
+                for (int j = 0; j < P; j++)
+                    if (j != k)
+                        r[row_mig(P, k, j)] = m[k][j];
+            }
+            r[row_beta(P)] = 1.0;
+        }
+        n++;
+        cur = next;
+    }
+    if (status)
+        *status |= err;
+    return n;
+}
+
+extern "C" int dgb_schednd_host(const dgb_instnd *insts, int ninst,
+                                const dgb_settings *settings, long max_steps, double dx0,
+                                int *row_cnt, const long *row_off, double *table, int *status)
+{
+    if (!insts || ninst < 0 || !settings || !row_cnt || max_steps < 1 || (table && !row_off))
+        return DGB_ERR_ARG;
+    for (int i = 0; i < ninst; i++)
+        if (insts[i].ndim < 1 || insts[i].ndim > DGB_MAX_DIM)
+            return DGB_ERR_ARG;
+    for (int i = 0; i < ninst; i++) {
+        const dgb_instnd &I = insts[i];
+        const int P = I.ndim;
+        if (!table) {
+            row_cnt[i] = (int)schednd_walk(I, *settings, dx0, max_steps, nullptr, 0, nullptr);
+        } else {
+            int err = 0;
+            long n = schednd_walk(I, *settings, dx0, max_steps,
+                                  table + row_off[i] * row_stride(P), row_cnt[i], &err);
+            row_cnt[i] = (int)n;
+            if (status)
+                status[i] |= err;
+        }
+    }
+    return DGB_OK;
+}

@@ -217,9 +217,170 @@ __global__ void __launch_bounds__(FS_THREADS) k_extrap_ll(const dgb_extrap_item 
         *it.ll_multinom = tot2;
 }
 
+
+// ---------------------------------------------- from_phi, any dimension
+
+// One contraction of Spectrum.from_phi's linear-algebra form
+// (dadi/Spectrum_mod.py:1509-1547, 1774-1810, 1841-1870): every row of L
+// values along the last axis of the current tensor (M rows, row m at m*L) is
+// integrated against the binomial sampling weights of n samples,
+//   out[k][m] = sum_j d1[k][j] c1[m][j] + (k+1)/((n+1)(n+2)) sum_j d2[k][j] s[m][j],
+//   s = (p[j+1] - p[j]) / (x[j+1] - x[j]),  c1 = (p[j] - s x[j]) / (n+1),
+// and the new axis of n+1 entries comes first: out is (n+1) x M.  Applied
+// once per axis, last axis first, this rotates the axes back into order and
+// gives the spectrum (the reference's 3-D/4-D code contracts the last axis
+// first as well).  A CTA takes CT_ROWS rows of one density: a coalesced copy
+// into shared memory ([j][r], odd pitch), the slopes and intercepts in
+// place, then each of its CT_KG warps accumulates every CT_KG-th output entry
+// for its 32 rows from the weight tables (warp-uniform reads), KC entries at
+// a time in registers.
+constexpr int CT_ROWS = 32;
+constexpr int CT_KG = 4;
+constexpr int CT_KC = 6;
+
+__host__ __device__ inline size_t ct_smem_doubles(int L)
+{
+    return 2 * (size_t)L + 2 * (size_t)L * (CT_ROWS + 1);
+}
+
+__global__ void __launch_bounds__(CT_ROWS *CT_KG)
+    k_contract_last(const double *in, long in_bs, double *out, long out_bs, long M, int L, int n,
+                    const double *xx, const double *d1, const double *d2)
+{
+    extern __shared__ __align__(16) double sm[];
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int r = tid % CT_ROWS, g = tid / CT_ROWS;
+    const long m0 = (long)blockIdx.x * CT_ROWS;
+    const int nr = (int)min((long)CT_ROWS, M - m0);
+    const double *src = in + (long)blockIdx.y * in_bs + m0 * L;
+    double *dst = out + (long)blockIdx.y * out_bs;
+    constexpr int PT = CT_ROWS + 1;
+    double *x = sm, *dx = sm + L;
+    double *P = dx + L;                 // phi, then the intercepts c1: [j][r]
+    double *S = P + (size_t)L * PT;     // slopes: [j][r]
+    for (int i = tid; i < L; i += nth)
+        x[i] = xx[i];
+    for (int e = tid; e < nr * L; e += nth) {
+        const int rr = e / L, j = e - rr * L;
+        P[j * PT + rr] = src[e];
+    }
+    __syncthreads();
+    for (int j = tid; j < L - 1; j += nth)
+        dx[j] = x[j + 1] - x[j];
+    __syncthreads();
+    const double inv_n = 1.0 / (n + 1);
+    for (int e = tid; e < (L - 1) * CT_ROWS; e += nth) {
+        const int j = e / CT_ROWS, rr = e - j * CT_ROWS;
+        S[j * PT + rr] = (P[(j + 1) * PT + rr] - P[j * PT + rr]) / dx[j];
+    }
+    __syncthreads();
+    for (int e = tid; e < (L - 1) * CT_ROWS; e += nth) {
+        const int j = e / CT_ROWS, rr = e - j * CT_ROWS;
+        P[j * PT + rr] = (P[j * PT + rr] - S[j * PT + rr] * x[j]) * inv_n;
+    }
+    __syncthreads();
+    const int Mj = L - 1;
+    for (int k0 = g; k0 <= n; k0 += CT_KG * CT_KC) {
+        double a1[CT_KC], a2[CT_KC];
+#pragma unroll
+        for (int q = 0; q < CT_KC; q++)
+            a1[q] = a2[q] = 0;
+        for (int j = 0; j < Mj; j++) {
+            const double c = P[j * PT + r], sv = S[j * PT + r];
+#pragma unroll
+            for (int q = 0; q < CT_KC; q++) {
+                const int k = k0 + q * CT_KG;
+                if (k <= n) {
+                    a1[q] = fma(d1[(size_t)k * Mj + j], c, a1[q]);
+                    a2[q] = fma(d2[(size_t)k * Mj + j], sv, a2[q]);
+                }
+            }
+        }
+        if (r < nr) {
+#pragma unroll
+            for (int q = 0; q < CT_KC; q++) {
+                const int k = k0 + q * CT_KG;
+                if (k <= n) {
+                    const double w = (double)(k + 1) / ((double)(n + 1) * (n + 2));
+                    dst[(long)k * M + m0 + r] = a1[q] + a2[q] * w;
+                }
+            }
+        }
+    }
+}
+
+// Sizes (doubles per density) of the tensors between contractions: after
+// contracting axes ndim-1 .. ndim-t the tensor has
+// prod_{a >= ndim-t} (ns[a]+1) x L^(ndim-t) entries.
+static long ct_size_after(int ndim, int L, const int *ns, int t)
+{
+    long s = 1;
+    for (int a = ndim - t; a < ndim; a++)
+        s *= ns[a] + 1;
+    for (int a = 0; a < ndim - t; a++)
+        s *= L;
+    return s;
+}
+
 } // namespace dgb
 
 using namespace dgb;
+
+extern "C" size_t dgb_from_phi_nd_workspace_bytes(int ndim, int L, const int *ns, int nbatch)
+{
+    if (ndim < 1 || ndim > DGB_MAX_DIM || L < 2 || !ns || nbatch < 1)
+        return 0;
+    long mx = 0;
+    for (int t = 1; t < ndim; t++)
+        mx = std::max(mx, ct_size_after(ndim, L, ns, t));
+    return (size_t)(2 * mx * (long)nbatch + 1) * sizeof(double);
+}
+
+extern "C" int dgb_from_phi_nd(const double *phi, int nbatch, int ndim, int L, const double *xx,
+                               const int *ns, const double *const *d1, const double *const *d2,
+                               double *out, void *ws, size_t ws_bytes, void *stream)
+{
+    if (!phi || nbatch < 0 || ndim < 1 || ndim > DGB_MAX_DIM || L < 2 || !xx || !ns || !d1 ||
+        !d2 || !out)
+        return DGB_ERR_ARG;
+    for (int a = 0; a < ndim; a++)
+        if (ns[a] < 1 || !d1[a] || !d2[a])
+            return DGB_ERR_ARG;
+    if (nbatch == 0)
+        return DGB_OK;
+    const size_t smem = ct_smem_doubles(L) * sizeof(double);
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+            cudaSuccess)
+        return DGB_ERR_CUDA;
+    if (smem > (size_t)optin)
+        return DGB_ERR_UNSUPPORTED;
+    if (ndim > 1 && (!ws || ws_bytes < dgb_from_phi_nd_workspace_bytes(ndim, L, ns, nbatch)))
+        return DGB_ERR_WORKSPACE;
+    if (raise_smem_limit(k_contract_last))
+        return DGB_ERR_CUDA;
+    long mx = 0;
+    for (int t = 1; t < ndim; t++)
+        mx = std::max(mx, ct_size_after(ndim, L, ns, t));
+    double *buf[2] = {(double *)ws, (double *)ws + mx * (long)nbatch};
+    const double *cur = phi;
+    long cur_bs = ct_size_after(ndim, L, ns, 0);
+    for (int t = 1; t <= ndim; t++) {
+        const int a = ndim - t; // the axis contracted now
+        const long M = ct_size_after(ndim, L, ns, t - 1) / L;
+        const long nxt_bs = ct_size_after(ndim, L, ns, t);
+        double *dst = (t == ndim) ? out : buf[t % 2];
+        dim3 grid((unsigned)((M + CT_ROWS - 1) / CT_ROWS), (unsigned)nbatch);
+        k_contract_last<<<grid, CT_ROWS * CT_KG, smem, (cudaStream_t)stream>>>(
+            cur, cur_bs, dst, nxt_bs, M, L, ns[a], xx, d1[a], d2[a]);
+        if (cudaGetLastError() != cudaSuccess)
+            return DGB_ERR_CUDA;
+        cur = dst;
+        cur_bs = nxt_bs;
+    }
+    return DGB_OK;
+}
 
 extern "C" size_t dgb_from_phi2d_smem_bytes(int Lmax, int nmax)
 {

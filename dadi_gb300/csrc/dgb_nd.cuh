@@ -242,6 +242,63 @@ __device__ __forceinline__ void nd_tile_io(const NDArgs &A, double *tile, int nt
     }
 }
 
+// Solve the CTA's tile of lines [l0, l0+n) in shared memory: per line the
+// migration weight W and the corner flags from its other coordinates, the
+// fused mutation injection (dadi/Integration.py:70-122) when this is the
+// step's first sweep, then the Thomas solve.
+template <bool DELJ>
+__device__ __forceinline__ void nd_solve_tile(const NDArgs &A, double *tile, double *gam, int nt,
+                                              long l0, int n, const GridVecs &g,
+                                              const AxisVecs &v, const AxisScalars &s,
+                                              const double *inj)
+{
+    const int L = A.L, P = A.ndim, ax = A.axis;
+    // grid index of the corner coordinates (value exactly 0 / 1)
+    const int j0 = (g.x[0] == 0.0) ? 0 : -1;
+    const int j1 = (g.x[L - 1] == 1.0) ? L - 1 : -1;
+    const int t = threadIdx.x;
+    if (t >= n)
+        return;
+    int coord[DGB_MAX_DIM];
+    nd_line_base(A, l0 + t, coord);
+    double W = 0;
+    double mo[DGB_MAX_DIM], oo[DGB_MAX_DIM];
+    int no = 0;
+    bool all0 = true, all1 = true;
+    int n1 = 0, k1 = -1;
+    for (int k = 0; k < P; k++) {
+        if (k == ax)
+            continue;
+        W = fma(s.mig[k], g.x[coord[k]], W);
+        mo[no] = s.mig[k];
+        oo[no] = g.x[coord[k]];
+        no++;
+        all0 = all0 && coord[k] == j0;
+        all1 = all1 && coord[k] == j1;
+        if (coord[k] == 1) {
+            n1++;
+            k1 = k;
+        } else if (coord[k] != 0) {
+            n1 = 99;
+        }
+    }
+    if (P == 1)
+        all0 = all1 = true; // 1-D applies both boundary terms unconditionally
+    const int tp = nt + 1;
+    if (A.inject_mask) {
+        if (n1 == 0 && inj[ax] != 0.0)
+            tile[1 * tp + t] += inj[ax];
+        if (n1 == 1 && inj[k1] != 0.0)
+            tile[0 * tp + t] += inj[k1];
+    }
+    double bs = all0 ? s.bcs : 0.0;
+    double be = all1 ? s.bce : 0.0;
+    if (DELJ)
+        solve_line_delj(tile + t, tp, gam + t, nt, L, mo, oo, no, bs, be, g, v);
+    else
+        solve_line(tile + t, tp, gam + t, nt, L, W, bs, be, v, s);
+}
+
 // ------------------------------------------------------------ host side
 
 static long ipow(int L, int p)

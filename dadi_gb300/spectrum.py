@@ -134,34 +134,66 @@ def _from_phi_5D(nx, ny, nz, na, nb, xx, yy, zz, aa, bb, phi):
     return data
 
 
+def from_phi_nd_batch(torch, phi_b, ns, xx):
+    """Raw spectra of a batch of densities phi_b (B, L, ..., L) of 1-5
+    populations resident on the GPU, all axes on grid xx: the hand-written
+    contraction kernel (dgb_from_phi_nd), one launch per axis.  Returns a
+    (B, n1+1, ..., nP+1) float64 CUDA tensor."""
+    import ctypes
+    from . import _lib
+    lib = _lib.lib()
+    B, P = phi_b.shape[0], phi_b.dim() - 1
+    L = phi_b.shape[1]
+    if any(s != L for s in phi_b.shape[1:]) or len(xx) != L or len(ns) != P:
+        raise ValueError("phi_b must be (B, L, ..., L) with len(xx) == L and len(ns) axes")
+    phi_b = phi_b.to(torch.float64).contiguous()
+    dev = phi_b.device
+    tabs = [_device_tables(torch, int(n), xx, dev) for n in ns]
+    x = tabs[0][2]
+    out = torch.empty((B,) + tuple(int(n) + 1 for n in ns), dtype=torch.float64, device=dev)
+    if B == 0:
+        return out
+    ns_c = (ctypes.c_int * P)(*[int(n) for n in ns])
+    d1 = (ctypes.c_void_p * P)(*[t[0].data_ptr() for t in tabs])
+    d2 = (ctypes.c_void_p * P)(*[t[1].data_ptr() for t in tabs])
+    nws = lib.dgb_from_phi_nd_workspace_bytes(P, L, ctypes.cast(ns_c, ctypes.c_void_p), B)
+    ws, nws = _lib.workspace(torch, nws)
+    _lib.check(lib.dgb_from_phi_nd(_lib.dptr(phi_b), B, P, L, _lib.dptr(x),
+                                   ctypes.cast(ns_c, ctypes.c_void_p),
+                                   ctypes.cast(d1, ctypes.c_void_p),
+                                   ctypes.cast(d2, ctypes.c_void_p), _lib.dptr(out),
+                                   _lib.dptr(ws), nws, _lib.stream_handle(torch)),
+               "dgb_from_phi_nd")
+    return out
+
+
 def _from_phi_device(phi, ns, xxs):
-    """Raw spectrum of a CUDA-tensor density: two populations on one grid
-    through the device epilogue, three through the batched torch contraction;
-    the spectrum (not the density) comes back to the host."""
+    """Raw spectrum of a CUDA-tensor density on one grid for every axis:
+    two populations through the device epilogue, three to five through the
+    contraction kernel; the spectrum (not the density) comes back to the
+    host."""
     import torch
     from . import _lib
     P = phi.dim()
     same = all(np.array_equal(xxs[0], x) for x in xxs[1:])
-    if P == 2 and same:
+    if not same:
+        return None
+    if P == 2:
         from . import epilogue
         fs, _, _ = epilogue.spectra_2d(torch, [([phi.to(torch.float64).contiguous()],
                                                 [np.asarray(xxs[0], dtype=np.float64)],
                                                 tuple(ns), None, 1.0)])
         return _lib.to_host(torch, fs[0])
-    if P == 3 and same:
-        from . import adjoint_nd
-        with torch.no_grad():
-            fs = adjoint_nd.from_phi_torch(torch, phi.to(torch.float64).contiguous(), ns,
-                                           np.asarray(xxs[0], dtype=np.float64))
-        return _lib.to_host(torch, fs)
-    return None
+    fs = from_phi_nd_batch(torch, phi[None], ns, np.asarray(xxs[0], dtype=np.float64))
+    return _lib.to_host(torch, fs[0])
 
 
 def from_phi(phi, ns, xxs, mask_corners=True, pop_ids=None):
     """Spectrum of sample sizes ns from phi on grids xxs (1-5 populations,
     the linear-algebra paths of dadi/Spectrum_mod.py:1938-2061).  phi may be
-    a CUDA tensor (a density kept on the device): 2-D and 3-D spectra are
-    then computed there."""
+    a CUDA tensor (a density kept on the device): its spectrum is then
+    computed there (all axes on one grid, as dadi's models use) and only the
+    spectrum is copied back."""
     if hasattr(phi, "is_cuda") and phi.is_cuda:
         if not phi.dim() == len(ns) == len(xxs):
             raise ValueError('Dimensionality of phi and lengths of ns and xxs do not all '

@@ -307,6 +307,60 @@ int dgb_adjoint_table_nd(double *lam, int ndim, int L, const double *xx, const d
                          int nsteps, int frozen_mask, int nomut_mask, const double *states,
                          double *gpart, double *ws, size_t ws_bytes, void *stream);
 
+/* Batched N-dimensional engine: nitems integrations of ndim populations
+ * (1-5) on one grid xx of L points advance together; each step sweeps every
+ * axis once over the lines of every integration still running.  Replaces
+ * many calls of Integration.three_pops / four_pops / five_pops
+ * (dadi/Integration.py:389-554, 556-727, 729-937; the reference runs them one
+ * at a time, or as host processes, dadi/DFE/Cache2D_mod.py:117-167).  Each
+ * integration's density is bitwise the one dgb_integrate_table computes for
+ * it alone.
+ *   items   device, nitems dgb_itemnd, longest first (nsteps non-increasing)
+ *   nsteps  HOST, the same nitems step counts (they drive the launches)
+ *   phi_all device, the densities (each L^ndim doubles at its phi_off):
+ *           initial densities on entry, results on exit
+ *   table   device, parameter rows (DGB_ROW_STRIDE(ndim) doubles each, the
+ *           layout above); integration i uses rows row_off .. row_off+nsteps
+ *   settings use_delj_trick; threads = lines per CTA (0 auto, 32, 64, 128);
+ *           gam_placement 0 auto (workspace), 1 shared memory, 2 workspace
+ *   ws      dgb_batchnd_workspace_bytes(ndim, L, nitems, settings) bytes */
+typedef struct {
+    long phi_off; /* offset of the density in phi_all, in doubles */
+    long row_off; /* first table row */
+    int nsteps;   /* rows (steps) */
+    int masks;    /* frozen_mask | nomut_mask << 8 */
+} dgb_itemnd;
+size_t dgb_batchnd_workspace_bytes(int ndim, int L, int nitems, const dgb_settings *settings);
+int dgb_batchnd_integrate(const dgb_itemnd *items, const int *nsteps, int nitems, int ndim,
+                          int L, const double *xx, double *phi_all, const double *table,
+                          const dgb_settings *settings, void *ws, size_t ws_bytes,
+                          void *stream);
+
+/* One P-population integration (P = 1-5) in parametric form: the arguments
+ * of Integration.one_pop .. five_pops (dadi/Integration.py:178-937) with
+ * every parameter a dgb_pform; mig[k][j] is the rate into population k from
+ * j (the diagonal is ignored). */
+typedef struct {
+    double T, initial_t;
+    dgb_pform nu[DGB_MAX_DIM], gamma[DGB_MAX_DIM], h[DGB_MAX_DIM];
+    dgb_pform mig[DGB_MAX_DIM][DGB_MAX_DIM];
+    dgb_pform theta0;
+    int ndim, pad_;
+} dgb_instnd;
+
+/* Parameter rows of parametric integrations, evaluated in C on the HOST
+ * (all arrays host): the loop of dadi/Integration.py:504-553 (three_pops),
+ * 672-726 (four_pops), 884-935 (five_pops), 224-257 (one_pop): dt from the
+ * current parameters by _compute_dt (:147-176, the minimum over
+ * populations), the parameters at the next time, the same validation
+ * (reported as DGB_ST_* bits in status[i], which the caller zeroes).
+ * table == NULL counts rows into row_cnt; otherwise row_cnt[i] bounds the
+ * rows written at table + row_off[i] * DGB_ROW_STRIDE(ndim) and is replaced
+ * by their number.  dx0 is the grid's first spacing (old-timestep mode). */
+int dgb_schednd_host(const dgb_instnd *insts, int ninst, const dgb_settings *settings,
+                     long max_steps, double dx0, int *row_cnt, const long *row_off,
+                     double *table, int *status);
+
 /* Spectrum epilogue of 2-D integrations (device-resident inputs, one launch
  * per list).  dgb_from_phi2d: raw spectrum of each density,
  * out[a][b] (n1+1 x n2+1) = the piecewise-linear integral of phi against
@@ -326,6 +380,21 @@ typedef struct {
 } dgb_fs_item2d;
 size_t dgb_from_phi2d_smem_bytes(int Lmax, int nmax);
 int dgb_from_phi2d(const dgb_fs_item2d *items, int nitems, int Lmax, int nmax, void *stream);
+
+/* Raw spectra of nbatch densities of ndim populations (1-5), each L^ndim
+ * doubles (C order, all axes on the grid xx of L points), stored one after
+ * another in phi: out receives nbatch spectra of prod(ns[a]+1) doubles.
+ * The linear-algebra form of Spectrum.from_phi (dadi/Spectrum_mod.py:
+ * 1509-1547 for 2-D, 1774-1810 for 3-D, 1841-1870 for 4-D, 1938-2061):
+ * each axis, last first, is contracted against its weight tables d1[a] =
+ * dbeta1 and d2[a] = dbeta2 of cached_dbeta(ns[a], xx) (:25-40), device
+ * pointers to (ns[a]+1) x (L-1) doubles; ns, d1 and d2 are HOST arrays of
+ * ndim entries.  ws: dgb_from_phi_nd_workspace_bytes (the tensors between
+ * contractions).  The reference computes these on the host with numpy. */
+size_t dgb_from_phi_nd_workspace_bytes(int ndim, int L, const int *ns, int nbatch);
+int dgb_from_phi_nd(const double *phi, int nbatch, int ndim, int L, const double *xx,
+                    const int *ns, const double *const *d1, const double *const *d2,
+                    double *out, void *ws, size_t ws_bytes, void *stream);
 
 /* Extrapolation of 1-3 grids' spectra to zero grid spacing at x = 0
  * (linear_extrap / quadratic_extrap, dadi/Numerics.py:644-669; x = each

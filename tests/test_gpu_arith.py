@@ -30,7 +30,7 @@ def test_fp64_rate_and_idle_lanes(cuda_lib):
     which is why the kernels pack lines into full warps."""
     import torch
     from dadi_gb300 import _lib
-    full = _lib.fp64_fma_peak_tflops(torch, iters=1024, active_lanes=32)
-    quarter = _lib.fp64_fma_peak_tflops(torch, iters=1024, active_lanes=8)
+    full = _lib.fp64_fma_peak_tflops(torch, active_lanes=32, target_s=0.01, repeats=2)
+    quarter = _lib.fp64_fma_peak_tflops(torch, active_lanes=8, target_s=0.01, repeats=2)
     assert full > 0.1
     assert quarter < 0.5 * full

@@ -1,0 +1,82 @@
+"""The batched N-dimensional engine (dgb_batchnd_integrate): every
+integration of a batch gives bitwise the density the one-at-a-time path
+(dgb_integrate_table) gives it alone -- 3-D, 4-D and 5-D, integrations of
+different lengths, frozen and nomut populations, the delj trick, both
+Thomas-scratch placements and every lines-per-CTA choice -- and config 2
+through the batch matches dadi's golden spectrum."""
+import numpy as np
+import pytest
+
+import cases
+from util import assert_fs_parity, table_rows
+
+pytestmark = pytest.mark.gpu
+
+
+def _alone(phi0, xx, table, masks, delj=False):
+    from dadi_gb300 import integration
+    saved = integration.use_delj_trick
+    integration.use_delj_trick = delj
+    try:
+        return integration.run_table(phi0, xx, table, masks & 0xff, masks >> 8)
+    finally:
+        integration.use_delj_trick = saved
+
+
+@pytest.mark.parametrize("P,L,gam,threads,delj", [
+    (3, 20, 0, 0, False), (3, 20, 1, 0, False), (3, 21, 2, 32, False), (3, 20, 2, 128, True),
+    (4, 12, 0, 0, False), (4, 12, 1, 64, True), (5, 7, 0, 0, False), (2, 24, 0, 0, False),
+])
+def test_batch_equals_alone(cuda_lib, P, L, gam, threads, delj):
+    import torch
+    from dadi_gb300 import batchnd, integration
+    xx = cases.grid("default", L)
+    n = 6
+    tables = [table_rows(P, nst, 100 + k) for k, nst in enumerate([7, 19, 3, 19, 11, 1])]
+    masks = [0, 1, 2 << 8, 0, (1 << (P - 1)) | (1 << 8), 0]
+    phi0 = np.stack([cases.initial_phi(40 + k, (L,) * P) for k in range(n)])
+    saved = integration.use_delj_trick
+    integration.use_delj_trick = delj
+    try:
+        eng = batchnd.BatchND(P, L, xx=xx, gam_placement=gam, threads=threads)
+        out = eng.integrate(torch.from_numpy(phi0).cuda(), tables, masks).cpu().numpy()
+    finally:
+        integration.use_delj_trick = saved
+    for k in range(n):
+        ref = _alone(phi0[k], xx, tables[k], masks[k], delj)
+        assert np.array_equal(out[k], ref), (k, float(np.max(np.abs(out[k] - ref))))
+
+
+def test_batch_shared_initial_density(cuda_lib):
+    """One initial density for every integration of the batch."""
+    import torch
+    from dadi_gb300 import batchnd
+    P, L = 3, 16
+    xx = cases.grid("default", L)
+    phi0 = cases.initial_phi(5, (L,) * P)
+    tables = [table_rows(P, 5 + k, 200 + k) for k in range(4)]
+    out = batchnd.BatchND(P, L, xx=xx).integrate(torch.from_numpy(phi0).cuda(), tables)
+    out = out.cpu().numpy()
+    for k in range(4):
+        assert np.array_equal(out[k], _alone(phi0, xx, tables[k], 0))
+
+
+def test_growth3_batch_extrapolated_matches_dadi(cuda_lib, golden):
+    """Config 2 (three populations, exponential growth, pts [70,80,90], ns
+    (20,20,20)) with schedules walked in C and the grids integrated as
+    batches: the extrapolated spectrum within the spectrum bar of dadi's."""
+    import torch
+    from dadi_gb300 import batchnd, numerics, spectrum
+    g = cases.GROWTH3
+    rec = batchnd.growth3_instance(g["params"])
+    tabs, status = batchnd.schedules([rec])
+    assert status[0] == 0 and len(tabs[0]) == 675
+    res = []
+    for L in g["pts_l"]:
+        eng = batchnd.BatchND(3, L)
+        phi0 = torch.from_numpy(batchnd.initial_density("growth3", L)).cuda()
+        phi = eng.integrate(phi0, [tabs[0]])[0]
+        xx = numerics.default_grid(L)
+        res.append(spectrum.from_phi(phi, g["ns"], (xx, xx, xx)))
+    fs = numerics.extrapolate(res, [r.extrap_x for r in res])
+    assert_fs_parity(np.asarray(fs.data), golden["models"]["growth3_fs"])

@@ -27,9 +27,9 @@ def _model(phi1d, xx, dev):
     return p2, p3, p4
 
 
-def test_device_chain_equals_host(cuda_lib):
+def test_device_chain_equals_host(cuda_lib, monkeypatch):
     import torch
-    from dadi_gb300 import numerics, phimanip, spectrum
+    from dadi_gb300 import _lib, numerics, phimanip, spectrum
     xx = numerics.default_grid(16)
     phi1d = phimanip.phi_1D(xx)
     host = _model(phi1d, xx, False)
@@ -37,11 +37,19 @@ def test_device_chain_equals_host(cuda_lib):
     for h, d in zip(host, dev):
         assert torch.is_tensor(d) and d.is_cuda
         assert np.array_equal(d.cpu().numpy(), h)
-    # spectra of device densities: 2-D through the device epilogue, 3-D
-    # through the batched torch contraction, 4-D on the host
-    for h, d, ns in zip(host, dev, [(8, 8), (6, 6, 6), (3, 3, 3, 3)]):
-        xs = (xx,) * len(ns)
-        fh = spectrum.from_phi(h, ns, xs)
-        fd = spectrum.from_phi(d, ns, xs)
+    # spectra of device densities: 2-D through the device epilogue, 3-D and
+    # 4-D through the contraction kernel; only spectra come back to the host
+    copied = []
+    real_to_host = _lib.to_host
+    monkeypatch.setattr(_lib, "to_host", lambda t, x: copied.append(tuple(x.shape)) or
+                        real_to_host(t, x))
+    monkeypatch.setattr(torch.Tensor, "cpu", lambda *a, **k: pytest.fail("density copied"))
+    spectra = []
+    for d, ns in zip(dev, [(8, 8), (6, 6, 6), (3, 3, 3, 3)]):
+        spectra.append(spectrum.from_phi(d, ns, (xx,) * len(ns)))
+    monkeypatch.undo()
+    assert all(np.prod(s) <= 9 ** 3 for s in copied), copied
+    for h, fd, ns in zip(host, spectra, [(8, 8), (6, 6, 6), (3, 3, 3, 3)]):
+        fh = spectrum.from_phi(h, ns, (xx,) * len(ns))
         assert fd.extrap_x == xx[1] and fd.mask.flat[0] and fd.mask.flat[-1]
         assert_fs_parity(np.asarray(fd.data), np.asarray(fh.data))

@@ -158,3 +158,26 @@ def test_multinomial_ll_in_epilogue(cuda_lib):
         assert abs(float(torch_llm[i]) - ref) <= 1e-12 * scale
     _, ll2, llm2 = eng.spectra_ll(phis, d_data, 2e3, multinom=True)
     assert np.array_equal(llm2.cpu().numpy(), llm.cpu().numpy())
+
+
+@pytest.mark.parametrize("P,L,ns", [(1, 30, (12,)), (2, 25, (8, 11)), (3, 20, (6, 7, 9)),
+                                    (3, 90, (20, 20, 20)), (4, 12, (4, 5, 3, 6)),
+                                    (4, 40, (10, 10, 10, 10)), (5, 8, (3, 2, 4, 3, 2))])
+def test_from_phi_nd_matches_reference_contraction(cuda_lib, P, L, ns):
+    """The N-dimensional contraction kernel (dgb_from_phi_nd) on a batch of
+    densities against the oracle's from_phi (1-4 populations) and the host
+    5-D path (pinned to dadi's golden vectors), to REL."""
+    import torch
+    import cases
+    from dadi_gb300 import spectrum
+    from oracle import numerics as onum
+    xx = cases.grid("default", L)
+    phis = np.stack([cases.initial_phi(70 + b, (L,) * P) for b in range(3)])
+    out = spectrum.from_phi_nd_batch(torch, torch.from_numpy(phis).cuda(), ns, xx)
+    out = out.cpu().numpy()
+    for b in range(3):
+        if P <= 4:
+            ref = onum.from_phi(phis[b], ns, xx)
+        else:
+            ref = spectrum._from_phi_5D(*ns, *(xx,) * 5, phis[b])
+        _close(out[b], ref)

@@ -24,7 +24,7 @@ import numpy as np
 import pytest
 
 import cases
-from util import assert_fs_parity, fs_parity
+from util import fs_parity
 
 pytestmark = pytest.mark.gpu
 
@@ -73,11 +73,15 @@ def test_batched_workload_sample_matches_dadi_and_oracle(cuda_lib, golden, scale
         ref[int(i)] = scale_golden["golden_fs"][k]
     worst = 0.0
     mask = onum.corner_mask(fs.shape[1:])
+    bad = []
     for k, i in enumerate(idx):
-        assert_fs_parity(fs[k], ref[i])
-        worst = max(worst, fs_parity(fs[k], ref[i])[0])
+        rel, ab, _ = fs_parity(fs[k], ref[i])
+        worst = max(worst, rel)
+        if rel > 1e-9 or ab > 1e-21:
+            bad.append((i, rel, ab))
         ll_ref = onum.ll(5e4 * ref[i], obs, mask)
         assert abs(ll[k] - ll_ref) <= 1e-9 * abs(ll_ref), (i, ll[k], ll_ref)
+    assert not bad, bad
     print("max rel over %d instances: %.3g" % (len(idx), worst))
 
 
@@ -96,9 +100,18 @@ def test_batched_default_launch_equals_tuned(cuda_lib, scale_golden):
     assert np.array_equal(fa, fb)
 
 
-def _fd_rich(eng, p, data, scale, eps=1e-4):
-    """Central differences at eps and eps/2 (relative steps) in one batch,
-    and their Richardson combination."""
+#: Relative step of the config-4 finite differences (and half of it for the
+#: Richardson combination).  At these grids the likelihood's dependence on T
+#: has structure on the scale of 1e-5 relative, so steps of 1e-4 are outside
+#: the asymptotic range of central differences (measured with the oracle on
+#: draw 15: D(1e-4) = -460208, D(1e-5) = -460301, D(1e-6) = -460282.6,
+#: D(1e-7) = -460283.1; the adjoint gives -460282.5).
+FD_EPS = 2e-6
+
+
+def _stencil(p, eps=FD_EPS):
+    """The parameter sets of central differences at eps and eps/2 (relative
+    steps), in the order _fd_rich reads them."""
     rows = []
     for e in (eps, eps / 2):
         for k in range(6):
@@ -106,23 +119,73 @@ def _fd_rich(eng, p, data, scale, eps=1e-4):
                 q = p.copy()
                 q[k] += sgn * e * p[k]
                 rows.append(q)
-    _, ll, st = eng.run(np.array(rows), data=data, scale=scale)
+    return np.array(rows)
+
+
+def _fd_rich(eng, p, data, scale, eps=FD_EPS):
+    """Central differences at eps and eps/2 in one batch, and their
+    Richardson combination."""
+    _, ll, st = eng.run(_stencil(p, eps), data=data, scale=scale)
     assert int(st.abs().sum()) == 0
     ll = ll.cpu().numpy().reshape(2, 6, 2)
     d = [(ll[j, :, 0] - ll[j, :, 1]) / (2 * e * p) for j, e in enumerate((eps, eps / 2))]
     return d[0], (4 * d[1] - d[0]) / 3
 
 
+def _branches(p, tsf=1e-3):
+    """Which term binds the timestep at each step of an IM schedule
+    (dadi/Integration.py:147-176, 346-386): population (the min over the
+    two) and 0.25/nu or the migration rate (the max), and whether the step
+    was cut to T - t."""
+    s, nu1, nu2, T, m12, m21 = p
+    f = [lambda t: s * (nu1 / s) ** (t / T), lambda t: (1 - s) * (nu2 / (1 - s)) ** (t / T)]
+    m = [m12, m21]
+    t, out = 0.0, []
+    nu = [f[0](t), f[1](t)]
+    while t < T:
+        d = [tsf / max(0.25 / nu[k], m[k]) for k in range(2)]
+        k = 1 if d[1] < d[0] else 0
+        term = 0 if 0.25 / nu[k] >= m[k] else 1
+        dt = d[k]
+        cut = T - t < dt
+        out.append((k, term, cut))
+        t = t + min(dt, T - t)
+        nu = [f[0](t), f[1](t)]
+    return out
+
+
+def _smooth_candidates(draws, want=2, lo=150, hi=900):
+    """Draws among the first 256 whose finite-difference stencil stays on one
+    smooth piece of the discrete likelihood.  The schedule is built from
+    max/min choices (dt = 1e-3 / max(0.25 / nu, m), the smaller of the two
+    populations' dt, the last step cut to T - t): where a stencil point takes
+    another number of steps or another branch at some step, the likelihood
+    has a kink between the points and a central difference measures the
+    kink, not the derivative the adjoint gives.  With m12 near 5 and T near
+    0.5 such kinks are only 4e-4 apart in relative m12.  (The stencil is
+    checked at 1e-4 so that it is safely inside one piece.)"""
+    from dadi_gb300 import batch
+    steps = batch.count_steps(batch.im_instances(draws[:256]))
+    out = []
+    for i in range(256):
+        if not lo <= steps[i] <= hi:
+            continue
+        base = _branches(draws[i])
+        if all(_branches(q) == base for q in _stencil(draws[i].copy(), 1e-4)):
+            out.append(i)
+            if len(out) == want:
+                break
+    return out
+
+
 @pytest.mark.parametrize("which", [0, 1])
 def test_adjoint_at_config4_grids_matches_fd(cuda_lib, golden, which):
     """Config 4: gradients of the Poisson likelihood at pts [100,110,120],
     ns (40,40) for seed-0 draws among the first 256, against Richardson
-    central differences, 1e-6 max-norm relative."""
+    central differences on a smooth piece, 1e-6 max-norm relative."""
     from dadi_gb300 import batch
     draws = cases.im_draws()
-    steps = batch.count_steps(batch.im_instances(draws[:256]))
-    cand = [i for i in range(256) if 150 <= steps[i] <= 900]
-    i = cand[which * 3]
+    i = _smooth_candidates(draws)[which]
     obs = golden["models"]["im_obs"]
     eng = batch.Batch2D((100, 110, 120), NS)
     ll, grad, st = eng.loglik_and_grad(draws[i][None, :], obs, scale=5e4)
