@@ -283,7 +283,10 @@ def parity_of(fs_gpu, fs_cpu):
         n_small += ns
     return {"n_checked": len(fs_cpu), "max_rel": worst, "worst_instance": worst_i,
             "n_small": n_small, "max_abs_small_over_max": worst_small,
-            "bar": "max_rel <= 1e-9 over entries >= 1e-12 x max; smaller entries <= 1e-21 x max",
+            "bar": "max_rel <= %g over entries >= %g x max; smaller entries <= %g x max "
+                   "absolutely (the reference's own rounding noise sets the level)"
+                   % (util.FS_REL, util.TINY_FRAC, util.FS_REL * util.TINY_FRAC),
+            "pass": bool(worst <= util.FS_REL and worst_small <= util.FS_REL * util.TINY_FRAC),
             "against": "the oracle (the reference's algorithm, bit-identical to dadi's "
                        "golden vectors) on the stratified 64-instance sample"}
 
@@ -658,9 +661,42 @@ def run_config2(a):
         times.append(time.perf_counter() - t0)
     ps = 675 * 3 * (70 ** 3 + 80 ** 3 + 90 ** 3)
     t = float(np.median(times))
-    return {"model": "three populations, exponential growth, pts [70,80,90], ns (20,20,20)",
-            "seconds": t, "times_s": times, "point_sweeps": ps,
-            "point_sweeps_per_s": ps / t, "finite": bool(np.all(np.isfinite(np.asarray(fs))))}
+    out = {"model": "three populations, exponential growth, pts [70,80,90], ns (20,20,20)",
+           "seconds": t, "times_s": times, "point_sweeps": ps,
+           "point_sweeps_per_s": ps / t, "finite": bool(np.all(np.isfinite(np.asarray(fs))))}
+    # 32 parameter sets of the model (each parameter scaled by exp(U(log .5,
+    # log 2)), seed 0) as one batch per grid through batchnd.ModelBatch
+    from dadi_gb300 import batchnd
+    sets = growth3_sets(32)
+    mb = batchnd.ModelBatch("growth3", [70, 80, 90], (20, 20, 20))
+    mb.run(sets[:2])
+    tabs, _ = mb.tables(sets)
+    ps32 = sum(len(tb) for tb in tabs[0]) * 3 * (70 ** 3 + 80 ** 3 + 90 ** 3)
+    bt = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fsb, _, st = mb.run(sets)
+        fsb.cpu()
+        bt.append(time.perf_counter() - t0)
+    tb = float(min(bt))
+    out["batch32"] = {"sets": 32, "seconds": tb, "spectra_per_s": 32 / tb,
+                      "point_sweeps": ps32, "point_sweeps_per_s": ps32 / tb,
+                      "failed_sets": int(np.count_nonzero(st)),
+                      "note": "host wall clock of ModelBatch.run (schedules walked in C, the "
+                              "three grids batched on their own streams, N-D from_phi and "
+                              "extrapolation on the device, spectra copied back); best of 2"}
+    return out
+
+
+def growth3_sets(n, seed=0):
+    """n parameter sets of the three-population growth model: each of (nu0 x3,
+    nuF x3, m12, m13, m23, T) scaled by exp(U(log .5, log 2)), seed 0."""
+    from dadi_gb300 import models
+    nu0, nuF, m, g, T = models.GROWTH3_DEFAULT
+    th0 = np.array(list(nu0) + list(nuF) + list(m) + [T])
+    th = th0 * np.exp(np.random.default_rng(seed).uniform(np.log(.5), np.log(2), (n, 10)))
+    return [(tuple(r[0:3]), tuple(r[3:6]), tuple(r[6:9]), g, float(r[9])) for r in th]
 
 
 def run_profile_case(a):

@@ -44,6 +44,13 @@ def install(dadi_module=None):
             if T - initial_t < 0:
                 raise ValueError('Final integration time T (%f) is less than intial_time (%f). '
                                  'Integration cannot be run backwards.' % (T, initial_t))
+            if np.all([np.isscalar(v) for v in (nu, gamma, h, theta0, beta)]):
+                # recorded as dadi records it before its constant-parameter
+                # loop (dadi/Integration.py:214-216); the GPU then takes the
+                # temporal loop, as dadi's two_pops does under CUDA (:318-345)
+                demes = dadi_module.Demes
+                demes.cache.append(demes.IntegrationConst(duration=T - initial_t,
+                                                          start_sizes=[nu], deme_ids=deme_ids))
             f = dadi_module.Misc.ensure_1arg_func
             return cuda.Integration._one_pop_temporal_params(
                 phi, xx, T, initial_t, f(nu), f(gamma), f(h), f(theta0), f(beta), deme_ids)

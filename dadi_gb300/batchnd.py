@@ -19,7 +19,7 @@ import ctypes
 
 import numpy as np
 
-from . import _lib, integration, numerics, phimanip
+from . import _lib, epilogue, integration, numerics, phimanip, spectrum
 
 PF_CONST, PF_EXPLOG = _lib.PF_CONST, _lib.PF_EXPLOG
 
@@ -181,3 +181,73 @@ def initial_density(kind, L):
     if kind == "four":
         phi = phimanip.phi_3D_to_4D(phi, 0.0, 0.0, xx, xx, xx, xx)
     return phi
+
+
+#: The workload models with a batched form: (ndim, record builder).
+MODELS = {"growth3": (3, growth3_instance), "four": (4, four_split_instance)}
+
+
+class ModelBatch:
+    """Extrapolated spectra of many parameter sets of a three- or
+    four-population workload model ("growth3": models.growth3, "four":
+    models.four_split) on grids pts_l with sample sizes ns: the GPU form of
+    make_extrap_func(model)(params, ns, pts_l) for each set
+    (dadi/Numerics.py:334-475).  Per grid one batched integration (all sets
+    advance together; the grids on their own streams), the N-dimensional
+    from_phi kernel, then extrapolation with the fail_mag guard and the
+    Poisson likelihood in one launch: densities never leave the device."""
+
+    def __init__(self, kind, pts_l, ns, gam_placement=0, threads=0):
+        self.torch = _lib.require_cuda()
+        self.kind = kind
+        self.ndim, self.make = MODELS[kind]
+        self.pts_l = list(pts_l)
+        self.ns = tuple(ns)
+        self.engines = [BatchND(self.ndim, L, gam_placement=gam_placement, threads=threads)
+                        for L in self.pts_l]
+        self.phi0 = [_lib.upload_resident(self.torch, initial_density(kind, L))
+                     for L in self.pts_l]
+        self.x_l = [e.xx[1] for e in self.engines]
+        self._side = None
+
+    def tables(self, params_list):
+        """Per grid, the parameter tables of every set (one list shared by
+        all grids unless old-timestep mode makes dt depend on the grid), and
+        the status bits per set."""
+        insts = [self.make(p) for p in params_list]
+        if integration.current_settings()[2]:
+            per, status = [], np.zeros(len(insts), dtype=np.int32)
+            for e in self.engines:
+                t, st = schedules(insts, dx0=e.xx[1] - e.xx[0])
+                per.append(t)
+                status |= st
+            return per, status
+        t, status = schedules(insts)
+        return [t] * len(self.engines), status
+
+    def run(self, params_list, data=None, scale=1.0, timer=None):
+        """(extrapolated spectra (n, n1+1, ...), Poisson ll (n,) or None,
+        status (n,) numpy) for the parameter sets; CUDA tensors."""
+        torch = self.torch
+        tabs, status = self.tables(params_list)
+        cur = torch.cuda.current_stream()
+        if self._side is None:
+            self._side = [torch.cuda.Stream() for _ in self.engines]
+        fork = torch.cuda.Event()
+        fork.record(cur)
+        if timer is not None:
+            timer[0].record(cur)
+        raws = []
+        for e, p0, t, side in zip(self.engines, self.phi0, tabs, self._side):
+            side.wait_event(fork)
+            with torch.cuda.stream(side):
+                phi = e.integrate(p0, t)
+                raws.append(spectrum.from_phi_nd_batch(torch, phi, self.ns, e.xx))
+                phi.record_stream(side)
+            cur.wait_stream(side)
+        for r, side in zip(raws, self._side):
+            r.record_stream(cur)
+        if timer is not None:
+            timer[1].record(cur)
+        fs, ll = epilogue.extrapolate_batch(torch, raws, self.x_l, data, scale)
+        return fs, ll, status

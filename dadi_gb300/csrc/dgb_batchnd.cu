@@ -86,7 +86,7 @@ __global__ void k_coef_batch(NDBatch B, int nsl)
     AxisVecs v;
     nd_vecs_at(rec + ND_HEAD, L, DELJ, v);
     for (int i = threadIdx.x; i < L; i += blockDim.x)
-        build_axis_entry(i, L, g, Sh.s, Sh.vscale, DELJ, v);
+        build_axis_entry(i, L, g, Sh.s, Sh.vscale, DELJ, v, Sh.beta1);
     if (threadIdx.x == 0) {
         NDRecHead h;
         h.s = Sh.s;

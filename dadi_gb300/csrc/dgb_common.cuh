@@ -19,6 +19,17 @@
 //    is accurate to about one ulp; quotients become products.
 // These reassociations move results by a few ulps per step relative to the
 // reference C, far inside the 1e-9 relative bar on extrapolated spectra.
+//
+// Under the delj trick (Chang-Cooper delta_j, dadi/integration_shared.c:
+// 52-70) none of this is done.  delta_j = (-e w + e V - V) / (w - e w),
+// e = exp(w / V), cancels catastrophically as w / V -> 0, so any rounding
+// of MInt or of delta_j's own terms is amplified; the delj path therefore
+// follows the reference operation by operation: unscaled rows (b starts at
+// 1/dt, r = phi/dt), every product and sum rounded on its own (the __d*_rn
+// intrinsics, which the compiler never fuses into a multiply-add, where C
+// compiled for x86-64 has no fused multiply-add either), IEEE division, and
+// the Numerical-Recipes recurrence as written.  Only exp is CUDA's (an
+// error bound of one ulp rather than the C library's half ulp).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -136,7 +147,8 @@ struct GridVecs {
 // Per-step coefficient vectors of one axis (see the header comment).
 struct AxisVecs {
     double *A1, *A0, *C1, *C0, *B0;
-    // delj-trick path only: per-interval G, P, Q, VInt and per-row dt*dfac
+    // delj-trick path only: per-interval selection term, V[i]/(2dx),
+    // V[i+1]/(2dx), VInt, and per-row dfactor
     double *G, *Pv, *Qv, *VI, *DF;
 };
 
@@ -171,12 +183,39 @@ DGB_HD void corner_bc(int P, int axis, const double *mig, double nu, double gamm
     bce = (ml >= 0) ? dt * (-(-0.5 / nu - ml) * 2. / dxl) : 0.0;
 }
 
+// ------------------------------------------- the delj path's exact operations
+
+__device__ __forceinline__ double xm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double xa(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double xs(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double xd(double a, double b) { return __ddiv_rn(a, b); }
+
+// Selection part of Mfunc (dadi/integration_shared.c:12-14) in the
+// reference's order: gamma * 2*(h + (1.-2*h)*x) * x*(1.-x).
+__device__ __forceinline__ double msel_ref(double x, double gamma, double h)
+{
+    return xm(xm(xm(xm(gamma, 2.0), xa(h, xm(xs(1.0, xm(2.0, h)), x))), x), xs(1.0, x));
+}
+
+// Vfunc (dadi/integration_shared.c:4-6), or Vfunc_beta (:8-10) when beta > 0
+// (one population): 1./nu * x*(1.-x) [* pow(beta+1, 2)/(4*beta)].
+__device__ __forceinline__ double vfunc_ref(double x, double nu, double beta)
+{
+    double v = xm(xm(xd(1.0, nu), x), xs(1.0, x));
+    if (beta > 0) {
+        const double b1 = xa(beta, 1.0);
+        v = xd(xm(v, xm(b1, b1)), xm(4.0, beta));
+    }
+    return v;
+}
+
 // Build entry i of the per-step vectors of one axis (called for i = 0..L-1
 // by different threads).  vscale multiplies V (the breeding-ratio factor of
-// Vfunc_beta in 1-D, 1 otherwise).
+// Vfunc_beta in 1-D, 1 otherwise); beta1 is the breeding ratio itself for one
+// population and 0 otherwise (the delj path evaluates Vfunc_beta as written).
 __device__ __forceinline__ void build_axis_entry(int i, int L, const GridVecs &g,
                                                  const AxisScalars &s, double vscale,
-                                                 bool delj, AxisVecs &v)
+                                                 bool delj, AxisVecs &v, double beta1 = 0.0)
 {
     const double dt = s.dt;
     const double iv = s.inv_nu * vscale;
@@ -191,13 +230,15 @@ __device__ __forceinline__ void build_axis_entry(int i, int L, const GridVecs &g
         v.C1[i] = 0.5 * dfi;
         v.C0[i] = -dfi * fma(-0.5, G, Q);
         if (delj) {
-            // the delj path rebuilds MInt per point in the reference order,
-            // so only the selection term and VInt are stored
-            // (dadi/integration2D.c:47-49: VInt = Vfunc(xInt, nu))
-            v.G[i] = msel(g.xInt[i], s.gamma, s.h);
-            v.Pv[i] = P;
-            v.Qv[i] = Q;
-            v.VI[i] = (s.inv_nu * g.xInt[i]) * (1. - g.xInt[i]) * vscale;
+            // the delj path rebuilds MInt per point in the reference order;
+            // per interval it needs the selection term, V[i]/(2 dx[i]),
+            // V[i+1]/(2 dx[i]) and VInt (dadi/integration2D.c:42-49,
+            // integration_shared.c:72-93), each rounded as the reference does
+            const double d2 = xm(2.0, g.dx[i]);
+            v.G[i] = msel_ref(g.xInt[i], s.gamma, s.h);
+            v.Pv[i] = xd(vfunc_ref(g.x[i], s.nu, beta1), d2);
+            v.Qv[i] = xd(vfunc_ref(g.x[i + 1], s.nu, beta1), d2);
+            v.VI[i] = vfunc_ref(g.xInt[i], s.nu, beta1);
         }
     } else {
         v.C1[i] = 0;
@@ -216,7 +257,7 @@ __device__ __forceinline__ void build_axis_entry(int i, int L, const GridVecs &g
     }
     v.B0[i] = fma(dfi, p_i + q_im1, 1.0);
     if (delj)
-        v.DF[i] = dfi;
+        v.DF[i] = g.dfac[i]; // unscaled: the delj rows are the reference's
 }
 
 // ------------------------------------------------------------ line solvers
@@ -286,69 +327,84 @@ __device__ __forceinline__ void solve_line(TP *__restrict__ ph, int sp, TG *__re
     back_substitute(ph, sp, gm, gs, L, u);
 }
 
-// Chang-Cooper delta_j (dadi/integration_shared.c:52-70) for one interval.
+// Chang-Cooper delta_j (dadi/integration_shared.c:52-70) for one interval,
+// in the reference's order.
 __device__ __forceinline__ double delj_of(double MInt, double VInt, double dx)
 {
-    double wj = 2 * MInt * dx;
-    double epsj = exp(wj / VInt);
+    const double wj = xm(xm(2.0, MInt), dx);
+    const double epsj = exp(xd(wj, VInt));
     if ((epsj != 1.0) && (wj != 0))
-        return (-epsj * wj + epsj * VInt - VInt) / (wj - epsj * wj);
+        return xd(xs(xa(xm(-epsj, wj), xm(epsj, VInt)), VInt), xs(wj, xm(epsj, wj)));
     return 0.5;
 }
 
-// Thomas solve of one line with the delj trick.  MInt is rebuilt per
-// interval exactly as Mfunc{2,3,4}D computes it (dadi/integration_shared.c:
-// 15-25: sum over the other axes of m_k (o_k - x), then the selection term),
-// because exp(wj/VInt) amplifies any rounding difference in MInt; the
-// coefficients then follow compute_abc_nobc, scaled by dt.
+// Thomas solve of one line with the delj trick, as the reference computes
+// it: MInt per interval as Mfunc{1..5}D (dadi/integration_shared.c:12-30:
+// the migration terms m_k (o_k - x) summed in increasing axis order, then
+// the selection term), delta_j, the unscaled rows of compute_abc_nobc
+// (:72-93, b = 1/dt + ...), the corner terms of dadi/integration2D.c:67-70
+// when c0 / c1 (this line's other coordinates are all 0 / all 1; always in
+// one dimension, integration1D.c:47-51), r = phi/dt, and tridiag_premalloc
+// (dadi/tridiag.c:14-34).  The gam scratch holds element p at gm[p*gs].
 template <typename TP, typename TG>
 __device__ __forceinline__ void solve_line_delj(TP *__restrict__ ph, int sp, TG *__restrict__ gm,
                                                 int gs, int L, const double *mo,
-                                                const double *oo, int nother, double bs,
-                                                double be, const GridVecs &gv,
-                                                const AxisVecs &v)
+                                                const double *oo, int nother, bool c0, bool c1,
+                                                const GridVecs &gv, const AxisVecs &v,
+                                                const AxisScalars &s)
 {
-    auto mint = [&](int k) {
-        double x = gv.xInt[k];
+    auto mfun = [&](double x, double sel) {
         if (nother == 0)
-            return v.G[k];
-        double acc = mo[0] * (oo[0] - x);
+            return sel;
+        double acc = xm(mo[0], xs(oo[0], x));
         for (int j = 1; j < nother; j++)
-            acc = acc + mo[j] * (oo[j] - x);
-        return acc + v.G[k];
+            acc = xa(acc, xm(mo[j], xs(oo[j], x)));
+        return xa(acc, sel);
     };
-    // interval k quantities: at_k = MInt d + P, ct_k = -MInt (1-d) + Q
-    double Mk = mint(0);
+    const double dt = s.dt;
+    const double idt = xd(1.0, dt);
+    // interval 0: atemp, ctemp (compute_abc_nobc)
+    double Mk = mfun(gv.xInt[0], v.G[0]);
     double d = delj_of(Mk, v.VI[0], gv.dx[0]);
-    double at = Mk * d + v.Pv[0];
-    double ct = -Mk * (1 - d) + v.Qv[0];
-    double b = fma(v.DF[0], at, 1.0) + bs;
-    double inv = rcp_full(b);
-    double u = ph[0] * inv;
-    ph[0] = u;
-    double g = (-v.DF[0] * ct) * inv;
-    gm[gs] = g;
-    for (int i = 1; i < L; i++) {
-        double a = -v.DF[i] * at;
-        double bsum = ct;
-        if (i < L - 1) {
-            Mk = mint(i);
-            d = delj_of(Mk, v.VI[i], gv.dx[i]);
-            at = Mk * d + v.Pv[i];
-            bsum = bsum + at;
-            ct = -Mk * (1 - d) + v.Qv[i];
-        }
-        double bb = fma(v.DF[i], bsum, 1.0) + (i == L - 1 ? be : 0.0);
-        double bet = fma(-a, g, bb);
-        inv = rcp_full(bet);
-        u = fma(-a, u, ph[i * sp]) * inv;
-        ph[i * sp] = u;
-        if (i < L - 1) {
-            g = (-v.DF[i] * ct) * inv;
-            gm[(i + 1) * gs] = g;
-        }
+    double at = xa(xm(Mk, d), v.Pv[0]);
+    double ct = xa(xm(-Mk, xs(1.0, d)), v.Qv[0]);
+    double b = xa(idt, xm(v.DF[0], at));
+    if (c0) {
+        const double mf = mfun(gv.x[0], msel_ref(gv.x[0], s.gamma, s.h));
+        if (mf <= 0)
+            b = xa(b, xd(xm(xs(xd(0.5, s.nu), mf), 2.0), gv.dx[0]));
     }
-    back_substitute(ph, sp, gm, gs, L, u);
+    double bet = b;
+    double u = xd(xd((double)ph[0], dt), bet);
+    ph[0] = u;
+    double cprev = -xm(v.DF[0], ct);
+    for (int i = 1; i < L; i++) {
+        const double a = -xm(v.DF[i], at);
+        double bb = xa(idt, xm(v.DF[i], ct));
+        double cnext = 0;
+        if (i < L - 1) {
+            Mk = mfun(gv.xInt[i], v.G[i]);
+            d = delj_of(Mk, v.VI[i], gv.dx[i]);
+            at = xa(xm(Mk, d), v.Pv[i]);
+            ct = xa(xm(-Mk, xs(1.0, d)), v.Qv[i]);
+            bb = xa(bb, xm(v.DF[i], at));
+            cnext = -xm(v.DF[i], ct);
+        } else if (c1) {
+            const double ml = mfun(gv.x[L - 1], msel_ref(gv.x[L - 1], s.gamma, s.h));
+            if (ml >= 0)
+                bb = xa(bb, xd(xm(-xs(-xd(0.5, s.nu), ml), 2.0), gv.dx[L - 2]));
+        }
+        const double g = xd(cprev, bet);
+        gm[i * gs] = g;
+        bet = xs(bb, xm(a, g));
+        u = xd(xs(xd((double)ph[i * sp], dt), xm(a, u)), bet);
+        ph[i * sp] = u;
+        cprev = cnext;
+    }
+    for (int i = L - 2; i >= 0; i--) {
+        u = xs((double)ph[i * sp], xm((double)gm[(i + 1) * gs], u));
+        ph[i * sp] = u;
+    }
 }
 
 } // namespace dgb

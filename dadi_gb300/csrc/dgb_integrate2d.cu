@@ -278,15 +278,15 @@ __global__ void __launch_bounds__(K2_THREADS) k_integrate2d(K2Args A)
                     if (A.gam_smem) {
                         double *gm = gam_s + line;
                         if (DELJ)
-                            solve_line_delj(ph, sp, gm, L, L, &s.mig[1 - a], &g.x[line], 1, bs,
-                                            be, g, v[a]);
+                            solve_line_delj(ph, sp, gm, L, L, &s.mig[1 - a], &g.x[line], 1,
+                                            line == j0, line == j1, g, v[a], s);
                         else
                             solve_line(ph, sp, gm, L, L, W, bs, be, v[a], s);
                     } else {
                         double *gm = gam_g + line;
                         if (DELJ)
-                            solve_line_delj(ph, sp, gm, L, L, &s.mig[1 - a], &g.x[line], 1, bs,
-                                            be, g, v[a]);
+                            solve_line_delj(ph, sp, gm, L, L, &s.mig[1 - a], &g.x[line], 1,
+                                            line == j0, line == j1, g, v[a], s);
                         else
                             solve_line(ph, sp, gm, L, L, W, bs, be, v[a], s);
                     }

@@ -34,6 +34,7 @@ __host__ __device__ inline size_t nd_smem_doubles(int L, int nt, bool delj)
 struct NDShared {
     AxisScalars s;
     double vscale;
+    double beta1; // the breeding ratio for one population, else 0
     double inj[DGB_MAX_DIM];
 };
 
@@ -150,6 +151,7 @@ static __device__ void nd_load_params(const NDArgs &A, NDShared &Sh, const GridV
               s.bcs, s.bce);
     // Vfunc_beta's factor in 1-D (dadi/integration_shared.c:8-10)
     Sh.vscale = (P == 1) ? pow(beta + 1, 2) / (4 * beta) : 1.0;
+    Sh.beta1 = (P == 1) ? beta : 0.0;
     double val = inject_value(P, s.dt, theta0, g.x[0], g.x[1], g.x[2]);
     for (int k = 0; k < DGB_MAX_DIM; k++)
         Sh.inj[k] = (A.inject_mask >> k & 1) ? val : 0.0;
@@ -294,7 +296,7 @@ __device__ __forceinline__ void nd_solve_tile(const NDArgs &A, double *tile, dou
     double bs = all0 ? s.bcs : 0.0;
     double be = all1 ? s.bce : 0.0;
     if (DELJ)
-        solve_line_delj(tile + t, tp, gam + t, nt, L, mo, oo, no, bs, be, g, v);
+        solve_line_delj(tile + t, tp, gam + t, nt, L, mo, oo, no, all0, all1, g, v, s);
     else
         solve_line(tile + t, tp, gam + t, nt, L, W, bs, be, v, s);
 }

@@ -40,7 +40,7 @@ __global__ void k_sweep_nd(NDArgs A)
         nd_load_params(A, Sh, g);
     __syncthreads();
     for (int i = threadIdx.x; i < L; i += blockDim.x)
-        build_axis_entry(i, L, g, Sh.s, Sh.vscale, DELJ, v);
+        build_axis_entry(i, L, g, Sh.s, Sh.vscale, DELJ, v, Sh.beta1);
     const long l0 = (long)blockIdx.x * nt;
     const int n = (int)min((long)nt, A.nlines - l0);
     nd_tile_io(A, tile, nt, l0, n, false);
@@ -88,7 +88,7 @@ __global__ void k_coef_nd(NDArgs A, long step0, int frozen_mask, int active, dou
     AxisVecs v;
     nd_vecs_at(rec + ND_HEAD, L, DELJ, v);
     for (int i = threadIdx.x; i < L; i += blockDim.x)
-        build_axis_entry(i, L, g, Sh.s, Sh.vscale, DELJ, v);
+        build_axis_entry(i, L, g, Sh.s, Sh.vscale, DELJ, v, Sh.beta1);
     if (threadIdx.x == 0) {
         NDRecHead h;
         h.s = Sh.s;

@@ -134,3 +134,47 @@ def spectra_2d_batch(torch, phis, xxs, ns, data=None, scale=1.0, fail_mag=10.0,
     if multinom:
         return out.view(n, n1 + 1, n2 + 1), ll, llm
     return out.view(n, n1 + 1, n2 + 1), ll
+
+
+def extrapolate_batch(torch, raws, x_l, data=None, scale=1.0, fail_mag=10.0, multinom=False):
+    """Extrapolation (with the fail_mag guard) and likelihoods of n spectra of
+    any dimension given on 1-3 grids: raws[g] is an (n, ...) contiguous CUDA
+    tensor of raw spectra on grid g, x_l the grids' extrap_x (xx[1]).  One
+    dgb_extrap_ll launch; the first and last entries are the masked corners
+    (dadi/Spectrum_mod.py:178-182).  Returns (fs (n, ...), ll (n,) or None)
+    and, with multinom, the multinomial likelihoods third."""
+    lib = _lib.lib()
+    dev = raws[0].device
+    n = int(raws[0].shape[0])
+    shape = tuple(raws[0].shape[1:])
+    size = int(np.prod(shape))
+    out = torch.empty((n,) + shape, dtype=torch.float64, device=dev)
+    ll = torch.empty(n, dtype=torch.float64, device=dev) if data is not None else None
+    llm = torch.empty(n, dtype=torch.float64, device=dev) \
+        if (data is not None and multinom) else None
+    ex = np.zeros(n, dtype=EX_ITEM)
+    idx = np.arange(n, dtype=np.uint64)
+    for q, (r, x) in enumerate(zip(raws, x_l)):
+        assert r.is_contiguous() and tuple(r.shape) == (n,) + shape
+        ex["fs"][:, q] = np.uint64(r.data_ptr()) + idx * np.uint64(8 * size)
+        ex["x"][:, q] = x
+    ex["out"] = np.uint64(out.data_ptr()) + idx * np.uint64(8 * size)
+    ex["ngrids"], ex["size"], ex["mask_corners"] = len(raws), size, 1
+    if data is not None:
+        d = data if torch.is_tensor(data) else _lib.to_device(torch, data)
+        d = d.to(torch.float64).contiguous()
+        assert d.numel() == size
+        ex["data"] = d.data_ptr()
+        ex["ll"] = np.uint64(ll.data_ptr()) + idx * np.uint64(8)
+        ex["scale"] = scale
+        if llm is not None:
+            ex["llm"] = np.uint64(llm.data_ptr()) + idx * np.uint64(8)
+        keep = d
+    d_ex = _lib.to_device(torch, ex.view(np.uint8), np.uint8)
+    _lib.check(lib.dgb_extrap_ll(_lib.dptr(d_ex), n, float(fail_mag),
+                                 _lib.stream_handle(torch)), "dgb_extrap_ll")
+    if data is not None:
+        del keep
+    if multinom:
+        return out, ll, llm
+    return out, ll

@@ -27,8 +27,13 @@ Scheduling:
   only spectra and likelihoods come back, in one copy per wave.
 * Gradient requests that share grid sizes, sample sizes and observed data
   are grouped the same way into one forward-with-checkpoints launch and one
-  adjoint launch; they and the 3-D and 4-D requests run on worker threads
-  with their own streams, overlapping the waves.
+  adjoint launch; they run on worker threads with their own streams,
+  overlapping the waves.
+* 3-D and 4-D requests wait on the host until a worker is free; the worker
+  then takes every waiting request of the same model, grids, sample sizes
+  and data and integrates them as one batch (batchnd.ModelBatch: all of
+  them advance together in each sweep launch, densities stay on the device,
+  only spectra and likelihoods come back).
 
 Every request records arrival, admission and completion times; latency is
 completion minus arrival.  The server uses up to max_inflight + 2 * workers
@@ -44,7 +49,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import _lib, batch, epilogue, models, numerics, phimanip, spectrum
+from . import _lib, batch, batchnd, epilogue, models, numerics, phimanip, spectrum
 
 ITEM_DTYPE = batch.ITEM2D_DTYPE
 
@@ -121,11 +126,11 @@ class Server:
     max_wave / min_wave: most / fewest requests per 2-D wave (fewer when
     fewer are waiting); max_inflight: waves in flight at once (one CUDA
     stream each); slots: most 2-D work items in flight (default two per
-    SM); workers: threads for 3-D/4-D requests, and as many again for
-    gradient groups."""
+    SM); workers: threads for 3-D/4-D request groups, and as many again for
+    gradient groups; max_nd_group: most 3-D/4-D requests per group."""
 
     def __init__(self, hbm_budget=16 << 30, max_wave=512, workers=4, max_inflight=16,
-                 min_wave=8, slots=None):
+                 min_wave=8, slots=None, max_nd_group=64):
         self.torch = _lib.require_cuda()
         self.budget = int(hbm_budget)
         self.max_wave = max_wave
@@ -136,11 +141,13 @@ class Server:
                 self.torch.cuda.current_device()).multi_processor_count
         self.slots = int(slots)
         self.workers = workers
+        self.max_nd_group = int(max_nd_group)
         self._used = 0
         self._lock = threading.Lock()
         self._grids = {}
         self._phi0 = {}
         self._engines = {}
+        self._batches = {}
         self._obs = {}
 
     # ----------------------------------------------------------- resources
@@ -316,23 +323,33 @@ class Server:
             r.fs, r.ll, r.grad, r.status = fs[k], float(ll[k]), grad[k], int(st[k])
         return reqs
 
-    def _run_other(self, req):
-        """3-D and 4-D requests: the drop-in drivers on a worker stream."""
+    def _model_batch(self, kind, pts_l, ns):
+        key = (kind, tuple(pts_l), tuple(ns))
+        with self._lock:
+            mb = self._batches.get(key)
+            if mb is None:
+                mb = self._batches[key] = batchnd.ModelBatch(kind, pts_l, ns)
+                mb.lock = threading.Lock()
+        return mb
+
+    def _run_other(self, reqs):
+        """3-D and 4-D requests sharing model, grids, sample sizes and data:
+        one batched integration per grid on a worker stream."""
         torch = self.torch
+        r0 = reqs[0]
+        mb = self._model_batch(r0.kind, r0.pts_l, r0.ns)
         s = torch.cuda.Stream(priority=-1)
-        with torch.cuda.stream(s):
-            if req.kind == "growth3":
-                f = numerics.make_extrap_func(models.growth3)
-            elif req.kind == "four":
-                f = numerics.make_extrap_func(models.four_split)
-            else:
-                raise ValueError(req.kind)
-            fs = f(req.params, req.ns, list(req.pts_l))
-            req.fs = np.asarray(fs.data)
-            if req.data is not None:
-                from . import inference
-                req.ll = float(inference.ll(req.scale * fs, spectrum.Spectrum(req.data)))
-        return [req]
+        with mb.lock, torch.cuda.stream(s):
+            data = self._data(r0.data) if r0.data is not None else None
+            fs, ll, status = mb.run([r.params for r in reqs], data=data, scale=r0.scale)
+            fs = _lib.to_host(torch, fs)
+            ll = _lib.to_host(torch, ll) if ll is not None else None
+        for k, r in enumerate(reqs):
+            r.fs = fs[k]
+            if ll is not None:
+                r.ll = float(ll[k])
+            r.status = int(status[k])
+        return reqs
 
     # ----------------------------------------------------------------- run
 
@@ -367,9 +384,11 @@ class Server:
         nxt = 0
         remaining = len(reqs)
         held = []   # non-wave requests waiting for budget
+        waiting_nd = []  # admitted 3-D / 4-D requests waiting for a worker
+        nd_busy = [0]
 
         def busy():
-            return bool(inflight or futures)
+            return bool(inflight or futures or waiting_nd)
 
         try:
             while remaining:
@@ -395,10 +414,22 @@ class Server:
                         key = (tuple(r.pts_l), tuple(r.ns), id(r.data), r.scale)
                         groups.setdefault(key, []).append(r)
                     else:
-                        futures.append(([r], pool.submit(self._run_other, r)))
+                        waiting_nd.append(r)
                 held = keep
                 for grp in groups.values():
                     futures.append((grp, gpool.submit(self._run_grad_group, grp)))
+                # 3-D / 4-D: a free worker takes every waiting request that
+                # shares the oldest one's model, grids, sample sizes and data
+                while waiting_nd and nd_busy[0] < self.workers:
+                    r0 = waiting_nd[0]
+                    key = (r0.kind, tuple(r0.pts_l), tuple(r0.ns), id(r0.data), r0.scale)
+                    grp = [r for r in waiting_nd
+                           if (r.kind, tuple(r.pts_l), tuple(r.ns), id(r.data), r.scale) == key]
+                    grp = grp[:self.max_nd_group]
+                    ids = set(id(r) for r in grp)
+                    waiting_nd = [r for r in waiting_nd if id(r) not in ids]
+                    nd_busy[0] += 1
+                    futures.append((grp, pool.submit(self._run_other, grp), True))
                 # 2-D waves, cheapest first, while streams and CTA slots are free
                 if waiting2d and arrived:
                     waiting2d.sort(key=self._cost)
@@ -442,8 +473,11 @@ class Server:
                             remaining -= 1
                 inflight = still
                 fst = []
-                for grp, fu in futures:
+                for item in futures:
+                    grp, fu = item[0], item[1]
                     if fu.done():
+                        if len(item) > 2:
+                            nd_busy[0] -= 1
                         try:
                             fu.result()
                         except Exception as e:  # report per request, keep serving
@@ -455,7 +489,7 @@ class Server:
                             self._used -= r._fp
                             remaining -= 1
                     else:
-                        fst.append((grp, fu))
+                        fst.append(item)
                 futures = fst
                 if remaining:
                     time.sleep(2e-4)

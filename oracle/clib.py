@@ -36,6 +36,8 @@ def lib():
         L.orc_sweep.restype = ctypes.c_int
         L.orc_sweep_rhs_variant.argtypes = L.orc_sweep.argtypes
         L.orc_sweep_rhs_variant.restype = ctypes.c_int
+        L.orc_sweep_exp_variant.argtypes = L.orc_sweep.argtypes
+        L.orc_sweep_exp_variant.restype = ctypes.c_int
         L.orc_sweep_precalc.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         _dp, _dp, _dp, ctypes.c_double]
         L.orc_sweep_precalc.restype = ctypes.c_int
@@ -61,6 +63,9 @@ def ref_lib():
 
 #: When True, sweep() uses orc_sweep_rhs_variant (noise-floor measurements).
 rhs_variant = False
+#: When True, sweep() uses orc_sweep_exp_variant (noise floor under the delj
+#: trick: another faithfully rounded exp).
+exp_variant = False
 
 
 def sweep(phi, xx, axis, nu, mig, gamma, h, dt, beta=1.0, use_delj_trick=False):
@@ -70,6 +75,8 @@ def sweep(phi, xx, axis, nu, mig, gamma, h, dt, beta=1.0, use_delj_trick=False):
     mig = np.ascontiguousarray(np.broadcast_to(np.asarray(mig, dtype=np.float64),
                                                (phi.ndim,)))
     fn = lib().orc_sweep_rhs_variant if rhs_variant else lib().orc_sweep
+    if exp_variant:
+        fn = lib().orc_sweep_exp_variant
     rc = fn(_ptr(phi), phi.ndim, phi.shape[0], axis, _ptr(xx),
                          float(nu), _ptr(mig), float(gamma), float(h), float(beta),
                          float(dt), int(bool(use_delj_trick)))

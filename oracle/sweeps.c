@@ -63,16 +63,36 @@ static double orc_M(double x, int nother, const double *o, const double *m,
     return acc + orc_Msel(x, gamma, h);
 }
 
+/* exp(z), or (exp_mode != 0) the other neighbour of the true value for
+ * about half of the arguments (picked by a hash of z's bits): the result of
+ * another faithfully rounded exp, such as one with a 1-ulp error bound.
+ * Used only to measure how far an equally valid exp moves the reference's
+ * results under the delj trick (its noise floor). */
+static double orc_exp(double z, int exp_mode)
+{
+    double e = exp(z);
+    if (!exp_mode)
+        return e;
+    unsigned long long b;
+    memcpy(&b, &z, sizeof b);
+    b ^= b >> 29;
+    b *= 0xbf58476d1ce4e5b9ull;
+    b ^= b >> 32;
+    if (b & 1)
+        return nextafter(e, (b & 2) ? INFINITY : 0.0);
+    return e;
+}
+
 /* Chang-Cooper delta_j, or 0.5 (dadi/integration_shared.c:52-70). */
 static void orc_delj(const double *dx, const double *MInt, const double *VInt,
-                     int n, double *delj, int use_delj_trick)
+                     int n, double *delj, int use_delj_trick, int exp_mode)
 {
     for (int i = 0; i < n - 1; i++) {
         delj[i] = 0.5;
         if (!use_delj_trick)
             continue;
         double wj = 2 * MInt[i] * dx[i];
-        double epsj = exp(wj / VInt[i]);
+        double epsj = orc_exp(wj / VInt[i], exp_mode);
         if ((epsj != 1.0) && (wj != 0))
             delj[i] = (-epsj * wj + epsj * VInt[i] - VInt[i]) / (wj - epsj * wj);
     }
@@ -180,6 +200,16 @@ int orc_sweep_rhs_variant(double *phi, int ndim, int L, int axis, const double *
                           use_delj_trick, 1);
 }
 
+/* The same sweep with exp replaced by another faithfully rounded exp (see
+ * orc_exp): the reference's noise floor under the delj trick. */
+int orc_sweep_exp_variant(double *phi, int ndim, int L, int axis, const double *xx,
+                          double nu, const double *mig, double gamma, double h,
+                          double beta, double dt, int use_delj_trick)
+{
+    return orc_sweep_impl(phi, ndim, L, axis, xx, nu, mig, gamma, h, beta, dt,
+                          use_delj_trick, 2);
+}
+
 static int orc_sweep_impl(double *phi, int ndim, int L, int axis, const double *xx,
                           double nu, const double *mig, double gamma, double h,
                           double beta, double dt, int use_delj_trick, int r_mode)
@@ -220,10 +250,10 @@ static int orc_sweep_impl(double *phi, int ndim, int L, int axis, const double *
         double Mlast = orc_M(xx[L - 1], nother, o, mo, gamma, h);
         for (int i = 0; i < L - 1; i++)
             MInt[i] = orc_M(xInt[i], nother, o, mo, gamma, h);
-        orc_delj(dx, MInt, VInt, L, delj, use_delj_trick);
+        orc_delj(dx, MInt, VInt, L, delj, use_delj_trick, r_mode == 2);
         orc_abc(dx, dfac, delj, MInt, V, dt, L, a, b, c);
         for (int i = 0; i < L; i++)
-            r[i] = r_mode ? (1 / dt) * phi[s0 + i * stride] : phi[s0 + i * stride] / dt;
+            r[i] = (r_mode == 1) ? (1 / dt) * phi[s0 + i * stride] : phi[s0 + i * stride] / dt;
         if (all0 && Mfirst <= 0)
             b[0] += (0.5 / nu - Mfirst) * 2. / dx[0];
         if (all1 && Mlast >= 0)

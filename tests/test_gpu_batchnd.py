@@ -80,3 +80,39 @@ def test_growth3_batch_extrapolated_matches_dadi(cuda_lib, golden):
         res.append(spectrum.from_phi(phi, g["ns"], (xx, xx, xx)))
     fs = numerics.extrapolate(res, [r.extrap_x for r in res])
     assert_fs_parity(np.asarray(fs.data), golden["models"]["growth3_fs"])
+
+
+@pytest.mark.parametrize("kind,pts_l,ns", [("growth3", [16, 20, 24], (6, 7, 8)),
+                                           ("four", [10, 12, 14], (3, 4, 3, 5))])
+def test_model_batch_equals_drop_in(cuda_lib, kind, pts_l, ns):
+    """ModelBatch (schedules in C, batched integration per grid, N-D
+    from_phi, device extrapolation and likelihood) gives each parameter set
+    the spectrum and likelihood of the one-at-a-time drop-in."""
+    from dadi_gb300 import batchnd, inference, models, numerics, spectrum
+    base = models.GROWTH3_DEFAULT if kind == "growth3" else models.FOUR_DEFAULT
+    if kind == "growth3":
+        sets = [base, (base[0], base[1], (1.0, 0.7, 2.0), base[3], 0.07),
+                ((1.0, 0.6, 3.0), (2.0, 0.3, 6.0), base[2], (0.0, 1.0, -3.0), 0.11)]
+        fn = models.growth3
+    else:
+        sets = [base, (0.9, 1.4, 0.6, 2.5, 0.8, 0.03), (2.0, 2.0, 0.5, 0.5, 0.1, 0.04)]
+        fn = models.four_split
+    data = np.random.default_rng(3).poisson(50, size=tuple(n + 1 for n in ns)).astype(float)
+    fs, ll, status = batchnd.ModelBatch(kind, pts_l, ns).run(sets, data=data, scale=1e3)
+    assert not status.any()
+    fs, ll = fs.cpu().numpy(), ll.cpu().numpy()
+    f = numerics.make_extrap_func(fn)
+    for k, p in enumerate(sets):
+        ref = f(p, ns, pts_l)
+        assert_fs_parity(fs[k], np.asarray(ref.data))
+        ll_ref = inference.ll(1e3 * ref, spectrum.Spectrum(data))
+        assert abs(ll[k] - ll_ref) <= 1e-9 * abs(ll_ref)
+
+
+def test_model_batch_config2_matches_dadi(cuda_lib, golden):
+    """Config 2 through ModelBatch (a batch of one) against dadi."""
+    from dadi_gb300 import batchnd
+    g = cases.GROWTH3
+    fs, _, status = batchnd.ModelBatch("growth3", g["pts_l"], g["ns"]).run([g["params"]])
+    assert not status.any()
+    assert_fs_parity(fs.cpu().numpy()[0], golden["models"]["growth3_fs"])

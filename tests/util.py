@@ -31,12 +31,16 @@ ALL_CASES = [(g, c) for g, lst in GROUPS for c in lst]
 #: Spectrum parity bar: entries at or above TINY_FRAC of the largest entry
 #: must agree to FS_REL relative error; smaller entries (which arise from
 #: cancellation and carry no likelihood weight) must agree to
-#: FS_REL * TINY_FRAC * max|ref| absolutely.  The reference's own rounding
-#: moves such tiny entries by more than 1e-9 relative (test_oracle.py::
-#: test_reference_noise_floor_tiny_entries), so a relative bar there would
-#: test rounding, not correctness.
+#: FS_REL * TINY_FRAC * max|ref| absolutely.  The level is the reference's
+#: own: over the stratified 64-instance sample of the batched workload,
+#: dadi's arithmetic with the right-hand side rounded as its own
+#: constant-parameter sweeps round it moves entries at or above 1e-9 of the
+#: maximum by at most 7.9e-10 relative, and smaller ones by up to 1.5e-8
+#: relative but at most 6.1e-19 of the maximum absolutely
+#: (test_oracle.py::test_reference_noise_floor_at_scale), so a relative bar
+#: below that level would test rounding, not correctness.
 FS_REL = 1e-9
-TINY_FRAC = 1e-12
+TINY_FRAC = 1e-9
 
 
 def fs_parity(fs, ref):
