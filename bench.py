@@ -750,6 +750,20 @@ def run_profile_kernel(a):
             eng = batch.Batch2D(PTS_L, NS)
             eng.loglik_and_grad(draws[sel], torch.ones(41, 41, dtype=torch.float64,
                                                        device="cuda"), 1.0)
+        elif a.profile == "batchnd":
+            # 48 sets of the three-population growth model at pts 70 as one
+            # batch (132 MB of densities, more than L2)
+            from dadi_gb300 import batchnd
+            sets = growth3_sets(48)
+            tabs, _ = batchnd.schedules([batchnd.growth3_instance(p) for p in sets])
+            eng = batchnd.BatchND(3, 70)
+            eng.integrate(torch.from_numpy(batchnd.initial_density("growth3", 70)).cuda(),
+                          tabs)
+        elif a.profile == "fromphind":
+            # spectra (20,20,20) of 32 three-population densities at pts 90
+            from dadi_gb300 import numerics, spectrum
+            phis = torch.rand(32, 90, 90, 90, dtype=torch.float64, device="cuda")
+            spectrum.from_phi_nd_batch(torch, phis, (20, 20, 20), numerics.default_grid(90))
         elif a.profile == "adjointnd":
             m = adjoint_nd.Growth3((40,), (10, 10, 10))
             th = adjoint_nd.Growth3.from_model_params(models.GROWTH3_DEFAULT)
@@ -794,7 +808,8 @@ def main():
                     help="run only a small batch (this many seed-0 instances with 200-800 "
                          "steps, twice) for profiler captures, then exit")
     ap.add_argument("--profile", default=None,
-                    choices=["epilogue", "sweep3d", "adjoint2d", "adjointnd"],
+                    choices=["epilogue", "sweep3d", "adjoint2d", "adjointnd", "batchnd",
+                             "fromphind"],
                     help="run a small case of another kernel for profiler captures, then exit")
     a = ap.parse_args()
     if a.profile_items:
