@@ -49,7 +49,11 @@ NS = (40, 40)
 NINST = 4096
 BYTES_PER_PS = 16      # algorithmic HBM bytes per point-sweep (phi read + write)
 FLOPS_PER_PS = 30      # algorithmic FP64 flops per point-sweep (reference formulation)
-FP64_INSTR_PER_PS = 10  # FP64 pipe instructions per point-sweep in k_integrate2d
+# FP64 thread instructions per point-sweep in k_integrate2d, from ncu
+# counters (sm__sass_thread_inst_executed_op_fp64_pred_on.sum over the
+# point-sweeps of 1024 seed-0 instances, all three grids): 10.40 (the
+# recurrence's 10 per point plus the per-step vector builds)
+FP64_INSTR_PER_PS = 10.4
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the integration of one
 # full step of this workload, by launch mode: one mixed launch, or the three
 # launches of per_grid (L = 100 with two items per CTA 1.06 + 0.318 GB,
@@ -520,10 +524,10 @@ def run_ours(a, world, rank, local):
                  "pipe_tflops": fp64_instr, "peak_tflops": fp64_peak,
                  "frac": fp64_instr / fp64_peak,
                  "peak_source": "measured in this run (dgb_probe_fp64_fma: FMA chains, "
-                                "4 warps/SM on every SM)",
-                 "note": "pipe_tflops counts %d FP64 instructions (as FMAs) per point-sweep; "
-                         "algorithmic_tflops counts %d reference flops per point-sweep"
-                         % (FP64_INSTR_PER_PS, FLOPS_PER_PS)},
+                                "4 and 8 warps/SM on every SM, ~0.1 s launches, best of 5)",
+                 "note": "pipe_tflops counts %.2f FP64 thread instructions (as FMAs) per "
+                         "point-sweep, measured with ncu counters; algorithmic_tflops counts "
+                         "%d reference flops per point-sweep" % (FP64_INSTR_PER_PS, FLOPS_PER_PS)},
         "kernel_ms_per_step": kmean * 1e3,
         "warmup_ms": warm_ms,
         "clocks": clk,

@@ -219,14 +219,19 @@ __device__ __forceinline__ void nd_tile_io(const NDArgs &A, double *tile, int nt
 {
     const int L = A.L, tp = nt + 1;
     if (A.S == 1) {
-        // contiguous axis: the n lines are n*L consecutive doubles
+        // contiguous axis: the n lines are n*L consecutive doubles; each
+        // warp copies whole lines with its lanes along the line (coalesced,
+        // and no division by L per element)
         double *g0 = A.phi + l0 * L;
-        for (int idx = threadIdx.x; idx < n * L; idx += blockDim.x) {
-            int t = idx / L, p = idx - t * L;
-            if (store)
-                g0[idx] = tile[p * tp + t];
-            else
-                tile[p * tp + t] = g0[idx];
+        const int lane = threadIdx.x & 31, nw = (int)(blockDim.x >> 5);
+        for (int t = (int)(threadIdx.x >> 5); t < n; t += nw) {
+            double *gl = g0 + (size_t)t * L;
+            for (int p = lane; p < L; p += 32) {
+                if (store)
+                    gl[p] = tile[p * tp + t];
+                else
+                    tile[p * tp + t] = gl[p];
+            }
         }
     } else {
         int t = threadIdx.x;

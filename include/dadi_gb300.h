@@ -77,6 +77,10 @@ typedef struct {
                                     work items per CTA on ceil(2L/32) warps), or 64 / 96 /
                                     128 where that many threads hold every line (else
                                     auto), one item per CTA */
+    int line_solver;             /* batched N-dimensional engine: 0 Thomas, one line per
+                                    thread (dadi/tridiag.c:14-34); 1 parallel cyclic
+                                    reduction, one warp per line (L <= 128) */
+    int pad_;
 } dgb_settings;
 
 int dgb_abi_version(void);

@@ -41,7 +41,7 @@ def test_status_strings(lib):
 
 def test_struct_layout():
     assert ctypes.sizeof(_lib.PForm) == 32
-    assert ctypes.sizeof(_lib.Settings) == 32
+    assert ctypes.sizeof(_lib.Settings) == 40
     assert ctypes.sizeof(_lib.Inst2D) == 16 + 9 * 32 + 8
 
 

@@ -116,3 +116,40 @@ def test_model_batch_config2_matches_dadi(cuda_lib, golden):
     fs, _, status = batchnd.ModelBatch("growth3", g["pts_l"], g["ns"]).run([g["params"]])
     assert not status.any()
     assert_fs_parity(fs.cpu().numpy()[0], golden["models"]["growth3_fs"])
+
+
+@pytest.mark.parametrize("P,L", [(3, 20), (3, 33), (4, 12), (1, 100), (2, 128)])
+def test_pcr_line_solver_matches_thomas(cuda_lib, P, L):
+    """The alternative line solver (parallel cyclic reduction, one warp per
+    line) solves the same systems as Thomas: the densities agree to 1e-12
+    relative (a different order of the same arithmetic)."""
+    import torch
+    from dadi_gb300 import batchnd
+    xx = cases.grid("default", L)
+    tables = [table_rows(P, nst, 300 + k) for k, nst in enumerate([9, 4, 9])]
+    masks = [0, 0, 1 << 8]
+    phi0 = np.stack([np.abs(cases.initial_phi(50 + k, (L,) * P)) + 1e-3 for k in range(3)])
+    d0 = torch.from_numpy(phi0).cuda()
+    th = batchnd.BatchND(P, L, xx=xx).integrate(d0, tables, masks).cpu().numpy()
+    pc = batchnd.BatchND(P, L, xx=xx, line_solver=1).integrate(d0, tables, masks)
+    pc = pc.cpu().numpy()
+    for k in range(3):
+        rel = np.max(np.abs(pc[k] - th[k]) / np.maximum(np.abs(th[k]), 1e-12 * np.abs(th[k]).max()))
+        assert rel < 1e-12, (k, rel)
+
+
+def test_pcr_line_solver_config2_matches_dadi(cuda_lib, golden):
+    """Config 2 with the PCR line solver, against dadi."""
+    import torch
+    from dadi_gb300 import batchnd, numerics, spectrum
+    g = cases.GROWTH3
+    tabs, _ = batchnd.schedules([batchnd.growth3_instance(g["params"])])
+    res = []
+    for L in g["pts_l"]:
+        eng = batchnd.BatchND(3, L, line_solver=1)
+        phi = eng.integrate(torch.from_numpy(batchnd.initial_density("growth3", L)).cuda(),
+                            tabs)[0]
+        xx = numerics.default_grid(L)
+        res.append(spectrum.from_phi(phi, g["ns"], (xx, xx, xx)))
+    fs = numerics.extrapolate(res, [r.extrap_x for r in res])
+    assert_fs_parity(np.asarray(fs.data), golden["models"]["growth3_fs"])
