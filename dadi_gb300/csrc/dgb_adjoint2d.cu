@@ -230,15 +230,27 @@ struct ADArgs {
     const int *order;
     int nwork;
     int *counter;
-    double *scratch;      // per CTA: (ckpt_every + 3) * Lmax^2 doubles
+    double *scratch;      // per CTA: (2 * ckpt_every + 3) * Lmax^2 doubles
     int lam_smem;         // the item's adjoint held in shared memory (odd pitch)
     int Lmax;
+};
+
+// Per-interval factors of the contraction for one axis and step:
+// P_i = V_i/(2 dx_i), Q_i = V_{i+1}/(2 dx_i) (with 1/nu), and the
+// derivatives of the selection term with respect to gamma (FG) and h (FH).
+struct ADCVecs {
+    double *P, *Q, *FG, *FH;
 };
 
 struct ADVecs {
     AxisVecs f[2]; // forward coefficient vectors
     AxisVecs t[2]; // transposed (sub/super swapped)
+    ADCVecs c[2];  // contraction factors
 };
+
+// Doubles of shared memory the carve takes (grid constants, the forward,
+// transposed and contraction vectors of both axes).
+constexpr int AD_VEC_DOUBLES = 6 + 2 * 10 + 2 * 4;
 
 struct ADShared {
     AxisScalars ax[2];
@@ -291,6 +303,15 @@ __device__ void ad_step_setup(ADShared &S, ADVecs &V, const GridVecs &g, int L, 
     if (transposed) {
         for (int t = tid; t < 2 * L; t += blockDim.x) {
             int a = t >= L, i = t - a * L;
+            if (i < L - 1) {
+                const double inu = S.ax[a].inv_nu, hh = S.ax[a].h, gam = S.ax[a].gamma;
+                const double xi = g.xInt[i];
+                const double xx1 = xi * (1. - xi);
+                V.c[a].P[i] = inu * g.xv[i] * g.ih[i];
+                V.c[a].Q[i] = inu * g.xv[i + 1] * g.ih[i];
+                V.c[a].FG[i] = 2 * (hh + (1. - 2 * hh) * xi) * xx1;
+                V.c[a].FH[i] = gam * 2 * (1. - 2 * xi) * xx1;
+            }
             V.t[a].A1[i] = (i > 0) ? V.f[a].C1[i - 1] : 0.0;
             V.t[a].A0[i] = (i > 0) ? V.f[a].C0[i - 1] : 0.0;
             V.t[a].C1[i] = (i < L - 1) ? V.f[a].A1[i + 1] : 0.0;
@@ -322,8 +343,8 @@ __device__ void ad_sweep(double *u, double *gam, int L, int a, const AxisVecs &v
 // thread, added into G[Q_DT], G[nu], G[m], G[gamma], G[h] of that axis.
 __device__ void ad_contract(const double *mu, const double *phi, const double *rhs,
                             const double *inj_pts, double inj, int L, int a,
-                            const AxisScalars &s, const GridVecs &g, int j0, int j1, double *G,
-                            int pm = 0)
+                            const AxisScalars &s, const GridVecs &g, const ADCVecs &cv, int j0,
+                            int j1, double *G, int pm = 0)
 {
     // mu has row pitch pm (L when 0); phi and rhs are row-major
     const int sp = (a == 0) ? L : 1, sl = (a == 0) ? 1 : L;
@@ -352,16 +373,12 @@ __device__ void ad_contract(const double *mu, const double *phi, const double *r
             smp = fma(mi, pi, smp);
             if (i < L - 1) {
                 double mn = m[(i + 1) * msp], pn = p[(i + 1) * sp];
-                double xi = g.xInt[i];
-                double Pi = inu * g.xv[i] * g.ih[i];
-                double Qi = inu * g.xv[i + 1] * g.ih[i];
                 double Di = g.dfac[i] * mi - g.dfac[i + 1] * mn;
                 double hp = 0.5 * (pi + pn);
-                double xx1 = xi * (1. - xi);
-                snu = fma(Di, (Qi * pn - Pi * pi) * inu, snu);
-                sm = fma(Di * (o - xi), hp, sm);
-                sg = fma(Di * (2 * (hh + (1. - 2 * hh) * xi) * xx1), hp, sg);
-                sh = fma(Di * (gam * 2 * (1. - 2 * xi) * xx1), hp, sh);
+                snu = fma(Di, (cv.Q[i] * pn - cv.P[i] * pi) * inu, snu);
+                sm = fma(Di * (o - g.xInt[i]), hp, sm);
+                sg = fma(Di * cv.FG[i], hp, sg);
+                sh = fma(Di * cv.FH[i], hp, sh);
                 mi = mn;
                 pi = pn;
             }
@@ -411,6 +428,12 @@ __device__ __forceinline__ void ad_carve(double *smem, int L, GridVecs &g, ADVec
         V.t[a].C0 = p; p += L;
         V.t[a].B0 = p; p += L;
     }
+    for (int a = 0; a < 2; a++) {
+        V.c[a].P = p; p += L;
+        V.c[a].Q = p; p += L;
+        V.c[a].FG = p; p += L;
+        V.c[a].FH = p; p += L;
+    }
 }
 
 __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
@@ -424,10 +447,13 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
     ad_carve(smem, A.Lmax, g, V);
     // the adjoint of the item in shared memory, after the vectors (26 Lmax)
     const int lpitch = (A.Lmax % 2) ? A.Lmax : A.Lmax + 1;
-    double *lam_s = smem + (size_t)26 * A.Lmax;
+    double *lam_s = smem + (size_t)AD_VEC_DOUBLES * A.Lmax;
     const size_t L2max = (size_t)A.Lmax * A.Lmax;
-    double *seg = A.scratch + (size_t)blockIdx.x * (A.ckpt_every + 3) * L2max;
-    double *W1 = seg + (size_t)(A.ckpt_every + 1) * L2max;
+    // per CTA: the segment's densities (C + 1 slots), the x-sweep outputs
+    // chi of its steps (C slots), one spare array and the Thomas scratch
+    double *seg = A.scratch + (size_t)blockIdx.x * (2 * A.ckpt_every + 3) * L2max;
+    double *chis = seg + (size_t)(A.ckpt_every + 1) * L2max;
+    double *W1 = chis + (size_t)A.ckpt_every * L2max;
     double *gam = W1 + L2max;
 
     for (;;) {
@@ -515,10 +541,17 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
                         dst[0 * L + 1] += S.inj;
                 }
                 __syncthreads();
-                for (int a = 0; a < 2; a++) {
-                    if (frozen & (1 << a))
-                        continue;
-                    ad_sweep(dst, gam, L, a, V.f[a], S.ax[a], g, j0, j1);
+                if (!(frozen & 1)) {
+                    ad_sweep(dst, gam, L, 0, V.f[0], S.ax[0], g, j0, j1);
+                    __syncthreads();
+                }
+                // chi_k = X^{-1}(phi_k + inj), kept for the backward step
+                double *chik = chis + (size_t)(k - k0) * LL;
+                for (size_t idx = tid; idx < LL; idx += blockDim.x)
+                    chik[idx] = dst[idx];
+                __syncthreads();
+                if (!(frozen & 2)) {
+                    ad_sweep(dst, gam, L, 1, V.f[1], S.ax[1], g, j0, j1);
                     __syncthreads();
                 }
             }
@@ -527,23 +560,25 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
                 ad_step_setup(S, V, g, L, rows + (size_t)k * 11,
                               drows + (size_t)k * NQ * NPAR, true);
                 const double *phik = seg + (size_t)(k - k0) * LL;
-                // phi_{k+1}: the next slot, or for the segment's last step the
-                // checkpoint of the next segment / the final density, both
-                // recomputed here into W1 after chi is no longer needed.
-                // chi_k = X^{-1}(phi_k + inj) into W1
-                for (size_t idx = tid; idx < LL; idx += blockDim.x)
-                    W1[idx] = phik[idx];
-                __syncthreads();
-                if (tid == 0) {
-                    if (injx)
-                        W1[1 * L + 0] += S.inj;
-                    if (injy)
-                        W1[0 * L + 1] += S.inj;
-                }
-                __syncthreads();
-                if (!(frozen & 1)) {
-                    ad_sweep(W1, gam, L, 0, V.f[0], S.ax[0], g, j0, j1);
+                // chi_k = X^{-1}(phi_k + inj): kept by the recomputation,
+                // except for the segment's last step, formed here in W1
+                const double *chi = chis + (size_t)(k - k0) * LL;
+                if (k == k1 - 1) {
+                    for (size_t idx = tid; idx < LL; idx += blockDim.x)
+                        W1[idx] = phik[idx];
                     __syncthreads();
+                    if (tid == 0) {
+                        if (injx)
+                            W1[1 * L + 0] += S.inj;
+                        if (injy)
+                            W1[0 * L + 1] += S.inj;
+                    }
+                    __syncthreads();
+                    if (!(frozen & 1)) {
+                        ad_sweep(W1, gam, L, 0, V.f[0], S.ax[0], g, j0, j1);
+                        __syncthreads();
+                    }
+                    chi = W1;
                 }
                 double G[NQ];
 #pragma unroll
@@ -565,14 +600,16 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
                 if (!(frozen & 2)) {
                     ad_sweep(lam, gam, L, 1, V.t[1], S.ax[1], g, j0, j1, lp);
                     __syncthreads();
-                    ad_contract(lam, phin, W1, nullptr, 0.0, L, 1, S.ax[1], g, j0, j1, G, lp);
+                    ad_contract(lam, phin, chi, nullptr, 0.0, L, 1, S.ax[1], g, V.c[1], j0, j1,
+                                G, lp);
                     __syncthreads();
                 }
                 // x: nu = X^{-T} mu, contract with chi, rhs psi
                 if (!(frozen & 1)) {
                     ad_sweep(lam, gam, L, 0, V.t[0], S.ax[0], g, j0, j1, lp);
                     __syncthreads();
-                    ad_contract(lam, W1, phik, inj_on, S.inj, L, 0, S.ax[0], g, j0, j1, G, lp);
+                    ad_contract(lam, chi, phik, inj_on, S.inj, L, 0, S.ax[0], g, V.c[0], j0, j1,
+                                G, lp);
                 }
                 // injection: d psi(1,0), psi(0,1) / d(dt, theta0)
                 if (tid == 0) {
@@ -639,7 +676,7 @@ extern "C" int dgb_sched2d_deriv(const dgb_inst2d *insts, const dgb_seed2d *seed
 
 extern "C" size_t dgb_adjoint2d_scratch_bytes(int Lmax, int ckpt_every, int nblocks)
 {
-    return (size_t)nblocks * (ckpt_every + 3) * Lmax * Lmax * sizeof(double);
+    return (size_t)nblocks * (2 * ckpt_every + 3) * Lmax * Lmax * sizeof(double);
 }
 
 extern "C" int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngrids,
@@ -688,13 +725,13 @@ extern "C" int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngr
     if (!ws || ws_bytes < 256)
         return DGB_ERR_WORKSPACE;
     A.counter = (int *)ws;
-    size_t per_cta = (size_t)(ckpt_every + 3) * Lmax * Lmax * sizeof(double);
+    const size_t per_cta = dgb_adjoint2d_scratch_bytes(Lmax, ckpt_every, 1);
     long nblocks = (long)((ws_bytes - 256) / per_cta);
     if (nblocks < 1)
         return DGB_ERR_WORKSPACE;
     nblocks = std::min<long>(nblocks, A.nwork);
     A.scratch = (double *)((char *)ws + 256);
-    size_t smem = (size_t)26 * Lmax * sizeof(double);
+    size_t smem = (size_t)AD_VEC_DOUBLES * Lmax * sizeof(double);
     {
         // the adjoint in shared memory when vectors + Lmax x odd pitch fit
         int dev = 0, optin = 0;

@@ -316,6 +316,9 @@ __global__ void __launch_bounds__(K2_THREADS) k_integrate2d(K2Args A)
 // delta_j only), so the results are bitwise the same.  Thomas scratch: a 2L x L slice of the
 // workspace per CTA (element p of line q at gam[p*2L + q]).
 constexpr int K2P_MAXTHREADS = 256;
+// dgb_settings.threads value: two work items per CTA at any grid size where
+// that fills the warps better (the automatic choice keeps it to L > 96)
+constexpr int K2_PAIR_ANY_L = -2;
 
 struct K2PairShared {
     AxisScalars ax[2][2]; // [item slot][axis]
@@ -667,9 +670,13 @@ static int k2_pair_occupancy(size_t smem, int threads)
 // Threads of a two-item CTA for grids of L points when pairing pays: one
 // grid of 97-128 points (a single item needs four warps there) whose 2L
 // lines fill their warps at least 5 % better than L lines fill four; else 0.
-static int k2_pair_threads(int L)
+// Threads of a two-item CTA for grids of L points, or 0 where one item per
+// CTA is kept: pairs only when they fill the warps' lanes at least 5 points
+// better, and (unless any_L) only for L > 96, where one item per CTA already
+// needs four warps.
+static int k2_pair_threads(int L, bool any_L = false)
 {
-    if (L <= 96 || L > K2P_MAXTHREADS / 2)
+    if ((!any_L && L <= 96) || L > K2P_MAXTHREADS / 2)
         return 0;
     const int w1 = (L + 31) / 32, w2 = (2 * L + 31) / 32;
     const double f1 = (double)L / (32 * w1), f2 = (double)(2 * L) / (32 * w2);
@@ -698,7 +705,7 @@ static int k2_num_sms()
 static int k2_pick_threads(const dgb_settings *settings, bool delj, size_t smem, int Lmax,
                            int &occ)
 {
-    const int want = settings->threads;
+    const int want = (settings->threads == K2_PAIR_ANY_L) ? 0 : settings->threads;
     if (want != 0 && want != 64 && want != 96 && want != 128)
         return 0;
     int warps = std::min(4, std::max(2, (Lmax + 31) / 32));
@@ -831,10 +838,11 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     // automatic thread count, no checkpoints, scratch in the workspace; the
     // two-item kernel implements the default delta_j only, so the delj
     // trick keeps one item per CTA)
-    const int pthreads =
-        (ngrids == 1 && !ckpt && !use_s && settings->threads == 0 && !A.use_delj)
-            ? k2_pair_threads(Lmax)
-            : 0;
+    const bool any_L = settings->threads == K2_PAIR_ANY_L;
+    const int pthreads = (ngrids == 1 && !ckpt && !use_s && (settings->threads == 0 || any_L) &&
+                          !A.use_delj)
+                             ? k2_pair_threads(Lmax, any_L)
+                             : 0;
     if (pthreads) {
         const size_t pbytes = k2_pair_doubles(Lmax) * sizeof(double);
         int dev = 0, optin = 0;

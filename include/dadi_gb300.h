@@ -76,7 +76,9 @@ typedef struct {
                                     lane; for a launch over one grid of 97-128 points, two
                                     work items per CTA on ceil(2L/32) warps), or 64 / 96 /
                                     128 where that many threads hold every line (else
-                                    auto), one item per CTA */
+                                    auto), one item per CTA, or -2: as auto but with two
+                                    items per CTA at any L where that fills the warps'
+                                    lanes better */
     int line_solver;             /* batched N-dimensional engine: 0 Thomas, one line per
                                     thread (dadi/tridiag.c:14-34); 1 parallel cyclic
                                     reduction, one warp per line (L <= 128) */
