@@ -35,7 +35,8 @@ EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
            "dgb_from_phi2d", "dgb_extrap_ll", "dgb_integrate_table_states",
            "dgb_adjoint_table_nd_gpart_doubles", "dgb_adjoint_table_nd",
            "dgb_batchnd_workspace_bytes", "dgb_batchnd_integrate", "dgb_schednd_host",
-           "dgb_from_phi_nd_workspace_bytes", "dgb_from_phi_nd"]
+           "dgb_from_phi_nd_workspace_bytes", "dgb_from_phi_nd", "dgb_adjoint2d_traj_ws_bytes",
+           "dgb_adjoint2d_traj"]
 
 
 class PForm(ctypes.Structure):
@@ -123,6 +124,10 @@ def _declare(L):
         "dgb_schednd_host": (i, [_vp, i, ctypes.POINTER(Settings), lg, d, _vp, _vp, _vp, _vp]),
         "dgb_from_phi_nd_workspace_bytes": (sz, [i, i, _vp, i]),
         "dgb_from_phi_nd": (i, [_vp, i, i, i, _vp, _vp, _vp, _vp, _vp, _vp, sz, _vp]),
+        "dgb_adjoint2d_traj_ws_bytes": (sz, [i, i]),
+        "dgb_adjoint2d_traj": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp,
+                                   _vp, _vp, _vp, i, _vp, _vp, _vp, _vp, _vp, _vp,
+                                   ctypes.POINTER(Settings), _vp, sz, _vp]),
         "dgb_adjoint2d": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp, _vp,
                               _vp, _vp, i, _vp, _vp, _vp, ctypes.POINTER(Settings), _vp, sz,
                               _vp]),

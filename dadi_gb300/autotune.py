@@ -8,7 +8,8 @@ The knobs, each a real alternative the kernels implement:
   launches share SMs);
 * ... or "per_grid": one persistent launch per grid size, each shaped for
   its own L (CTAs per SM, warps per CTA, two work items per CTA for a grid
-  of 97-128 points), on side streams so that one launch's tail overlaps the
+  of 73-128 points where that fills the lanes better), on side streams so
+  that one launch's tail overlaps the
   next;
 * gam placement — the Thomas recurrence's scratch in shared memory (fewer
   CTAs per SM when the density already fills it) or in a per-CTA slice of

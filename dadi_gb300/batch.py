@@ -433,7 +433,7 @@ class Batch2D:
         return phis, status
 
     def loglik_and_grad(self, params, data, scale=1.0, ckpt_every=None, seeds=None, rec=None,
-                        mask=None, multinom=False):
+                        mask=None, multinom=False, trajectory=None):
         """Poisson log-likelihood of scale * (extrapolated IM spectrum) against
         data for each parameter row (or its multinomial form, see loglik), and
         its gradient with respect to (s, nu1, nu2, T, m12, m21) by the
@@ -441,7 +441,7 @@ class Batch2D:
         status (n,))."""
         ll, ctx = self.forward_for_adjoint(params, data, scale, ckpt_every, seeds, rec,
                                            mask=mask, multinom=multinom)
-        grad = self.adjoint(ctx, self.torch.ones_like(ll))
+        grad = self.adjoint(ctx, self.torch.ones_like(ll), trajectory=trajectory)
         return ll.detach(), grad, ctx["status"]
 
     def forward_for_adjoint(self, params, data, scale=1.0, ckpt_every=None, seeds=None,
@@ -515,8 +515,33 @@ class Batch2D:
                    ck_off=ck_off, C=C, masks=d_masks, order=d_order, status=status, n=n, st=st)
         return ll, ctx
 
-    def adjoint(self, ctx, grad_ll):
-        """d(sum_i grad_ll[i] * ll_i)/d(params) by the discrete adjoint: (n, 6)."""
+    #: Largest trajectory (bytes) the adjoint stores so that every checkpoint
+    #: segment is recomputed at once (dgb_adjoint2d_traj); beyond it each
+    #: work item's CTA recomputes its segments in turn (dgb_adjoint2d).
+    traj_budget = 24 << 30
+
+    def trajectory_bytes(self, ctx):
+        """Bytes of the adjoint's full trajectory for a forward context:
+        per work item (2 n + 1) L^2 doubles (every density and x-sweep
+        output of its n steps)."""
+        steps = self._work_steps(ctx)
+        Lsq = np.array([L * L for L in self.pts_l], dtype=np.int64)
+        return int(8 * np.sum((2 * steps + 1) * Lsq[None, :]))
+
+    def _work_steps(self, ctx):
+        """Steps of each (instance, grid) work item, (n, ngrids), host."""
+        n, ng = ctx["n"], len(self.pts_l)
+        cnt = _lib.to_host(self.torch, ctx["cnt"]).astype(np.int64)
+        if ctx["st"].use_old_timestep:      # one schedule per work item
+            return cnt.reshape(n, ng)
+        return np.repeat(cnt.reshape(n, 1), ng, axis=1)
+
+    def adjoint(self, ctx, grad_ll, trajectory=None):
+        """d(sum_i grad_ll[i] * ll_i)/d(params) by the discrete adjoint: (n, 6).
+        trajectory: recompute every checkpoint segment at once into a stored
+        trajectory first (True), each work item's segments in turn (False),
+        or the first when it fits traj_budget (None); the gradients are the
+        same bit for bit."""
         torch = self.torch
         lib = _lib.lib()
         phis = ctx["phis"]
@@ -528,7 +553,6 @@ class Batch2D:
         part = torch.empty(n, ng, 6, dtype=torch.float64, device="cuda")
         C = ctx["C"]
         Lmax = max(self.pts_l)
-        per_cta = lib.dgb_adjoint2d_scratch_bytes(Lmax, C, 1)
         props = torch.cuda.get_device_properties(torch.cuda.current_device())
         nsm = props.multi_processor_count
         per_sm = self.adjoint_ctas_per_sm
@@ -541,14 +565,36 @@ class Batch2D:
             per_sm = int(0.75 * l2 // (nsm * 5 * Lmax * Lmax * 8))
             per_sm = max(1, min(4, per_sm))
         nblocks = min(n * ng, nsm * per_sm)
-        ws, nws = _lib.workspace(torch, 256 + per_cta * nblocks)
         st = ctx["st"]
-        _lib.check(lib.dgb_adjoint2d(
-            _lib.dptr(ctx["masks"]), n, self.Ls, ng, _lib.dptr(self.d_xx), _lib.dptr(ctx["table"]),
-            _lib.dptr(ctx["drows"]), _lib.dptr(ctx["off"]), _lib.dptr(ctx["cnt"]),
-            _lib.dptr(ctx["ckpt"]), _lib.dptr(ctx["ck_off"]), C, _lib.dptr(lam), _lib.dptr(part),
-            _lib.dptr(ctx["order"]), ctypes.byref(st), _lib.dptr(ws), nws,
-            _lib.stream_handle(torch)), "dgb_adjoint2d")
+        if trajectory is None:
+            trajectory = self.trajectory_bytes(ctx) <= self.traj_budget
+        common = (_lib.dptr(ctx["masks"]), n, self.Ls, ng, _lib.dptr(self.d_xx),
+                  _lib.dptr(ctx["table"]), _lib.dptr(ctx["drows"]), _lib.dptr(ctx["off"]),
+                  _lib.dptr(ctx["cnt"]), _lib.dptr(ctx["ckpt"]), _lib.dptr(ctx["ck_off"]), C)
+        if trajectory:
+            steps = self._work_steps(ctx).reshape(-1)
+            Lsq = np.tile(np.array([L * L for L in self.pts_l], dtype=np.int64), n)
+            size = (2 * steps + 1) * Lsq
+            t_off = np.zeros(n * ng, dtype=np.int64)
+            np.cumsum(size[:-1], out=t_off[1:])
+            seg_off = np.zeros(n * ng + 1, dtype=np.int64)
+            np.cumsum((steps + C - 1) // C, out=seg_off[1:])
+            traj = torch.empty(max(int(size.sum()), 1), dtype=torch.float64, device="cuda")
+            d_toff = _lib.to_device(torch, t_off, np.int64)
+            d_soff = _lib.to_device(torch, seg_off, np.int64)
+            ws, nws = _lib.workspace(torch, lib.dgb_adjoint2d_traj_ws_bytes(
+                Lmax, max(nblocks, 2 * nsm)))
+            _lib.check(lib.dgb_adjoint2d_traj(
+                *common, _lib.dptr(traj), _lib.dptr(d_toff), _lib.dptr(d_soff), _lib.dptr(lam),
+                _lib.dptr(part), _lib.dptr(ctx["order"]), ctypes.byref(st), _lib.dptr(ws), nws,
+                _lib.stream_handle(torch)), "dgb_adjoint2d_traj")
+        else:
+            per_cta = lib.dgb_adjoint2d_scratch_bytes(Lmax, C, 1)
+            ws, nws = _lib.workspace(torch, 256 + per_cta * nblocks)
+            _lib.check(lib.dgb_adjoint2d(
+                *common, _lib.dptr(lam), _lib.dptr(part), _lib.dptr(ctx["order"]),
+                ctypes.byref(st), _lib.dptr(ws), nws, _lib.stream_handle(torch)),
+                "dgb_adjoint2d")
         grad = part[:, 0].clone()
         for gi in range(1, ng):
             grad += part[:, gi]

@@ -233,6 +233,11 @@ struct ADArgs {
     double *scratch;      // per CTA: (2 * ckpt_every + 3) * Lmax^2 doubles
     int lam_smem;         // the item's adjoint held in shared memory (odd pitch)
     int Lmax;
+    // trajectory mode (null: segments recomputed by each work item's CTA):
+    // for work item w, traj + traj_off[w] holds phi_0..phi_n then
+    // chi_0..chi_{n-1}, (2n + 1) L^2 doubles, filled by k_adjoint2d_traj
+    double *traj;
+    const long *traj_off;
 };
 
 // Per-interval factors of the contraction for one axis and step:
@@ -436,6 +441,7 @@ __device__ __forceinline__ void ad_carve(double *smem, int L, GridVecs &g, ADVec
     }
 }
 
+template <bool TRAJ>
 __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
 {
     extern __shared__ __align__(16) double smem[];
@@ -450,11 +456,17 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
     double *lam_s = smem + (size_t)AD_VEC_DOUBLES * A.Lmax;
     const size_t L2max = (size_t)A.Lmax * A.Lmax;
     // per CTA: the segment's densities (C + 1 slots), the x-sweep outputs
-    // chi of its steps (C slots), one spare array and the Thomas scratch
-    double *seg = A.scratch + (size_t)blockIdx.x * (2 * A.ckpt_every + 3) * L2max;
-    double *chis = seg + (size_t)(A.ckpt_every + 1) * L2max;
-    double *W1 = chis + (size_t)A.ckpt_every * L2max;
-    double *gam = W1 + L2max;
+    // chi of its steps (C slots), one spare array and the Thomas scratch;
+    // in trajectory mode only the Thomas scratch (L^2 doubles)
+    double *seg = nullptr, *chis = nullptr, *W1 = nullptr, *gam;
+    if (TRAJ) {
+        gam = A.scratch + (size_t)blockIdx.x * L2max;
+    } else {
+        seg = A.scratch + (size_t)blockIdx.x * (2 * A.ckpt_every + 3) * L2max;
+        chis = seg + (size_t)(A.ckpt_every + 1) * L2max;
+        W1 = chis + (size_t)A.ckpt_every * L2max;
+        gam = W1 + L2max;
+    }
 
     for (;;) {
         if (tid == 0)
@@ -521,14 +533,22 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
             acc[p] = 0;
         const double inj_on[2] = {injx ? 1.0 : 0.0, injy ? 1.0 : 0.0};
 
-        const int nseg = (n + C - 1) / C;
+        // trajectory mode: the whole walk is one segment whose densities and
+        // chi were recomputed beforehand (k_adjoint2d_traj)
+        constexpr bool traj = TRAJ;
+        double *tphi = traj ? A.traj + A.traj_off[wid] : nullptr;
+        double *tchi = traj ? tphi + (size_t)(n + 1) * LL : nullptr;
+        const int nseg = traj ? (n > 0 ? 1 : 0) : (n + C - 1) / C;
         for (int sgi = nseg - 1; sgi >= 0; sgi--) {
-            const int k0 = sgi * C, k1 = min(k0 + C, n);
-            for (size_t idx = tid; idx < LL; idx += blockDim.x)
-                seg[idx] = ck[(size_t)sgi * LL + idx];
+            const int k0 = traj ? 0 : sgi * C, k1 = traj ? n : min(k0 + C, n);
+            double *sphi = traj ? tphi : seg, *schi = traj ? tchi : chis;
+            if (!traj) {
+                for (size_t idx = tid; idx < LL; idx += blockDim.x)
+                    seg[idx] = ck[(size_t)sgi * LL + idx];
+            }
             __syncthreads();
             // recompute phi_{k0+1} .. phi_{k1} into seg slots 1 .. k1-k0
-            for (int k = k0; k < k1 - 1; k++) {
+            for (int k = k0; k < (traj ? k0 : k1 - 1); k++) {
                 ad_step_setup(S, V, g, L, rows + (size_t)k * 11, nullptr, false);
                 double *src = seg + (size_t)(k - k0) * LL, *dst = src + LL;
                 for (size_t idx = tid; idx < LL; idx += blockDim.x)
@@ -559,11 +579,11 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
             for (int k = k1 - 1; k >= k0; k--) {
                 ad_step_setup(S, V, g, L, rows + (size_t)k * 11,
                               drows + (size_t)k * NQ * NPAR, true);
-                const double *phik = seg + (size_t)(k - k0) * LL;
+                const double *phik = sphi + (size_t)(k - k0) * LL;
                 // chi_k = X^{-1}(phi_k + inj): kept by the recomputation,
                 // except for the segment's last step, formed here in W1
-                const double *chi = chis + (size_t)(k - k0) * LL;
-                if (k == k1 - 1) {
+                const double *chi = schi + (size_t)(k - k0) * LL;
+                if (k == k1 - 1 && !traj) {
                     for (size_t idx = tid; idx < LL; idx += blockDim.x)
                         W1[idx] = phik[idx];
                     __syncthreads();
@@ -586,8 +606,8 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
                     G[q] = 0;
                 // phi_{k+1} = Y^{-1} chi: slot k-k0+1 holds it unless k is the
                 // segment's last step; then recompute it in the spare slot.
-                double *phin = seg + (size_t)(k - k0 + 1) * LL;
-                if (k == k1 - 1) {
+                double *phin = sphi + (size_t)(k - k0 + 1) * LL;
+                if (k == k1 - 1 && !traj) {
                     for (size_t idx = tid; idx < LL; idx += blockDim.x)
                         phin[idx] = W1[idx];
                     __syncthreads();
@@ -655,6 +675,114 @@ __global__ void __launch_bounds__(AD_THREADS) k_adjoint2d(ADArgs A)
     }
 }
 
+
+// Trajectory recomputation for the adjoint: one CTA per (work item,
+// checkpoint segment), all segments at once in a grid-stride loop, instead
+// of each work item's CTA recomputing its segments one after another before
+// walking them back.  Segment s of item w starts from its checkpoint
+// (phi_{sC}) and writes phi_{k+1} and chi_k = X^{-1}(phi_k + inj) for its
+// steps into the item's trajectory; phi at a segment boundary is written by
+// the next segment's CTA (its checkpoint), so no slot has two writers.  The
+// steps use ad_step_setup and ad_sweep as k_adjoint2d's own recomputation
+// does, so the trajectory is bitwise what it would recompute.
+__global__ void __launch_bounds__(AD_THREADS) k_adjoint2d_traj(ADArgs A, const long *seg_off)
+{
+    extern __shared__ __align__(16) double smem[];
+    __shared__ ADShared S;
+    const int tid = threadIdx.x;
+    GridVecs g;
+    ADVecs V;
+    ad_carve(smem, A.Lmax, g, V);
+    const size_t L2max = (size_t)A.Lmax * A.Lmax;
+    double *gam = A.scratch + (size_t)blockIdx.x * L2max;
+    const long total = seg_off[A.nwork];
+    const int C = A.ckpt_every;
+    for (long gs = blockIdx.x; gs < total; gs += gridDim.x) {
+        int lo = 0, hi = A.nwork; // seg_off[lo] <= gs < seg_off[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (seg_off[mid] <= gs)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        const int wid = lo;
+        const int sgi = (int)(gs - seg_off[wid]);
+        const int inst = wid / A.ngrids;
+        const int gi = wid - inst * A.ngrids;
+        const int L = A.L[gi];
+        const size_t LL = (size_t)L * L;
+        const double *xx = A.xx_all + A.xx_off[gi];
+        const int sidx = A.sched_per_grid ? wid : inst;
+        const double *rows = A.table + A.row_off[sidx] * 11;
+        const int n = A.row_cnt[sidx];
+        const double *ck = A.ckpt + A.ckpt_off[wid];
+        const int frozen = A.masks ? (A.masks[inst] & 0xff) : 0;
+        const int nomut = A.masks ? (A.masks[inst] >> 8 & 0xff) : 0;
+        const bool injx = !(frozen & 1) && !(nomut & 1), injy = !(frozen & 2) && !(nomut & 2);
+        double *tphi = A.traj + A.traj_off[wid];
+        double *tchi = tphi + (size_t)(n + 1) * LL;
+        for (int i = tid; i < L; i += blockDim.x) {
+            double x = xx[i];
+            g.x[i] = x;
+            g.xv[i] = x * (1. - x);
+            if (i < L - 1) {
+                double d = xx[i + 1] - x;
+                g.dx[i] = d;
+                g.ih[i] = 1.0 / (2 * d);
+                g.xInt[i] = 0.5 * (xx[i + 1] + x);
+            }
+        }
+        __syncthreads();
+        for (int i = tid; i < L; i += blockDim.x) {
+            if (i == 0)
+                g.dfac[i] = 2. / g.dx[0];
+            else if (i == L - 1)
+                g.dfac[i] = 2. / g.dx[L - 2];
+            else
+                g.dfac[i] = 2. / (g.dx[i] + g.dx[i - 1]);
+        }
+        __syncthreads();
+        const int j0 = (g.x[0] == 0.0) ? 0 : -1;
+        const int j1 = (g.x[L - 1] == 1.0) ? L - 1 : -1;
+        const int k0 = sgi * C, k1 = min(k0 + C, n);
+        for (size_t idx = tid; idx < LL; idx += blockDim.x)
+            tphi[(size_t)k0 * LL + idx] = ck[(size_t)sgi * LL + idx];
+        __syncthreads();
+        for (int k = k0; k < k1; k++) {
+            ad_step_setup(S, V, g, L, rows + (size_t)k * 11, nullptr, false);
+            const double *src = tphi + (size_t)k * LL;
+            double *chik = tchi + (size_t)k * LL;
+            for (size_t idx = tid; idx < LL; idx += blockDim.x)
+                chik[idx] = src[idx];
+            __syncthreads();
+            if (tid == 0) {
+                if (injx)
+                    chik[1 * L + 0] += S.inj;
+                if (injy)
+                    chik[0 * L + 1] += S.inj;
+            }
+            __syncthreads();
+            if (!(frozen & 1)) {
+                ad_sweep(chik, gam, L, 0, V.f[0], S.ax[0], g, j0, j1);
+                __syncthreads();
+            }
+            // phi_{k+1}, except at a segment boundary (the next CTA's checkpoint)
+            if (k < k1 - 1 || k1 == n) {
+                double *dst = tphi + (size_t)(k + 1) * LL;
+                for (size_t idx = tid; idx < LL; idx += blockDim.x)
+                    dst[idx] = chik[idx];
+                __syncthreads();
+                if (!(frozen & 2)) {
+                    ad_sweep(dst, gam, L, 1, V.f[1], S.ax[1], g, j0, j1);
+                    __syncthreads();
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 } // namespace dgb
 
 // ------------------------------------------------------------------ C ABI
@@ -679,12 +807,13 @@ extern "C" size_t dgb_adjoint2d_scratch_bytes(int Lmax, int ckpt_every, int nblo
     return (size_t)nblocks * (2 * ckpt_every + 3) * Lmax * Lmax * sizeof(double);
 }
 
-extern "C" int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngrids,
-                             const double *xx_all, const double *table, const double *drows,
-                             const long *row_off, const int *row_cnt, const double *ckpt,
-                             const long *ckpt_off, int ckpt_every, double *lam, double *grad,
-                             const int *order, const dgb_settings *settings, void *ws,
-                             size_t ws_bytes, void *stream)
+static int adjoint2d_run(const int *masks, int ninst, const int *Ls, int ngrids,
+                         const double *xx_all, const double *table, const double *drows,
+                         const long *row_off, const int *row_cnt, const double *ckpt,
+                         const long *ckpt_off, int ckpt_every, double *lam, double *grad,
+                         const int *order, const dgb_settings *settings, double *traj,
+                         const long *traj_off, const long *seg_off, void *ws, size_t ws_bytes,
+                         void *stream)
 {
     using namespace dgb;
     if (!Ls || !xx_all || !table || !drows || !row_off || !row_cnt || !ckpt || !ckpt_off ||
@@ -725,7 +854,11 @@ extern "C" int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngr
     if (!ws || ws_bytes < 256)
         return DGB_ERR_WORKSPACE;
     A.counter = (int *)ws;
-    const size_t per_cta = dgb_adjoint2d_scratch_bytes(Lmax, ckpt_every, 1);
+    A.traj = traj;
+    A.traj_off = traj_off;
+    // per CTA: the segment buffers, or in trajectory mode the Thomas scratch
+    const size_t per_cta = traj ? (size_t)Lmax * Lmax * sizeof(double)
+                                : dgb_adjoint2d_scratch_bytes(Lmax, ckpt_every, 1);
     long nblocks = (long)((ws_bytes - 256) / per_cta);
     if (nblocks < 1)
         return DGB_ERR_WORKSPACE;
@@ -744,10 +877,61 @@ extern "C" int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngr
             smem = with_lam;
         }
     }
-    if (raise_smem_limit(k_adjoint2d))
+    if (traj ? raise_smem_limit(k_adjoint2d<true>) : raise_smem_limit(k_adjoint2d<false>))
         return DGB_ERR_CUDA;
+    if (traj) {
+        // every checkpoint segment at once, on as many CTAs as the
+        // workspace holds Thomas scratch for (at most two per SM)
+        const size_t rsmem = (size_t)AD_VEC_DOUBLES * Lmax * sizeof(double);
+        if (raise_smem_limit(k_adjoint2d_traj))
+            return DGB_ERR_CUDA;
+        int dev = 0, nsm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        const long rblocks = std::min<long>((long)((ws_bytes - 256) / per_cta), 2L * nsm);
+        k_adjoint2d_traj<<<(unsigned)rblocks, AD_THREADS, rsmem, (cudaStream_t)stream>>>(
+            A, seg_off);
+        if (cudaGetLastError() != cudaSuccess)
+            return DGB_ERR_CUDA;
+    }
     if (cudaMemsetAsync(A.counter, 0, sizeof(int), (cudaStream_t)stream) != cudaSuccess)
         return DGB_ERR_CUDA;
-    k_adjoint2d<<<(unsigned)nblocks, AD_THREADS, smem, (cudaStream_t)stream>>>(A);
+    if (traj)
+        k_adjoint2d<true><<<(unsigned)nblocks, AD_THREADS, smem, (cudaStream_t)stream>>>(A);
+    else
+        k_adjoint2d<false><<<(unsigned)nblocks, AD_THREADS, smem, (cudaStream_t)stream>>>(A);
     return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
+}
+
+extern "C" int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngrids,
+                             const double *xx_all, const double *table, const double *drows,
+                             const long *row_off, const int *row_cnt, const double *ckpt,
+                             const long *ckpt_off, int ckpt_every, double *lam, double *grad,
+                             const int *order, const dgb_settings *settings, void *ws,
+                             size_t ws_bytes, void *stream)
+{
+    return adjoint2d_run(masks, ninst, Ls, ngrids, xx_all, table, drows, row_off, row_cnt, ckpt,
+                         ckpt_off, ckpt_every, lam, grad, order, settings, nullptr, nullptr,
+                         nullptr, ws, ws_bytes, stream);
+}
+
+extern "C" size_t dgb_adjoint2d_traj_ws_bytes(int Lmax, int nblocks)
+{
+    return 256 + (size_t)nblocks * Lmax * Lmax * sizeof(double);
+}
+
+extern "C" int dgb_adjoint2d_traj(const int *masks, int ninst, const int *Ls, int ngrids,
+                                  const double *xx_all, const double *table,
+                                  const double *drows, const long *row_off, const int *row_cnt,
+                                  const double *ckpt, const long *ckpt_off, int ckpt_every,
+                                  double *traj, const long *traj_off, const long *seg_off,
+                                  double *lam, double *grad, const int *order,
+                                  const dgb_settings *settings, void *ws, size_t ws_bytes,
+                                  void *stream)
+{
+    if (!traj || !traj_off || !seg_off)
+        return DGB_ERR_ARG;
+    return adjoint2d_run(masks, ninst, Ls, ngrids, xx_all, table, drows, row_off, row_cnt, ckpt,
+                         ckpt_off, ckpt_every, lam, grad, order, settings, traj, traj_off,
+                         seg_off, ws, ws_bytes, stream);
 }

@@ -672,11 +672,14 @@ static int k2_pair_occupancy(size_t smem, int threads)
 // lines fill their warps at least 5 % better than L lines fill four; else 0.
 // Threads of a two-item CTA for grids of L points, or 0 where one item per
 // CTA is kept: pairs only when they fill the warps' lanes at least 5 points
-// better, and (unless any_L) only for L > 96, where one item per CTA already
-// needs four warps.
+// better, and (unless any_L) only for L > 72.  Measured on the 4096-instance
+// IM batch: at L = 100 (200 lines on 7 warps against 100 on 4) the launch
+// went from 4977 to 4590 ms, at L = 80 (160 lines on 5 warps against 80 on
+// 3, one CTA per SM instead of three) the step's integration from 11.30 to
+// 11.00 s; at L = 90 pairs fill the lanes no better (180 of 192).
 static int k2_pair_threads(int L, bool any_L = false)
 {
-    if ((!any_L && L <= 96) || L > K2P_MAXTHREADS / 2)
+    if ((!any_L && L <= 72) || L > K2P_MAXTHREADS / 2)
         return 0;
     const int w1 = (L + 31) / 32, w2 = (2 * L + 31) / 32;
     const double f1 = (double)L / (32 * w1), f2 = (double)(2 * L) / (32 * w2);

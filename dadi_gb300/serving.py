@@ -160,8 +160,10 @@ class Server:
         rows = steps * 11 * 8
         extra = 0
         if req.want_grad:
+            # checkpoints, derivative rows and the adjoint's stored trajectory
             C = max(8, int(np.ceil(np.sqrt(max(steps, 1)))))
             extra = sum(8 * L * L * ((steps + C - 1) // C) for L in req.pts_l) + steps * 60 * 8
+            extra += sum(8 * L * L * (2 * steps + 1) for L in req.pts_l)
         return dens * 2 + rows + extra
 
     def _steps(self, req):

@@ -73,8 +73,9 @@ typedef struct {
     int gam_placement;           /* batched engine: 0 auto, 1 shared memory, 2 workspace */
     int threads;                 /* batched engine: threads per CTA, 0 auto (the fewest
                                     warps, 2-4, that give every line of the largest grid a
-                                    lane; for a launch over one grid of 97-128 points, two
-                                    work items per CTA on ceil(2L/32) warps), or 64 / 96 /
+                                    lane; for a launch over one grid of 73-128 points, two
+                                    work items per CTA on ceil(2L/32) warps where that fills
+                                    the lanes better), or 64 / 96 /
                                     128 where that many threads hold every line (else
                                     auto), one item per CTA, or -2: as auto but with two
                                     items per CTA at any L where that fills the warps'
@@ -239,6 +240,24 @@ int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngrids, const 
                   const int *row_cnt, const double *ckpt, const long *ckpt_off, int ckpt_every,
                   double *lam, double *grad, const int *order, const dgb_settings *settings,
                   void *ws, size_t ws_bytes, void *stream);
+
+/* dgb_adjoint2d with every checkpoint segment of every work item recomputed
+ * at once, one CTA per (work item, segment), before the backward walks: a
+ * long integration's recomputation no longer runs serially on its own
+ * CTA.  traj (device) holds, for work item w at traj_off[w], the densities
+ * phi_0..phi_n followed by the x-sweep outputs chi_0..chi_{n-1}
+ * ((2 n_w + 1) L_g^2 doubles, n_w its steps); seg_off (device, nwork + 1
+ * longs) is the exclusive scan of each work item's segment count
+ * ceil(n_w / ckpt_every).  ws: dgb_adjoint2d_traj_ws_bytes(Lmax, nblocks)
+ * for nblocks CTAs.  The same arithmetic as dgb_adjoint2d, so the same
+ * gradients bit for bit. */
+size_t dgb_adjoint2d_traj_ws_bytes(int Lmax, int nblocks);
+int dgb_adjoint2d_traj(const int *masks, int ninst, const int *Ls, int ngrids,
+                       const double *xx_all, const double *table, const double *drows,
+                       const long *row_off, const int *row_cnt, const double *ckpt,
+                       const long *ckpt_off, int ckpt_every, double *traj, const long *traj_off,
+                       const long *seg_off, double *lam, double *grad, const int *order,
+                       const dgb_settings *settings, void *ws, size_t ws_bytes, void *stream);
 
 /* One work item of dgb_items2d_integrate: a 2-D integration on grid
  * xx_all[xx_off .. xx_off+L) whose density sits at phi_out + out_off (initial

@@ -111,3 +111,22 @@ def test_autograd_function(cuda_lib, golden):
     ll.sum().backward()
     _, direct, _ = eng.loglik_and_grad(g["grad_p0"][None, :], g["grad_data"], scale=1e4)
     assert _close(p.grad.numpy()[0], direct.cpu().numpy()[0]) < 1e-12
+
+
+def test_adjoint_trajectory_mode_is_bitwise(cuda_lib, golden):
+    """Recomputing every checkpoint segment at once into a stored trajectory
+    (dgb_adjoint2d_traj) gives the gradients of the segment-by-segment
+    adjoint bit for bit, for sets with different step counts and a
+    checkpoint interval that leaves a partial last segment."""
+    from dadi_gb300 import batch
+    draws = cases.im_draws(4096)
+    steps = batch.count_steps(batch.im_instances(draws))
+    sel = [i for i in range(64) if 30 <= steps[i] <= 1500][:5]
+    data = golden["grad"]["grad_data"]
+    eng = _engine()
+    for C in (None, 7):
+        _, g_seg, _ = eng.loglik_and_grad(draws[sel], data, scale=1e4, ckpt_every=C,
+                                          trajectory=False)
+        _, g_traj, _ = eng.loglik_and_grad(draws[sel], data, scale=1e4, ckpt_every=C,
+                                           trajectory=True)
+        assert np.array_equal(g_seg.cpu().numpy(), g_traj.cpu().numpy()), C
