@@ -36,7 +36,7 @@ EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
            "dgb_adjoint_table_nd_gpart_doubles", "dgb_adjoint_table_nd",
            "dgb_batchnd_workspace_bytes", "dgb_batchnd_integrate", "dgb_schednd_host",
            "dgb_from_phi_nd_workspace_bytes", "dgb_from_phi_nd", "dgb_adjoint2d_traj_ws_bytes",
-           "dgb_adjoint2d_traj"]
+           "dgb_adjoint2d_traj", "dgb_schednd_dual_host"]
 
 
 class PForm(ctypes.Structure):
@@ -56,6 +56,17 @@ class InstND(ctypes.Structure):
                 ("nu", PForm * 5), ("gamma", PForm * 5), ("h", PForm * 5),
                 ("mig", (PForm * 5) * 5), ("theta0", PForm),
                 ("ndim", ctypes.c_int), ("pad_", ctypes.c_int)]
+
+
+#: Model parameters a dgb_seednd can seed (DGB_ND_MAXPAR).
+ND_MAXPAR = 16
+
+
+class SeedND(ctypes.Structure):
+    """dgb_seednd: d(a, b, c)/dtheta of every form of a dgb_instnd."""
+    _V = ctypes.c_double * ND_MAXPAR
+    _fields_ = [("dT", _V), ("dt0", _V), ("dnu", (_V * 3) * 5), ("dgamma", (_V * 3) * 5),
+                ("dh", (_V * 3) * 5), ("dmig", ((_V * 3) * 5) * 5), ("dtheta0", _V * 3)]
 
 
 class ItemND(ctypes.Structure):
@@ -122,6 +133,8 @@ def _declare(L):
         "dgb_batchnd_integrate": (i, [_vp, _vp, i, i, i, _vp, _vp, _vp,
                                       ctypes.POINTER(Settings), _vp, sz, _vp]),
         "dgb_schednd_host": (i, [_vp, i, ctypes.POINTER(Settings), lg, d, _vp, _vp, _vp, _vp]),
+        "dgb_schednd_dual_host": (i, [_vp, _vp, i, ctypes.POINTER(Settings), lg, d, _vp, _vp,
+                                      _vp, _vp]),
         "dgb_from_phi_nd_workspace_bytes": (sz, [i, i, _vp, i]),
         "dgb_from_phi_nd": (i, [_vp, i, i, i, _vp, _vp, _vp, _vp, _vp, _vp, sz, _vp]),
         "dgb_adjoint2d_traj_ws_bytes": (sz, [i, i]),

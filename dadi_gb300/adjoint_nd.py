@@ -21,6 +21,8 @@ migration): parameters (nu0_1, nu0_2, nu0_3, nuF_1, nuF_2, nuF_3, m12, m13,
 m23, T) with fixed selection gammas.
 """
 
+import ctypes
+
 import numpy as np
 
 from . import _lib, integration, numerics, phimanip, spectrum
@@ -136,6 +138,32 @@ def table_dual(P, xx, T, dT, nu_forms, mig_forms, gamma_forms, h_forms, theta0_f
         drows.append(drow)
     return (np.array(rows, dtype=np.float64).reshape(len(rows), stride),
             np.array(drows, dtype=np.float64).reshape(len(rows), stride, npar))
+
+
+def schedule_dual(rec, seed, npar, xx, max_steps=10 ** 7):
+    """table_dual walked in C (dgb_schednd_dual_host) for a dgb_instnd record
+    and its dgb_seednd derivative seeds: (table (n, stride), drows (n,
+    stride, npar)), the rows bit for bit those of batchnd.schedules."""
+    lib = _lib.lib()
+    st = _lib.settings_struct(*integration.current_settings())
+    dx0 = float(xx[1] - xx[0])
+    n = ctypes.c_int(0)
+    status = ctypes.c_int(0)
+    args = (ctypes.byref(rec), ctypes.byref(seed), int(npar), ctypes.byref(st), int(max_steps),
+            dx0)
+    _lib.check(lib.dgb_schednd_dual_host(*args, ctypes.byref(n), None, None,
+                                         ctypes.byref(status)), "dgb_schednd_dual_host(count)")
+    stride = integration.row_stride(rec.ndim)
+    table = np.zeros((max(n.value, 1), stride))
+    drows = np.zeros((max(n.value, 1), stride, npar))
+    status.value = 0
+    _lib.check(lib.dgb_schednd_dual_host(*args, ctypes.byref(n),
+                                         table.ctypes.data_as(ctypes.c_void_p),
+                                         drows.ctypes.data_as(ctypes.c_void_p),
+                                         ctypes.byref(status)), "dgb_schednd_dual_host")
+    if status.value:
+        raise ValueError("schedule walk failed: status %d" % status.value)
+    return table[:n.value], drows[:n.value]
 
 
 class TableModel:
@@ -294,6 +322,22 @@ class Growth3(TableModel):
         return phimanip.phi_2D_to_3D_split_2(xx, phi)
 
     def table(self, theta, xx):
+        """The parameter table and its derivatives, walked in C."""
+        from . import batchnd
+        th = [float(v) for v in theta]
+        rec = batchnd.growth3_instance(self.model_params(th))
+        seed = _lib.SeedND()
+        for i in range(3):
+            seed.dnu[i][0][i] = 1.0       # nu0_i
+            seed.dnu[i][1][3 + i] = 1.0   # nuF_i
+            seed.dnu[i][2][9] = 1.0       # the growth time is T
+        for q, (k, j) in zip((6, 7, 8), ((0, 1), (0, 2), (1, 2))):
+            seed.dmig[k][j][0][q] = seed.dmig[j][k][0][q] = 1.0
+        seed.dT[9] = 1.0
+        return schedule_dual(rec, seed, self.npar, xx)
+
+    def table_python(self, theta, xx):
+        """The same table walked in Python (table_dual)."""
         th = np.asarray(theta, dtype=np.float64)
         e = np.eye(self.npar)
         T = th[9]

@@ -587,3 +587,210 @@ extern "C" int dgb_schednd_host(const dgb_instnd *insts, int ninst,
     }
     return DGB_OK;
 }
+
+// ------------------------------------- parametric schedules in dual numbers
+
+// A value and its derivatives with respect to the seeded model parameters.
+struct DualN {
+    double v;
+    double d[DGB_ND_MAXPAR];
+};
+
+// A form at time t (dt/dtheta = dtd) with its derivative: the value exactly
+// as pform_eval gives it, the derivative by differentiating the form.
+static DualN pf_dual(const dgb_pform &f, const double (*dabc)[DGB_ND_MAXPAR], double t,
+                     const double *dtd, int npar)
+{
+    DualN r;
+    r.v = pform_eval(f, t);
+    const double *da = dabc[0], *db = dabc[1], *dc = dabc[2];
+    const double a = f.a, b = f.b, c = f.c;
+    switch (f.kind) {
+    case DGB_PF_EXPGROW:
+    case DGB_PF_EXPLOG: {
+        // v = a exp(lq t / c), lq = log(b / a)
+        const double lq = log(b / a);
+        const double e = r.v / a;
+        for (int p = 0; p < npar; p++) {
+            double dlq = db[p] / b - da[p] / a;
+            double dz = (dlq * t + lq * dtd[p]) / c - (lq * t / c) * dc[p] / c;
+            r.d[p] = da[p] * e + a * e * dz;
+        }
+        break;
+    }
+    case DGB_PF_LINEAR:
+        for (int p = 0; p < npar; p++)
+            r.d[p] = da[p] + db[p] * t + b * dtd[p];
+        break;
+    default:
+        for (int p = 0; p < npar; p++)
+            r.d[p] = da[p];
+    }
+    return r;
+}
+
+// compute_dt with its derivative along the branch its max takes (ties go to
+// the first candidate, as Python's max does).
+static DualN dt_dual(const DualN &nu, const DualN &ms, const DualN &g, const DualN &h,
+                     const dgb_settings &st, double dx0, int npar)
+{
+    DualN r;
+    r.v = compute_dt(nu.v, ms.v, g.v, h.v, st, dx0);
+    for (int p = 0; p < npar; p++)
+        r.d[p] = 0;
+    if (st.use_old_timestep)
+        return r;
+    const double v1 = 0.25 / nu.v;
+    const double t1 = fabs(h.v + (1 - 2 * h.v) * 0.5) * 0.5 * (1 - 0.5);
+    const double u2 = h.v + (1 - 2 * h.v) * 0.25;
+    const double t2 = fabs(u2) * 0.25 * (1 - 0.25);
+    const double tm = (t2 > t1) ? t2 : t1;
+    const double v3 = fabs(g.v) * 2 * tm;
+    int br = 0;
+    double mx = v1;
+    if (ms.v > mx) {
+        mx = ms.v;
+        br = 1;
+    }
+    if (v3 > mx) {
+        mx = v3;
+        br = 2;
+    }
+    if (!(mx > 0))
+        return r;
+    const double sg = (g.v > 0) ? 1.0 : ((g.v < 0) ? -1.0 : 0.0);
+    const double su = (u2 > 0) ? 1.0 : ((u2 < 0) ? -1.0 : 0.0);
+    for (int p = 0; p < npar; p++) {
+        double dmx;
+        if (br == 0) {
+            dmx = -0.25 * nu.d[p] / (nu.v * nu.v);
+        } else if (br == 1) {
+            dmx = ms.d[p];
+        } else {
+            // t1 does not depend on h; t2 = |u2| 3/16 with du2/dh = 1/2
+            double dtm = (t2 > t1) ? su * 0.5 * h.d[p] * 0.25 * (1 - 0.25) : 0.0;
+            dmx = sg * g.d[p] * 2 * tm + fabs(g.v) * 2 * dtm;
+        }
+        r.d[p] = -st.timescale_factor * dmx / (mx * mx);
+    }
+    return r;
+}
+
+extern "C" int dgb_schednd_dual_host(const dgb_instnd *inst, const dgb_seednd *seed, int npar,
+                                     const dgb_settings *settings, long max_steps, double dx0,
+                                     int *nrows, double *table, double *drows, int *status)
+{
+    if (!inst || !seed || !settings || !nrows || npar < 0 || npar > DGB_ND_MAXPAR ||
+        max_steps < 1 || (table && !drows) || inst->ndim < 1 || inst->ndim > DGB_MAX_DIM)
+        return DGB_ERR_ARG;
+    const dgb_instnd &I = *inst;
+    const dgb_seednd &S = *seed;
+    const dgb_settings &st = *settings;
+    const int P = I.ndim;
+    const int stride = row_stride(P);
+    const long room = table ? *nrows : 0;
+    DualN nu[DGB_MAX_DIM], g[DGB_MAX_DIM], h[DGB_MAX_DIM], m[DGB_MAX_DIM][DGB_MAX_DIM];
+    double dtd[DGB_ND_MAXPAR];
+    auto eval = [&](double t) {
+        for (int k = 0; k < P; k++) {
+            nu[k] = pf_dual(I.nu[k], S.dnu[k], t, dtd, npar);
+            g[k] = pf_dual(I.gamma[k], S.dgamma[k], t, dtd, npar);
+            h[k] = pf_dual(I.h[k], S.dh[k], t, dtd, npar);
+            for (int j = 0; j < P; j++)
+                if (j != k)
+                    m[k][j] = pf_dual(I.mig[k][j], S.dmig[k][j], t, dtd, npar);
+        }
+    };
+    for (int p = 0; p < npar; p++)
+        dtd[p] = S.dt0[p];
+    double cur = I.initial_t;
+    eval(cur);
+    long n = 0;
+    int err = 0;
+    while (cur < I.T) {
+        if (n >= max_steps) {
+            err |= DGB_ST_STEPCAP;
+            break;
+        }
+        DualN best;
+        for (int k = 0; k < P; k++) {
+            DualN ms;
+            ms.v = 0;
+            for (int p = 0; p < npar; p++)
+                ms.d[p] = 0;
+            for (int j = 0; j < P; j++)
+                if (j != k) {
+                    ms.v = ms.v + m[k][j].v;
+                    for (int p = 0; p < npar; p++)
+                        ms.d[p] += m[k][j].d[p];
+                }
+            DualN d = dt_dual(nu[k], ms, g[k], h[k], st, dx0, npar);
+            if (k == 0 || d.v < best.v)
+                best = d;
+        }
+        if (best.v == 0) {
+            err |= DGB_ST_ZERODT;
+            break;
+        }
+        const double rem = I.T - cur;
+        DualN step;
+        if (rem < best.v) {
+            step.v = rem;
+            for (int p = 0; p < npar; p++)
+                step.d[p] = S.dT[p] - dtd[p];
+        } else {
+            step = best;
+        }
+        const double next = cur + step.v;
+        if (!(step.v > 0) || !std::isfinite(next)) {
+            err |= DGB_ST_NONFINITE;
+            break;
+        }
+        for (int p = 0; p < npar; p++)
+            dtd[p] += step.d[p];
+        eval(next);
+        const DualN th0 = pf_dual(I.theta0, S.dtheta0, next, dtd, npar);
+        bool bad = I.T < 0 || th0.v < 0;
+        for (int k = 0; k < P; k++) {
+            bad = bad || nu[k].v < 0 || nu[k].v == 0;
+            for (int j = 0; j < P; j++)
+                bad = bad || (j != k && m[k][j].v < 0);
+        }
+        if (bad) {
+            err |= DGB_ST_BADPARAM;
+            break;
+        }
+        if (table && n >= room) {
+            err |= DGB_ST_STEPCAP;
+            break;
+        }
+        if (table) {
+            double *r = table + n * stride;
+            double *dr = drows + n * stride * npar;
+            for (int c = 0; c < stride * npar; c++)
+                dr[c] = 0;
+            auto put = [&](int c, const DualN &x) {
+                r[c] = x.v;
+                for (int p = 0; p < npar; p++)
+                    dr[c * npar + p] = x.d[p];
+            };
+            put(0, step);
+            put(1, th0);
+            for (int k = 0; k < P; k++) {
+                put(row_nu(P, k), nu[k]);
+                put(row_gamma(P, k), g[k]);
+                put(row_h(P, k), h[k]);
+                for (int j = 0; j < P; j++)
+                    if (j != k)
+                        put(row_mig(P, k, j), m[k][j]);
+            }
+            r[row_beta(P)] = 1.0;
+        }
+        n++;
+        cur = next;
+    }
+    *nrows = (int)n;
+    if (status)
+        *status |= err;
+    return DGB_OK;
+}

@@ -386,6 +386,32 @@ int dgb_schednd_host(const dgb_instnd *insts, int ninst, const dgb_settings *set
                      long max_steps, double dx0, int *row_cnt, const long *row_off,
                      double *table, int *status);
 
+/* Derivative seeds of a dgb_instnd with respect to npar <= DGB_ND_MAXPAR
+ * model parameters: d(a, b, c)/dtheta of every form (index 0, 1, 2 of the
+ * middle dimension), dT and d(initial_t).  Unused entries are zero. */
+#define DGB_ND_MAXPAR 16
+typedef struct {
+    double dT[DGB_ND_MAXPAR], dt0[DGB_ND_MAXPAR];
+    double dnu[DGB_MAX_DIM][3][DGB_ND_MAXPAR];
+    double dgamma[DGB_MAX_DIM][3][DGB_ND_MAXPAR];
+    double dh[DGB_MAX_DIM][3][DGB_ND_MAXPAR];
+    double dmig[DGB_MAX_DIM][DGB_MAX_DIM][3][DGB_ND_MAXPAR];
+    double dtheta0[3][DGB_ND_MAXPAR];
+} dgb_seednd;
+
+/* The schedule walk of dgb_schednd_host for one integration in forward-mode
+ * dual numbers (HOST arrays): the same rows, bit for bit, and their
+ * derivatives with respect to the seeded parameters, drows[n][c][p] =
+ * d table[n][c] / d theta_p (rows x DGB_ROW_STRIDE(ndim) x npar), along
+ * the branch each max/min of the walk takes (_compute_dt,
+ * dadi/Integration.py:147-176; the final partial step T - t).  The rows
+ * feed the discrete adjoint's chain rule dJ/dtheta = sum dJ/drow drow/dtheta.
+ * table == NULL counts into *nrows; otherwise *nrows bounds the rows
+ * written and is replaced by their number.  status as dgb_schednd_host. */
+int dgb_schednd_dual_host(const dgb_instnd *inst, const dgb_seednd *seed, int npar,
+                          const dgb_settings *settings, long max_steps, double dx0,
+                          int *nrows, double *table, double *drows, int *status);
+
 /* Spectrum epilogue of 2-D integrations (device-resident inputs, one launch
  * per list).  dgb_from_phi2d: raw spectrum of each density,
  * out[a][b] (n1+1 x n2+1) = the piecewise-linear integral of phi against

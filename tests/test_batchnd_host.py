@@ -62,3 +62,51 @@ def test_schedule_reports_bad_parameters():
     _, status = batchnd.schedules([batchnd.growth3_instance(bad),
                                    batchnd.growth3_instance(models.GROWTH3_DEFAULT)])
     assert status[0] & _lib.ST_BADPARAM and status[1] == 0
+
+
+@pytest.mark.parametrize("theta_scale", [1.0, 0.7, 1.3])
+def test_dual_schedule_in_c_equals_python(theta_scale):
+    """The schedule walk in dual numbers (dgb_schednd_dual_host) gives the
+    rows of dgb_schednd_host bit for bit, and rows and derivatives equal to
+    the Python walk (adjoint_nd.table_dual) within an ulp or two (libm
+    against numpy's exp and log)."""
+    from dadi_gb300 import adjoint_nd, numerics
+    g3 = adjoint_nd.Growth3.__new__(adjoint_nd.Growth3)  # the table needs no device
+    g3.gammas = (-2.0, 0.0, 5.0)
+    theta = g3.from_model_params(models.GROWTH3_DEFAULT) * theta_scale
+    xx = numerics.default_grid(12)
+    tab, drows = g3.table(theta, xx)
+    plain, status = batchnd.schedules([batchnd.growth3_instance(g3.model_params(theta))])
+    assert status[0] == 0 and np.array_equal(tab, plain[0])
+    ref, dref = g3.table_python(theta, xx)
+    _assert_same_table(tab, ref)
+    assert drows.shape == dref.shape == tab.shape + (10,)
+    scale = np.maximum(np.abs(dref).max(axis=0, keepdims=True), 1e-300)
+    assert float((np.abs(drows - dref) / scale).max()) <= 1e-14
+
+
+def test_dual_schedule_linear_and_power_forms_match_differences():
+    """Derivatives of the forms the Python walk does not cover (a + b t and
+    a (b / a)^(t / c)) against central differences of the rows."""
+    from dadi_gb300 import adjoint_nd
+    T = 0.05
+    xx = np.linspace(0, 1, 12)
+
+    def rec(v):
+        nu = [batchnd._pf(_lib.PF_LINEAR, v[0], 2.0), batchnd._pf(_lib.PF_EXPGROW, 0.5, v[1], T)]
+        return batchnd.instance(2, T, nu, [[0, 0.3], [0.2, 0]], gamma=[0.0, 1.0])
+    v0 = np.array([1.0, 3.0])
+    seed = _lib.SeedND()
+    seed.dnu[0][0][0] = 1.0
+    seed.dnu[1][1][1] = 1.0
+    tab, drows = adjoint_nd.schedule_dual(rec(v0), seed, 2, xx)
+    cols = [2, 3]  # nu1, nu2
+    for p in range(2):
+        e = np.zeros(2)
+        e[p] = 1e-6 * v0[p]
+        tp, _ = adjoint_nd.schedule_dual(rec(v0 + e), seed, 2, xx)
+        tm, _ = adjoint_nd.schedule_dual(rec(v0 - e), seed, 2, xx)
+        assert len(tp) == len(tm) == len(tab)
+        fd = (tp[:, cols] - tm[:, cols]) / (2 * e[p])
+        err = np.abs(fd - drows[:, cols, p]).max() / max(np.abs(fd).max(), 1e-300)
+        assert err < 1e-6, (p, err)
