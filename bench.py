@@ -693,6 +693,98 @@ def run_config2(a):
     return out
 
 
+def run_line_solvers(a):
+    """The line solvers of the batched N-D engine on the growth model's
+    grids (pts 70, 80, 90): Thomas per thread, warp PCR and the partitioned
+    Thomas with 2, 4 and 8 segments per line, for one parameter set alone
+    (a single 3-D integration: one grid's lines per launch) and for 32 sets
+    batched.  CUDA events around dgb_batchnd_integrate, best of 3 after a
+    warm-up; prints one JSON line."""
+    import torch
+    from dadi_gb300 import batchnd, models
+    sets = growth3_sets(32)
+    tabs, st = batchnd.schedules([batchnd.growth3_instance(p) for p in sets])
+    assert not st.any()
+    one, _ = batchnd.schedules([batchnd.growth3_instance(models.GROWTH3_DEFAULT)])
+    solvers = [("thomas", 0, 0), ("pcr", 1, 0), ("part2", 2, 2), ("part4", 2, 4),
+               ("part8", 2, 8)]
+    out = {}
+    for L in (70, 80, 90):
+        phi0 = torch.from_numpy(batchnd.initial_density("growth3", L)).cuda()
+        row = {}
+        for name, ls, seg in solvers:
+            eng = batchnd.BatchND(3, L, line_solver=ls, segments=seg)
+            res = {}
+            for label, tb in (("one_ms", one), ("batch32_ms", tabs)):
+                ts = []
+                for _ in range(4):
+                    ev = (torch.cuda.Event(enable_timing=True),
+                          torch.cuda.Event(enable_timing=True))
+                    eng.integrate(phi0, tb, timer=ev)
+                    torch.cuda.synchronize()
+                    ts.append(ev[0].elapsed_time(ev[1]))
+                res[label] = float(min(ts[1:]))
+            steps = [len(t) for t in tabs]
+            res["batch32_point_sweeps_per_s"] = 3 * sum(steps) * L ** 3 / (res["batch32_ms"] / 1e3)
+            res["one_point_sweeps_per_s"] = 3 * len(one[0]) * L ** 3 / (res["one_ms"] / 1e3)
+            row[name] = res
+        out["pts%d" % L] = row
+    # single integrations of other shapes: 3-D grids of 40, 60 and 120
+    # points, and the four-population model at 20, 30 and 40 points
+    four, _ = batchnd.schedules([batchnd.four_split_instance(models.FOUR_DEFAULT)])
+    alone = {}
+    for P, L, tb, kind in [(3, 40, one, "growth3"), (3, 60, one, "growth3"),
+                           (3, 120, one, "growth3"), (4, 20, four, "four"),
+                           (4, 30, four, "four"), (4, 40, four, "four")]:
+        phi0 = torch.from_numpy(batchnd.initial_density(kind, L)).cuda()
+        row = {}
+        for name, ls, seg in [("thomas", 0, 0), ("part2", 2, 2), ("part4", 2, 4),
+                              ("part8", 2, 8)]:
+            if ls and L < 3 * seg:
+                continue
+            eng = batchnd.BatchND(P, L, line_solver=ls, segments=seg)
+            ts = []
+            for _ in range(4):
+                ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                eng.integrate(phi0, tb, timer=ev)
+                torch.cuda.synchronize()
+                ts.append(ev[0].elapsed_time(ev[1]))
+            row[name + "_ms"] = float(min(ts[1:]))
+        alone["%dD_pts%d" % (P, L)] = row
+    # the drop-in on config 2: make_extrap_func (the grids on their own
+    # streams) and the grids one after another as dadi's make_extrap_func
+    # runs them, with the Thomas solve and with the automatic choice
+    from dadi_gb300 import integration, numerics
+    f = numerics.make_extrap_func(models.growth3)
+    args = (models.GROWTH3_DEFAULT, (20, 20, 20), [70, 80, 90])
+    dropin = {}
+    saved = integration.nd_line_solver
+    try:
+        for mode in ("thomas", "auto"):
+            integration.nd_line_solver = mode
+            for label, fn in (("concurrent_grids_s", lambda: f(*args)),
+                              ("sequential_grids_s",
+                               lambda: [models.growth3(args[0], args[1], L) for L in args[2]])):
+                fn()
+                ts = []
+                for _ in range(3):
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    fn()
+                    torch.cuda.synchronize()
+                    ts.append(time.perf_counter() - t0)
+                dropin["%s_%s" % (mode, label)] = float(np.median(ts))
+    finally:
+        integration.nd_line_solver = saved
+    print(json.dumps({"line_solvers": out, "alone": alone, "dropin_config2": dropin,
+                      "model": "three-population growth model (models.growth3): one set = "
+                      "the default parameters, 675 steps; 32 sets as run_config2's batch; "
+                      "four populations: models.four_split at its defaults",
+                      "timing": "CUDA events around the integration, best of 3 after one "
+                      "warm-up; dropin_config2: host wall clock, median of 3"}))
+    return 0
+
+
 def growth3_sets(n, seed=0):
     """n parameter sets of the three-population growth model: each of (nu0 x3,
     nuF x3, m12, m13, m23, T) scaled by exp(U(log .5, log 2)), seed 0."""
@@ -763,6 +855,15 @@ def run_profile_kernel(a):
             eng = batchnd.BatchND(3, 70)
             eng.integrate(torch.from_numpy(batchnd.initial_density("growth3", 70)).cuda(),
                           tabs)
+        elif a.profile in ("thomas3d", "part3d"):
+            # one set of the three-population growth model at pts 70 as a
+            # batch of one: Thomas, or the partitioned solve with 8 segments
+            from dadi_gb300 import batchnd
+            tabs, _ = batchnd.schedules([batchnd.growth3_instance(models.GROWTH3_DEFAULT)])
+            part = a.profile == "part3d"
+            eng = batchnd.BatchND(3, 70, line_solver=2 if part else 0, segments=8 if part else 0)
+            eng.integrate(torch.from_numpy(batchnd.initial_density("growth3", 70)).cuda(),
+                          tabs)
         elif a.profile == "fromphind":
             # spectra (20,20,20) of 32 three-population densities at pts 90
             from dadi_gb300 import numerics, spectrum
@@ -813,9 +914,14 @@ def main():
                          "steps, twice) for profiler captures, then exit")
     ap.add_argument("--profile", default=None,
                     choices=["epilogue", "sweep3d", "adjoint2d", "adjointnd", "batchnd",
-                             "fromphind"],
+                             "fromphind", "thomas3d", "part3d"],
                     help="run a small case of another kernel for profiler captures, then exit")
+    ap.add_argument("--line-solvers", action="store_true",
+                    help="time the batched N-D engine's line solvers on the growth model's "
+                         "grids, one set and 32 sets, then exit")
     a = ap.parse_args()
+    if a.line_solvers:
+        return run_line_solvers(a)
     if a.profile_items:
         return run_profile_case(a)
     if a.profile:

@@ -78,7 +78,7 @@ class Settings(ctypes.Structure):
     _fields_ = [("timescale_factor", ctypes.c_double), ("old_timescale_factor", ctypes.c_double),
                 ("use_old_timestep", ctypes.c_int), ("use_delj_trick", ctypes.c_int),
                 ("gam_placement", ctypes.c_int), ("threads", ctypes.c_int),
-                ("line_solver", ctypes.c_int), ("pad_", ctypes.c_int)]
+                ("line_solver", ctypes.c_int), ("segments", ctypes.c_int)]
 
 
 class DgbError(RuntimeError):
@@ -244,10 +244,11 @@ def workspace(torch, nbytes):
 
 
 def settings_struct(timescale_factor=1e-3, old_timescale_factor=0.1, use_old_timestep=False,
-                    use_delj_trick=False, gam_placement=0, threads=0, line_solver=0):
+                    use_delj_trick=False, gam_placement=0, threads=0, line_solver=0,
+                    segments=0):
     return Settings(float(timescale_factor), float(old_timescale_factor),
                     int(bool(use_old_timestep)), int(bool(use_delj_trick)), int(gam_placement),
-                    int(threads), int(line_solver), 0)
+                    int(threads), int(line_solver), int(segments))
 
 
 def fp64_fma_peak_tflops(torch, active_lanes=32, target_s=0.1, repeats=5):

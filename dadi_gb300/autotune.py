@@ -1,4 +1,5 @@
-"""Autotuner of the batched 2-D engine's launch configuration.
+"""Autotuners: the batched 2-D engine's launch configuration, and the line
+solver of a lone 3-5 population integration.
 
 The knobs, each a real alternative the kernels implement:
 
@@ -119,3 +120,66 @@ def tune_batch2d(eng, rec, sample_size=None, candidates=None, large_size=2048):
     _cache[key] = {"choice": choice, "ms": times, "ms_large": large,
                    "sample": int(len(sample)), "large_sample": int(big)}
     return _cache[key]
+
+
+#: Segments per line of the partitioned Thomas solve tried for a lone N-D
+#: grid (0: Thomas, one line per thread).
+ND_SEGMENTS = (0, 2, 4, 8)
+
+_nd_cache = {}
+_nd_lock = None
+
+
+def tune_nd_line_solver(P, L, steps=8):
+    """Segments of the partitioned solve (0: Thomas) with which a lone
+    P-population integration on L points runs fastest on this GPU.  Each
+    candidate (segments of at least three rows that fit shared memory)
+    integrates `steps` steps of a constant parameter table through
+    dgb_batchnd_integrate as a batch of one, timed with CUDA events, best of
+    3 after a warm-up.  Cached per (device, P, L); returns {"segments": s,
+    "ms": {s: ms}}.  Where the few lines of one grid leave the FP64 pipes
+    idle the partition wins (3-D grids of 40-90 points: 1.4-1.9x); where
+    the grid's lines fill them, or the partition's shared memory leaves one
+    CTA per SM, Thomas does (3-D at 120 points, 4-D at 30-40)."""
+    import threading
+    import torch
+    from . import batchnd, integration
+    global _nd_lock
+    if _nd_lock is None:
+        _nd_lock = threading.Lock()
+    key = (torch.cuda.get_device_name(torch.cuda.current_device()), int(P), int(L))
+    with _nd_lock:
+        if key in _nd_cache:
+            return _nd_cache[key]
+        stride = integration.row_stride(P)
+        tab = np.zeros((steps, stride))
+        tab[:, 0] = 1e-4                     # dt
+        tab[:, 1] = 1.0                      # theta0
+        tab[:, 2:2 + P] = 1.0                # nu
+        tab[:, 2 + 2 * P:2 + 3 * P] = 0.5    # h
+        tab[:, 2 + 3 * P] = 1.0              # beta
+        tab[:, 3 + 3 * P:] = 1.0             # migration
+        phi0 = torch.ones((L,) * P, dtype=torch.float64, device="cuda")
+        times = {}
+        for seg in ND_SEGMENTS:
+            if seg and L < 3 * seg:
+                continue
+            eng = batchnd.BatchND(P, L, line_solver=2 if seg else 0, segments=seg)
+            try:
+                best = None
+                for rep in range(4):
+                    ev = (torch.cuda.Event(enable_timing=True),
+                          torch.cuda.Event(enable_timing=True))
+                    eng.integrate(phi0, [tab], timer=ev)
+                    torch.cuda.synchronize()
+                    if rep:
+                        ms = ev[0].elapsed_time(ev[1])
+                        best = ms if best is None else min(best, ms)
+            except _lib.DgbError as e:
+                if e.status == _lib.DGB_ERR_UNSUPPORTED:
+                    continue
+                raise
+            times[seg] = best
+        choice = min(times, key=times.get)
+        _nd_cache[key] = {"segments": int(choice), "ms": times}
+        return _nd_cache[key]

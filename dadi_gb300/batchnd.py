@@ -102,24 +102,27 @@ def schedules(insts, settings=None, dx0=None, max_steps=10 ** 7):
     return tabs, status
 
 
-def integration_settings(gam_placement=0, threads=0, line_solver=0):
+def integration_settings(gam_placement=0, threads=0, line_solver=0, segments=0):
     tsf, otsf, old, delj = integration.current_settings()
-    return _lib.settings_struct(tsf, otsf, old, delj, gam_placement, threads, line_solver)
+    return _lib.settings_struct(tsf, otsf, old, delj, gam_placement, threads, line_solver,
+                                segments)
 
 
 class BatchND:
     """Integrations of `ndim` populations on one grid xx (default grid of L
     points unless given).  gam_placement / threads: the launch knobs of
     dgb_batchnd_integrate (0 = auto); line_solver: 0 Thomas (one line per
-    thread), 1 parallel cyclic reduction (one warp per line)."""
+    thread), 1 parallel cyclic reduction (one warp per line), 2 partitioned
+    Thomas (`segments` threads per line: 2, 4 or 8, 0 = 4)."""
 
-    def __init__(self, ndim, L, xx=None, gam_placement=0, threads=0, line_solver=0):
+    def __init__(self, ndim, L, xx=None, gam_placement=0, threads=0, line_solver=0,
+                 segments=0):
         self.torch = _lib.require_cuda()
         self.ndim, self.L = int(ndim), int(L)
         self.xx = numerics.default_grid(L) if xx is None else np.asarray(xx, dtype=np.float64)
         self.d_xx = _lib.upload_resident(self.torch, self.xx)
         self.gam_placement, self.threads = gam_placement, threads
-        self.line_solver = line_solver
+        self.line_solver, self.segments = line_solver, segments
 
     def integrate(self, phi0, tables, masks=None, timer=None):
         """Integrate n densities through their tables.  phi0: a CUDA tensor
@@ -152,7 +155,8 @@ class BatchND:
         items["nsteps"] = steps[order]
         items["masks"] = 0 if masks is None else np.asarray(masks, dtype=np.int32)[order]
         nsteps_h = np.ascontiguousarray(steps[order])
-        st = integration_settings(self.gam_placement, self.threads, self.line_solver)
+        st = integration_settings(self.gam_placement, self.threads, self.line_solver,
+                                  self.segments)
         d_items = _lib.to_device(torch, items.view(np.uint8), np.uint8)
         d_tab = _lib.to_device(torch, tab)
         nws = lib.dgb_batchnd_workspace_bytes(P, L, n, ctypes.byref(st))

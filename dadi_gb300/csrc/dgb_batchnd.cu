@@ -13,7 +13,11 @@
 // does; the Thomas gam scratch sits in shared memory or in a per-CTA slice
 // of the workspace (L2), which leaves room for twice the CTAs per SM.
 // Per line the arithmetic is that of k_sweep_nd_rec, so every integration's
-// density is bitwise the one dgb_integrate_table computes alone.
+// density is bitwise the one dgb_integrate_table computes alone.  Two other
+// line solvers are selectable (dgb_settings.line_solver): warp-level
+// parallel cyclic reduction and the partitioned Thomas solve; they agree
+// with Thomas to rounding, and the partition is the faster one for a lone
+// grid whose few lines leave the FP64 pipes idle.
 //
 // Replaces many calls of Integration.three_pops / four_pops / five_pops
 // (dadi/Integration.py:389-554, 556-727, 729-937), which the reference runs
@@ -295,10 +299,236 @@ __global__ void __launch_bounds__(32 * PCR_LINES) k_sweep_batch_pcr(NDBatch B, l
         A.phi[base + p * A.S] = d[p] * rcp_full(b[p]);
 }
 
+// The second alternative: partitioned Thomas (the partition method of
+// H. H. Wang, ACM TOMS 7 (1981) 170-183, in the two-sweep "modified Thomas"
+// form used for batched GPU solvers by Laszlo, Giles and Appleyard, ACM TOMS
+// 42 (2016) 31).  Each line is cut into SEG segments, one thread each (warp
+// q of the CTA holds segment q of the CTA's 32 lines), so a launch over one
+// grid carries SEG times the threads of the Thomas sweep.  Per segment of
+// rows s0 .. s0+m-1 (local j = 0 .. m-1, rows as in the Thomas path):
+//   downward, j >= 1: every row becomes  al_j x_0 + x_j + ga_j x_{j+1} = de_j
+//     (j = 1: al = a/b, ga = c/b, de = d/b; then with r = 1/(b_j - a_j ga_{j-1}):
+//      al_j = -a_j al_{j-1} r, ga_j = c_j r, de_j = (d_j - a_j de_{j-1}) r);
+//   upward, j <= m-3: x_j = de_j - al_j x_0 - ga_j x_{m-1}
+//     (de_j -= ga_j de_{j+1}, al_j -= ga_j al_{j+1}, ga_j = -ga_j ga_{j+1});
+//   row 0 with x_1 substituted:  a_0 x_prev + (b_0 - c_0 al_1) x_0
+//                                - c_0 ga_1 x_{m-1} = d_0 - c_0 de_1;
+//   row m-1 as it stands:        al x_0 + x_{m-1} + ga x_next = de.
+// Those two rows of every segment form a tridiagonal system of 2 SEG
+// unknowns (the segments' end points), solved by one thread per line; then
+// x_j = de_j - al_j x_0 - ga_j x_{m-1} inside.  About 17 FP64 instructions
+// per row against 10 for Thomas.  Default delta_j only; segments of at least
+// three rows.
+constexpr int PART_LINES = 32;
+
+__host__ __device__ inline size_t part_smem_doubles(int L, int seg)
+{
+    return (size_t)6 * L + (size_t)L * (PART_LINES + 1) + (size_t)2 * L * PART_LINES +
+           (size_t)8 * seg * PART_LINES;
+}
+
+template <int SEG>
+__global__ void __launch_bounds__(32 * SEG) k_sweep_batch_part(NDBatch B, long step)
+{
+    extern __shared__ __align__(16) double smem[];
+    __shared__ NDRecHead H;
+    const int L = B.A.L, P = B.A.ndim;
+    constexpr int nt = PART_LINES, tp = PART_LINES + 1;
+    const int tid = threadIdx.x, q = tid >> 5, t = tid & 31;
+    const long it = blockIdx.x / B.bpi;
+    const long tl = blockIdx.x - it * B.bpi;
+    const dgb_itemnd I = B.items[it];
+    const int frozen = I.masks & 0xff, nomut = (I.masks >> 8) & 0xff;
+    if (step >= I.nsteps || (frozen >> B.A.axis & 1))
+        return;
+    NDArgs A = B.A;
+    A.phi = B.phi_all + I.phi_off;
+    const int inject =
+        (A.axis == first_swept(frozen)) ? (((1 << P) - 1) & ~frozen & ~nomut) : 0;
+    double *vv = smem;                        // A1, A0, C1, C0, B0
+    double *gx = vv + 5 * L;                  // x
+    double *tile = gx + L;                    // d, then de, then x
+    double *al = tile + (size_t)L * tp;       // al_j
+    double *ga = al + (size_t)L * nt;         // ga_j
+    double *red = ga + (size_t)L * nt;        // 8 doubles per (segment, line)
+    const double *rec = B.coef + nd_grid_doubles(L) + it * B.item_coef +
+                        ((size_t)(step - B.step0) * P + A.axis) * nd_rec_doubles(L, false);
+    double *hp = reinterpret_cast<double *>(&H);
+    for (int i = tid; i < ND_HEAD; i += blockDim.x)
+        hp[i] = rec[i];
+    for (int i = tid; i < 5 * L; i += blockDim.x)
+        vv[i] = rec[ND_HEAD + i];
+    for (int i = tid; i < L; i += blockDim.x)
+        gx[i] = B.coef[i];
+    // this thread's segment
+    const int mlen = L / SEG, extra = L % SEG;
+    const int s0 = q * mlen + min(q, extra);
+    const int m = mlen + (q < extra ? 1 : 0);
+    const long l0 = tl * nt;
+    const int n = (int)min((long)nt, A.nlines - l0);
+    if (A.S == 1) {
+        // contiguous lines: each warp copies whole lines, lanes along the line
+        const double *g0 = A.phi + l0 * L;
+        for (int w = q; w < n; w += SEG)
+            for (int p = t; p < L; p += 32)
+                tile[p * tp + w] = g0[(size_t)w * L + p];
+    } else if (t < n) {
+        const long line = l0 + t;
+        const long outer = line / A.S, inner = line - outer * A.S;
+        const double *g0 = A.phi + outer * A.LS + inner;
+        for (int p = s0; p < s0 + m; p++)
+            tile[p * tp + t] = g0[p * A.S];
+    }
+    __syncthreads();
+    AxisVecs v;
+    nd_vecs_at(vv, L, false, v);
+    const AxisScalars &s = H.s;
+    double *r8 = red + (size_t)q * 8 * nt + t; // this segment's reduced rows, stride nt
+    if (t < n) {
+        int coord[DGB_MAX_DIM];
+        nd_line_base(A, l0 + t, coord);
+        const int j0 = (gx[0] == 0.0) ? 0 : -1;
+        const int j1 = (gx[L - 1] == 1.0) ? L - 1 : -1;
+        double W = 0;
+        bool all0 = true, all1 = true;
+        int n1 = 0, k1 = -1;
+        for (int k = 0; k < P; k++) {
+            if (k == A.axis)
+                continue;
+            W = fma(s.mig[k], gx[coord[k]], W);
+            all0 = all0 && coord[k] == j0;
+            all1 = all1 && coord[k] == j1;
+            if (coord[k] == 1) {
+                n1++;
+                k1 = k;
+            } else if (coord[k] != 0) {
+                n1 = 99;
+            }
+        }
+        if (P == 1)
+            all0 = all1 = true;
+        if (inject && q == 0) {
+            if (n1 == 0 && H.inj[A.axis] != 0.0)
+                tile[1 * tp + t] += H.inj[A.axis];
+            if (n1 == 1 && H.inj[k1] != 0.0)
+                tile[0 * tp + t] += H.inj[k1];
+        }
+        auto arow = [&](int p) { return (p > 0) ? fma(W, v.A1[p], v.A0[p]) : 0.0; };
+        auto crow = [&](int p) { return (p < L - 1) ? fma(W, v.C1[p], v.C0[p]) : 0.0; };
+        auto brow = [&](int p) {
+            if (p == 0)
+                return fma(W, s.B1s, v.B0[0]) + (all0 ? s.bcs : 0.0);
+            if (p == L - 1)
+                return fma(W, s.B1e, v.B0[L - 1]) + (all1 ? s.bce : 0.0);
+            return v.B0[p];
+        };
+        // downward
+        int p = s0 + 1;
+        double inv = rcp_full(brow(p));
+        double a = arow(p);
+        double alp = a * inv, gap = crow(p) * inv, dep = tile[p * tp + t] * inv;
+        al[p * nt + t] = alp;
+        ga[p * nt + t] = gap;
+        tile[p * tp + t] = dep;
+        for (p = s0 + 2; p < s0 + m; p++) {
+            a = arow(p);
+            inv = rcp_full(fma(-a, gap, brow(p)));
+            alp = -a * alp * inv;
+            gap = crow(p) * inv;
+            dep = fma(-a, dep, tile[p * tp + t]) * inv;
+            al[p * nt + t] = alp;
+            ga[p * nt + t] = gap;
+            tile[p * tp + t] = dep;
+        }
+        // the segment's last row, as it stands
+        r8[4 * nt] = alp;
+        r8[5 * nt] = gap;
+        r8[6 * nt] = dep;
+        // upward, from row m-3: ga_j now couples to x_{m-1}
+        p = s0 + m - 2;
+        double deu = tile[p * tp + t], alu = al[p * nt + t], gau = ga[p * nt + t];
+        for (p = s0 + m - 3; p >= s0 + 1; p--) {
+            const double g = ga[p * nt + t];
+            deu = fma(-g, deu, tile[p * tp + t]);
+            alu = fma(-g, alu, al[p * nt + t]);
+            gau = -g * gau;
+            tile[p * tp + t] = deu;
+            al[p * nt + t] = alu;
+            ga[p * nt + t] = gau;
+        }
+        // row 0 with x_1 substituted
+        const double c0 = crow(s0);
+        r8[0] = arow(s0);
+        r8[1 * nt] = fma(-c0, alu, brow(s0));
+        r8[2 * nt] = -c0 * gau;
+        r8[3 * nt] = fma(-c0, deu, tile[s0 * tp + t]);
+    }
+    __syncthreads();
+    if (q == 0 && t < n) {
+        // the 2 SEG end points: Thomas on rows (row 0, row m-1) of each
+        // segment in order; unknowns y_{2k} = x_first(k), y_{2k+1} = x_last(k)
+        double gm[2 * SEG], y[2 * SEG];
+        double g = 0, u = 0;
+#pragma unroll
+        for (int r = 0; r < 2 * SEG; r++) {
+            const double *rr = red + (size_t)(r >> 1) * 8 * nt + t;
+            double ra, rb, rc, rd;
+            if ((r & 1) == 0) {
+                ra = rr[0];
+                rb = rr[1 * nt];
+                rc = rr[2 * nt];
+                rd = rr[3 * nt];
+            } else {
+                ra = rr[4 * nt];
+                rb = 1.0;
+                rc = rr[5 * nt];
+                rd = rr[6 * nt];
+            }
+            const double bet = (r == 0) ? rb : fma(-ra, g, rb);
+            const double iv = rcp_full(bet);
+            u = ((r == 0) ? rd : fma(-ra, u, rd)) * iv;
+            g = rc * iv;
+            gm[r] = g;
+            y[r] = u;
+        }
+#pragma unroll
+        for (int r = 2 * SEG - 2; r >= 0; r--)
+            y[r] = fma(-gm[r], y[r + 1], y[r]);
+#pragma unroll
+        for (int k = 0; k < SEG; k++) {
+            red[(size_t)k * 8 * nt + 3 * nt + t] = y[2 * k];
+            red[(size_t)k * 8 * nt + 6 * nt + t] = y[2 * k + 1];
+        }
+    }
+    __syncthreads();
+    if (t < n) {
+        const double xf = r8[3 * nt], xl = r8[6 * nt];
+        tile[s0 * tp + t] = xf;
+        tile[(s0 + m - 1) * tp + t] = xl;
+        for (int p = s0 + 1; p < s0 + m - 1; p++)
+            tile[p * tp + t] = fma(-ga[p * nt + t], xl,
+                                   fma(-al[p * nt + t], xf, tile[p * tp + t]));
+    }
+    __syncthreads();
+    if (A.S == 1) {
+        double *g0 = A.phi + l0 * L;
+        for (int w = q; w < n; w += SEG)
+            for (int p = t; p < L; p += 32)
+                g0[(size_t)w * L + p] = tile[p * tp + w];
+    } else if (t < n) {
+        const long line = l0 + t;
+        const long outer = line / A.S, inner = line - outer * A.S;
+        double *g0 = A.phi + outer * A.LS + inner;
+        for (int p = s0; p < s0 + m; p++)
+            g0[p * A.S] = tile[p * tp + t];
+    }
+}
+
 // ------------------------------------------------------------ host side
 
 struct BatchPlan {
     int pcr;       // parallel cyclic reduction (one warp per line)
+    int seg;       // partitioned Thomas: segments per line (0: not used)
     int nt;        // lines per CTA
     int gsmem;     // gam in shared memory
     int chunk;     // steps per record chunk
@@ -327,6 +557,7 @@ static int batch_plan(int ndim, int L, int nitems, const dgb_settings *st, Batch
 {
     const long nlines = ipow(L, ndim - 1);
     p.pcr = st && st->line_solver == 1;
+    p.seg = 0;
     if (p.pcr) {
         if (L > 128 || st->use_delj_trick)
             return DGB_ERR_UNSUPPORTED;
@@ -335,6 +566,30 @@ static int batch_plan(int ndim, int L, int nitems, const dgb_settings *st, Batch
         p.bpi = (int)((nlines + PCR_LINES - 1) / PCR_LINES);
         p.chunk = batch_chunk(ndim, L, nitems);
         p.smem = (6 + 5 * PCR_LINES) * (size_t)L * sizeof(double);
+        p.coef_doubles = (size_t)nd_grid_doubles(L) +
+                         (size_t)nitems * p.chunk * ndim * nd_rec_doubles(L, false);
+        p.gam_doubles = 0;
+        return DGB_OK;
+    }
+    if (st && st->line_solver == 2) {
+        const int seg = st->segments ? st->segments : 4;
+        if (seg != 2 && seg != 4 && seg != 8)
+            return DGB_ERR_ARG;
+        if (L < 3 * seg || st->use_delj_trick)
+            return DGB_ERR_UNSUPPORTED;
+        int optin = 0, dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+                cudaSuccess)
+            return DGB_ERR_CUDA;
+        p.seg = seg;
+        p.gsmem = 0;
+        p.nt = PART_LINES;
+        p.bpi = (int)((nlines + PART_LINES - 1) / PART_LINES);
+        p.chunk = batch_chunk(ndim, L, nitems);
+        p.smem = part_smem_doubles(L, seg) * sizeof(double);
+        if (p.smem + sizeof(NDRecHead) + 1024 > (size_t)optin)
+            return DGB_ERR_UNSUPPORTED;
         p.coef_doubles = (size_t)nd_grid_doubles(L) +
                          (size_t)nitems * p.chunk * ndim * nd_rec_doubles(L, false);
         p.gam_doubles = 0;
@@ -368,6 +623,15 @@ static int batch_plan(int ndim, int L, int nitems, const dgb_settings *st, Batch
                      (size_t)nitems * p.chunk * ndim * nd_rec_doubles(L, delj);
     p.gam_doubles = p.gsmem ? 0 : (size_t)nitems * p.bpi * nt * L;
     return DGB_OK;
+}
+
+template <int SEG>
+static int batch_part_launch(NDBatch &B, long nact, size_t smem, long step, cudaStream_t st)
+{
+    if (raise_smem_limit(k_sweep_batch_part<SEG>))
+        return DGB_ERR_CUDA;
+    k_sweep_batch_part<SEG><<<(unsigned)(nact * B.bpi), 32 * SEG, smem, st>>>(B, step);
+    return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
 }
 
 template <bool DELJ, bool GSMEM>
@@ -453,6 +717,14 @@ extern "C" int dgb_batchnd_integrate(const dgb_itemnd *items, const int *nsteps,
                 k_sweep_batch_pcr<<<(unsigned)(nact * B.bpi), 32 * PCR_LINES, p.smem, st>>>(B, s);
                 if (cudaGetLastError() != cudaSuccess)
                     return DGB_ERR_CUDA;
+                continue;
+            }
+            if (p.seg) {
+                rc = (p.seg == 2)   ? batch_part_launch<2>(B, nact, p.smem, s, st)
+                     : (p.seg == 4) ? batch_part_launch<4>(B, nact, p.smem, s, st)
+                                    : batch_part_launch<8>(B, nact, p.smem, s, st);
+                if (rc)
+                    return rc;
                 continue;
             }
             if (delj)

@@ -7,8 +7,11 @@ parameters at the current time (`_compute_dt`), every parameter at the next
 time, the same validation errors -- and records one table row per step.  The
 whole table then runs in one call of the C ABI (dgb_integrate_table): a
 shared-memory-resident single-CTA kernel for 2-D grids, one fused sweep kernel
-per axis per step for 1-D/3-D/4-D.  phi crosses the host/device boundary once
-in each direction per call.
+per axis per step for 1-D/3-D/4-D.  A 3-5 population grid whose lines are too
+few to fill the FP64 pipes (fewer than two warps per SM sub-partition with one
+line per thread) runs instead through dgb_batchnd_integrate as a batch of one
+with the partitioned Thomas solve (nd_line_solver).  phi crosses the
+host/device boundary once in each direction per call.
 
 Constant-parameter 2-D/3-D calls take the temporal path, as the reference
 does when CUDA is enabled (dadi/Integration.py:324, 468); with
@@ -16,6 +19,7 @@ enable_cuda_cached=True they take the constant-coefficient path instead
 (dgb_integrate_precalc with the a/b/c arrays of dadi/Integration.py:1037-1242).
 """
 import sys
+import threading
 
 import numpy as np
 
@@ -27,6 +31,15 @@ use_delj_trick = False
 timescale_factor = 1e-3
 use_old_timestep = False
 old_timescale_factor = 0.1
+
+#: Line solver of the 3-5 population integrations: "thomas" (one line per
+#: thread, dgb_integrate_table), "partition" (the partitioned Thomas solve of
+#: dgb_batchnd_integrate, segments per line from nd_segments or by grid size)
+#: or "auto" (autotune.tune_nd_line_solver times both on this GPU once per
+#: grid shape).  The results agree to rounding (1e-12); "thomas" keeps them
+#: bitwise those of the batched engine.
+nd_line_solver = "auto"
+nd_segments = 0
 
 
 def current_settings():
@@ -151,6 +164,52 @@ def _device_phi(torch, phi):
     return _lib.to_device(torch, np.ascontiguousarray(phi, dtype=np.float64)), False
 
 
+#: Per-thread state: `sharing_gpu` is set on the threads of
+#: numerics.make_extrap_func that integrate several grids at once, whose
+#: Thomas sweeps together already fill the pipes.
+local = threading.local()
+
+
+def partition_segments(P, L, delj=False):
+    """Segments per line of the partitioned solve for a lone P-population
+    grid of L points under nd_line_solver, or 0 for Thomas.  "partition":
+    nd_segments, or as many as keep 8 rows per segment (8 from L = 64, 4
+    from 32, 2 from 16); "auto": the autotuner's choice for the shape, and
+    Thomas on threads that share the GPU with other grids' integrations
+    (measured on the growth model at pts 70/80/90 run concurrently: 0.184 s
+    with Thomas, 0.189 s with the partition; one grid after another 0.372 s
+    and 0.295 s)."""
+    mode = nd_line_solver
+    if mode not in ("auto", "thomas", "partition"):
+        raise ValueError("nd_line_solver must be 'auto', 'thomas' or 'partition'")
+    if P < 3 or delj or mode == "thomas":
+        return 0
+    if mode == "auto":
+        if getattr(local, "sharing_gpu", False):
+            return 0
+        from . import autotune
+        return autotune.tune_nd_line_solver(P, L)["segments"]
+    seg = int(nd_segments) or next((s for s in (8, 4, 2) if L >= 8 * s), 0)
+    return seg if seg and L >= 3 * seg else 0
+
+
+_engines = {}
+
+
+def _partition_engine(P, L, xx, seg):
+    """A batch-of-one engine with the partitioned solve, kept per (P, grid,
+    segments) for the life of the process: its grid stays on the device,
+    and is never freed under a launch still in flight on another stream."""
+    from . import batchnd
+    xx = np.ascontiguousarray(xx, dtype=np.float64)
+    key = (P, seg, xx.tobytes())
+    eng = _engines.get(key)
+    if eng is None:
+        eng = _engines.setdefault(key, batchnd.BatchND(P, L, xx=xx, line_solver=2,
+                                                       segments=seg))
+    return eng
+
+
 def run_table(phi, xx, table, frozen_mask=0, nomut_mask=0):
     """Integrate phi (host ndarray, or CUDA tensor kept on the device)
     through a parameter table on the GPU; returns a new array of the same
@@ -162,6 +221,12 @@ def run_table(phi, xx, table, frozen_mask=0, nomut_mask=0):
     if len(table) == 0:
         return _copy_in(phi)
     d_phi, dev = _device_phi(torch, phi)
+    seg = partition_segments(P, L, current_settings()[3])
+    if seg:
+        out = _partition_engine(P, L, xx, seg).integrate(
+            d_phi, [np.asarray(table, dtype=np.float64)],
+            [int(frozen_mask) | int(nomut_mask) << 8])[0]
+        return out if dev else _lib.to_host(torch, out)
     d_xx = _lib.to_device(torch, xx)
     d_tab = _lib.to_device(torch, table)
     ws, nws = _lib.workspace(torch, _lib.lib().dgb_workspace_bytes(0, P, L, 0))

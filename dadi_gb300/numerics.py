@@ -68,7 +68,8 @@ def _map_grids(fn, pts_l):
     on its own thread and CUDA stream: one integration of a few grids leaves
     most SMs idle (a 3-D sweep at L = 70 is 77 CTAs), and the integrations of
     different grids are independent.  The results are the same as one at a
-    time."""
+    time (to rounding where the drop-in would pick the partitioned solve
+    for a lone 3-5 population grid)."""
     if len(pts_l) < 2:
         return [fn(p) for p in pts_l]
     try:
@@ -79,11 +80,17 @@ def _map_grids(fn, pts_l):
     if not gpu:
         return [fn(p) for p in pts_l]
     from concurrent.futures import ThreadPoolExecutor
+    from . import integration
     dev = torch.cuda.current_device()
 
     def one(p):
-        with torch.cuda.device(dev), torch.cuda.stream(torch.cuda.Stream()):
-            return fn(p)
+        # Thomas for 3-5 populations: the grids' sweeps together fill the pipes
+        integration.local.sharing_gpu = True
+        try:
+            with torch.cuda.device(dev), torch.cuda.stream(torch.cuda.Stream()):
+                return fn(p)
+        finally:
+            integration.local.sharing_gpu = False
     with ThreadPoolExecutor(max_workers=len(pts_l)) as ex:
         return list(ex.map(one, pts_l))
 

@@ -82,8 +82,10 @@ typedef struct {
                                     lanes better */
     int line_solver;             /* batched N-dimensional engine: 0 Thomas, one line per
                                     thread (dadi/tridiag.c:14-34); 1 parallel cyclic
-                                    reduction, one warp per line (L <= 128) */
-    int pad_;
+                                    reduction, one warp per line (L <= 128); 2 partitioned
+                                    Thomas, `segments` threads per line (L >= 3 segments);
+                                    1 and 2 without the delj trick */
+    int segments;                /* line_solver 2: segments per line, 2, 4 or 8 (0: 4) */
 } dgb_settings;
 
 int dgb_abi_version(void);
@@ -347,7 +349,10 @@ int dgb_adjoint_table_nd(double *lam, int ndim, int L, const double *xx, const d
  *   table   device, parameter rows (DGB_ROW_STRIDE(ndim) doubles each, the
  *           layout above); integration i uses rows row_off .. row_off+nsteps
  *   settings use_delj_trick; threads = lines per CTA (0 auto, 32, 64, 128);
- *           gam_placement 0 auto (workspace), 1 shared memory, 2 workspace
+ *           gam_placement 0 auto (workspace), 1 shared memory, 2 workspace;
+ *           line_solver / segments (Thomas by default; the partitioned
+ *           Thomas solve with one item is the fast form of a lone 3-D grid
+ *           of few lines, e.g. 63 ms instead of 92 ms for 675 steps at L=70)
  *   ws      dgb_batchnd_workspace_bytes(ndim, L, nitems, settings) bytes */
 typedef struct {
     long phi_off; /* offset of the density in phi_all, in doubles */

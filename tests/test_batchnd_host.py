@@ -110,3 +110,28 @@ def test_dual_schedule_linear_and_power_forms_match_differences():
         fd = (tp[:, cols] - tm[:, cols]) / (2 * e[p])
         err = np.abs(fd - drows[:, cols, p]).max() / max(np.abs(fd).max(), 1e-300)
         assert err < 1e-6, (p, err)
+
+
+def test_partition_segment_rule():
+    """Segments per line of the drop-in's partitioned solve: at least 8 rows
+    per segment, none for 1-2 populations, the delj trick or "thomas"; a
+    fixed count when nd_segments is set (without a GPU: "partition" mode)."""
+    saved = integration.nd_line_solver, integration.nd_segments
+    try:
+        integration.nd_line_solver = "partition"
+        assert integration.partition_segments(3, 70) == 8
+        assert integration.partition_segments(3, 40) == 4
+        assert integration.partition_segments(4, 20) == 2
+        assert integration.partition_segments(4, 12) == 0
+        assert integration.partition_segments(2, 90) == 0
+        assert integration.partition_segments(3, 90, delj=True) == 0
+        integration.nd_segments = 4
+        assert integration.partition_segments(3, 12) == 4
+        assert integration.partition_segments(3, 11) == 0
+        integration.nd_line_solver = "thomas"
+        assert integration.partition_segments(3, 90) == 0
+        integration.nd_line_solver = "fast"
+        with pytest.raises(ValueError):
+            integration.partition_segments(3, 90)
+    finally:
+        integration.nd_line_solver, integration.nd_segments = saved

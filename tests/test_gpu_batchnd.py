@@ -14,13 +14,15 @@ pytestmark = pytest.mark.gpu
 
 
 def _alone(phi0, xx, table, masks, delj=False):
+    """The drop-in's one-at-a-time integration with the Thomas solve
+    (dgb_integrate_table)."""
     from dadi_gb300 import integration
-    saved = integration.use_delj_trick
-    integration.use_delj_trick = delj
+    saved = integration.use_delj_trick, integration.nd_line_solver
+    integration.use_delj_trick, integration.nd_line_solver = delj, "thomas"
     try:
         return integration.run_table(phi0, xx, table, masks & 0xff, masks >> 8)
     finally:
-        integration.use_delj_trick = saved
+        integration.use_delj_trick, integration.nd_line_solver = saved
 
 
 @pytest.mark.parametrize("P,L,gam,threads,delj", [
@@ -153,3 +155,100 @@ def test_pcr_line_solver_config2_matches_dadi(cuda_lib, golden):
         res.append(spectrum.from_phi(phi, g["ns"], (xx, xx, xx)))
     fs = numerics.extrapolate(res, [r.extrap_x for r in res])
     assert_fs_parity(np.asarray(fs.data), golden["models"]["growth3_fs"])
+
+
+@pytest.mark.parametrize("P,L,seg", [(3, 20, 4), (3, 33, 2), (3, 33, 8), (4, 12, 4),
+                                     (1, 100, 8), (2, 128, 4), (3, 9, 2)])
+def test_partition_line_solver_matches_thomas(cuda_lib, P, L, seg):
+    """The partitioned Thomas solve (segments of a line on their own threads,
+    the segments' end points from a small tridiagonal system) solves the same
+    systems as Thomas: the densities agree to 1e-12 relative, every axis,
+    contiguous and strided, uneven segment lengths, a frozen population."""
+    import torch
+    from dadi_gb300 import batchnd
+    xx = cases.grid("default", L)
+    tables = [table_rows(P, nst, 400 + k) for k, nst in enumerate([9, 4, 9])]
+    masks = [0, 0, 1 << 8] if P == 1 else [0, 1, 1 << 8]
+    phi0 = np.stack([np.abs(cases.initial_phi(60 + k, (L,) * P)) + 1e-3 for k in range(3)])
+    d0 = torch.from_numpy(phi0).cuda()
+    th = batchnd.BatchND(P, L, xx=xx).integrate(d0, tables, masks).cpu().numpy()
+    pt = batchnd.BatchND(P, L, xx=xx, line_solver=2, segments=seg).integrate(d0, tables, masks)
+    pt = pt.cpu().numpy()
+    for k in range(3):
+        rel = np.max(np.abs(pt[k] - th[k]) / np.maximum(np.abs(th[k]), 1e-12 * np.abs(th[k]).max()))
+        assert rel < 1e-12, (k, rel)
+
+
+def test_partition_line_solver_config2_matches_dadi(cuda_lib, golden):
+    """Config 2 with the partitioned solver (4 segments), against dadi."""
+    import torch
+    from dadi_gb300 import batchnd, numerics, spectrum
+    g = cases.GROWTH3
+    tabs, _ = batchnd.schedules([batchnd.growth3_instance(g["params"])])
+    res = []
+    for L in g["pts_l"]:
+        eng = batchnd.BatchND(3, L, line_solver=2, segments=4)
+        phi = eng.integrate(torch.from_numpy(batchnd.initial_density("growth3", L)).cuda(),
+                            tabs)[0]
+        xx = numerics.default_grid(L)
+        res.append(spectrum.from_phi(phi, g["ns"], (xx, xx, xx)))
+    fs = numerics.extrapolate(res, [r.extrap_x for r in res])
+    assert_fs_parity(np.asarray(fs.data), golden["models"]["growth3_fs"])
+
+
+def test_partition_rejects_what_it_does_not_solve(cuda_lib):
+    """Segments of fewer than three rows, an unknown segment count and the
+    delj trick are refused with a status, not solved differently."""
+    import torch
+    from dadi_gb300 import _lib, batchnd, integration
+    tab = [table_rows(3, 2, 7)]
+    for L, seg in ((8, 4), (20, 3)):
+        eng = batchnd.BatchND(3, L, line_solver=2, segments=seg)
+        with pytest.raises(_lib.DgbError):
+            eng.integrate(torch.ones((L,) * 3, dtype=torch.float64, device="cuda"), tab)
+    saved = integration.use_delj_trick
+    integration.use_delj_trick = True
+    try:
+        eng = batchnd.BatchND(3, 20, line_solver=2)
+        with pytest.raises(_lib.DgbError):
+            eng.integrate(torch.ones((20,) * 3, dtype=torch.float64, device="cuda"), tab)
+    finally:
+        integration.use_delj_trick = saved
+
+
+@pytest.mark.parametrize("P,L,frozen", [(3, 70, 0), (3, 40, 2), (4, 20, 0)])
+def test_dropin_partition_path_matches_thomas(cuda_lib, P, L, frozen):
+    """The drop-in's partitioned path (a lone 3-D / 4-D grid as a batch of
+    one) gives densities within 1e-12 relative of the Thomas path, masks
+    included, from host and from device densities alike."""
+    import torch
+    from dadi_gb300 import integration
+    xx = cases.grid("default", L)
+    phi0 = np.abs(cases.initial_phi(3, (L,) * P)) + 1e-3
+    tab = table_rows(P, 40, 77)
+    saved = integration.nd_line_solver
+    integration.nd_line_solver = "partition"
+    try:
+        assert integration.partition_segments(P, L) > 0
+        part = integration.run_table(phi0, xx, tab, frozen, 0)
+        dev = integration.run_table(torch.from_numpy(phi0).cuda(), xx, tab, frozen, 0)
+    finally:
+        integration.nd_line_solver = saved
+    assert np.array_equal(dev.cpu().numpy(), part)
+    th = _alone(phi0, xx, tab, frozen)
+    rel = np.max(np.abs(part - th) / np.maximum(np.abs(th), 1e-12 * np.abs(th).max()))
+    assert rel < 1e-12, rel
+
+
+def test_dropin_auto_line_solver_is_tuned_per_shape(cuda_lib):
+    """"auto" asks the autotuner once per shape: the partition for a 3-D
+    grid of 60 points (few lines: measured 1.9x), a cached answer the second
+    time; never for the delj trick or two populations."""
+    from dadi_gb300 import autotune, integration
+    assert integration.nd_line_solver == "auto"
+    t = autotune.tune_nd_line_solver(3, 60)
+    assert t["segments"] in (2, 4, 8) and set(t["ms"]) >= {0, 2, 4, 8}
+    assert autotune.tune_nd_line_solver(3, 60) is t
+    assert integration.partition_segments(3, 60) == t["segments"]
+    assert integration.partition_segments(3, 70, delj=True) == 0
+    assert integration.partition_segments(2, 100) == 0
