@@ -56,10 +56,10 @@ FLOPS_PER_PS = 30      # algorithmic FP64 flops per point-sweep (reference formu
 FP64_INSTR_PER_PS = 10.4
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the integration of one
 # full step of this workload, by launch mode: one mixed launch, or the three
-# launches of per_grid (L = 100 with two items per CTA 1.06 + 0.318 GB,
-# L = 90 1.04 + 0.244, L = 80 1.02 + 0.191)
+# launches of per_grid (L = 100 and L = 80 with two items per CTA: 1.061 +
+# 0.319 GB and 0.997 + 0.176 GB; L = 90 one item per CTA: 1.033 + 0.245 GB)
 K2_TRAFFIC_BYTES = {"persistent": 2.89e9 + 0.886e9,
-                    "per_grid": (1.06 + 1.04 + 1.02) * 1e9 + (318.36 + 243.98 + 191.32) * 1e6}
+                    "per_grid": (1.0611 + 1.0325 + 0.9971) * 1e9 + (318.70 + 244.73 + 175.57) * 1e6}
 
 
 def im_draws(n, seed):

@@ -659,6 +659,111 @@ extern "C" size_t dgb_batchnd_workspace_bytes(int ndim, int L, int nitems,
     return (p.coef_doubles + p.gam_doubles) * sizeof(double) + 256;
 }
 
+namespace dgb {
+
+// The records kernel's shared memory (the grid constants).
+static int batch_coef_prepare(bool delj, size_t &csmem, int L)
+{
+    csmem = (size_t)nd_grid_doubles(L) * sizeof(double);
+    return (delj ? raise_smem_limit(k_coef_batch<true>) : raise_smem_limit(k_coef_batch<false>))
+               ? DGB_ERR_CUDA
+               : DGB_OK;
+}
+
+// One sweep along B.A.axis at step s over the first nact items, with the
+// plan's line solver.
+static int batch_sweep(NDBatch &B, const BatchPlan &p, long nact, long s, bool delj,
+                       cudaStream_t st)
+{
+    if (p.pcr) {
+        k_sweep_batch_pcr<<<(unsigned)(nact * B.bpi), 32 * PCR_LINES, p.smem, st>>>(B, s);
+        return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
+    }
+    if (p.seg)
+        return (p.seg == 2)   ? batch_part_launch<2>(B, nact, p.smem, s, st)
+               : (p.seg == 4) ? batch_part_launch<4>(B, nact, p.smem, s, st)
+                              : batch_part_launch<8>(B, nact, p.smem, s, st);
+    if (delj)
+        return p.gsmem ? batch_sweep_launch<true, true>(B, nact, p.smem, p.nt, s, st)
+                       : batch_sweep_launch<true, false>(B, nact, p.smem, p.nt, s, st);
+    return p.gsmem ? batch_sweep_launch<false, true>(B, nact, p.smem, p.nt, s, st)
+                   : batch_sweep_launch<false, false>(B, nact, p.smem, p.nt, s, st);
+}
+
+static void batch_set_axis(NDBatch &B, int ax)
+{
+    B.A.axis = ax;
+    B.A.S = ipow(B.A.L, B.A.ndim - 1 - ax);
+    B.A.LS = B.A.S * B.A.L;
+}
+
+// Densities recorded by the batched forward of the adjoint: before step s
+// of every item with s <= nsteps (s == nsteps: its final density),
+// states[state_off + s N] = phi_all[phi_off].  blockIdx.y = item.
+__global__ void k_store_states(const dgb_itemnd_adj *items, const double *phi_all,
+                               double *states_all, long s, long N)
+{
+    const dgb_itemnd_adj I = items[blockIdx.y];
+    if (s > I.nsteps)
+        return;
+    const double *src = phi_all + I.phi_off;
+    double *dst = states_all + I.state_off + s * N;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+         i += (long)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+// The time loop of a batch: records per chunk of steps, one sweep launch per
+// step and axis over the items still running; with `adj` (the same items as
+// adjoint records, device) every density is recorded as k_store_states
+// says.
+static int batch_loop(NDBatch &B, const BatchPlan &p, const int *nsteps, int nitems, bool delj,
+                      const dgb_itemnd_adj *adj, double *states_all, cudaStream_t st)
+{
+    const int ndim = B.A.ndim, L = B.A.L;
+    const long N = ipow(L, ndim);
+    size_t csmem;
+    if (batch_coef_prepare(delj, csmem, L))
+        return DGB_ERR_CUDA;
+    long nact = nitems;
+    const long total = nsteps[0];
+    for (long s = 0; s <= total; s++) {
+        if (adj) {
+            long nrec = nitems; // items with s <= nsteps: a prefix
+            while (nrec > 0 && nsteps[nrec - 1] < s)
+                nrec--;
+            const dim3 grid((unsigned)std::min<long>((N + 255) / 256, 64), (unsigned)nrec);
+            k_store_states<<<grid, 256, 0, st>>>(adj, B.phi_all, states_all, s, N);
+            if (cudaGetLastError() != cudaSuccess)
+                return DGB_ERR_CUDA;
+        }
+        if (s == total)
+            break;
+        while (nact > 0 && nsteps[nact - 1] <= s)
+            nact--;
+        if (s % p.chunk == 0) {
+            B.step0 = s;
+            const int nsl = (int)std::min<long>(p.chunk, total - s);
+            const unsigned grid = (unsigned)(nact * nsl * ndim);
+            if (delj)
+                k_coef_batch<true><<<grid, 128, csmem, st>>>(B, nsl);
+            else
+                k_coef_batch<false><<<grid, 128, csmem, st>>>(B, nsl);
+            if (cudaGetLastError() != cudaSuccess)
+                return DGB_ERR_CUDA;
+        }
+        for (int ax = 0; ax < ndim; ax++) {
+            batch_set_axis(B, ax);
+            int rc = batch_sweep(B, p, nact, s, delj, st);
+            if (rc)
+                return rc;
+        }
+    }
+    return DGB_OK;
+}
+
+} // namespace dgb
+
 extern "C" int dgb_batchnd_integrate(const dgb_itemnd *items, const int *nsteps, int nitems,
                                      int ndim, int L, const double *xx, double *phi_all,
                                      const double *table, const dgb_settings *settings,
@@ -678,7 +783,6 @@ extern "C" int dgb_batchnd_integrate(const dgb_itemnd *items, const int *nsteps,
         return rc;
     if (!ws || ws_bytes < (p.coef_doubles + p.gam_doubles) * sizeof(double))
         return DGB_ERR_WORKSPACE;
-    cudaStream_t st = (cudaStream_t)stream;
     const bool delj = settings->use_delj_trick != 0;
     NDBatch B = {};
     nd_fill(B.A, phi_all, ndim, L, 0, xx);
@@ -690,54 +794,7 @@ extern "C" int dgb_batchnd_integrate(const dgb_itemnd *items, const int *nsteps,
     B.item_coef = (long)p.chunk * ndim * (long)nd_rec_doubles(L, delj);
     B.bpi = p.bpi;
     B.gam_glob = p.gsmem ? nullptr : (double *)ws + p.coef_doubles;
-    const size_t csmem = (size_t)nd_grid_doubles(L) * sizeof(double);
-    if (delj ? raise_smem_limit(k_coef_batch<true>) : raise_smem_limit(k_coef_batch<false>))
-        return DGB_ERR_CUDA;
-    long nact = nitems;
-    const long total = nsteps[0];
-    for (long s = 0; s < total; s++) {
-        while (nact > 0 && nsteps[nact - 1] <= s)
-            nact--;
-        if (s % p.chunk == 0) {
-            B.step0 = s;
-            const int nsl = (int)std::min<long>(p.chunk, total - s);
-            const unsigned grid = (unsigned)(nact * nsl * ndim);
-            if (delj)
-                k_coef_batch<true><<<grid, 128, csmem, st>>>(B, nsl);
-            else
-                k_coef_batch<false><<<grid, 128, csmem, st>>>(B, nsl);
-            if (cudaGetLastError() != cudaSuccess)
-                return DGB_ERR_CUDA;
-        }
-        for (int ax = 0; ax < ndim; ax++) {
-            B.A.axis = ax;
-            B.A.S = ipow(L, ndim - 1 - ax);
-            B.A.LS = B.A.S * L;
-            if (p.pcr) {
-                k_sweep_batch_pcr<<<(unsigned)(nact * B.bpi), 32 * PCR_LINES, p.smem, st>>>(B, s);
-                if (cudaGetLastError() != cudaSuccess)
-                    return DGB_ERR_CUDA;
-                continue;
-            }
-            if (p.seg) {
-                rc = (p.seg == 2)   ? batch_part_launch<2>(B, nact, p.smem, s, st)
-                     : (p.seg == 4) ? batch_part_launch<4>(B, nact, p.smem, s, st)
-                                    : batch_part_launch<8>(B, nact, p.smem, s, st);
-                if (rc)
-                    return rc;
-                continue;
-            }
-            if (delj)
-                rc = p.gsmem ? batch_sweep_launch<true, true>(B, nact, p.smem, p.nt, s, st)
-                             : batch_sweep_launch<true, false>(B, nact, p.smem, p.nt, s, st);
-            else
-                rc = p.gsmem ? batch_sweep_launch<false, true>(B, nact, p.smem, p.nt, s, st)
-                             : batch_sweep_launch<false, false>(B, nact, p.smem, p.nt, s, st);
-            if (rc)
-                return rc;
-        }
-    }
-    return DGB_OK;
+    return batch_loop(B, p, nsteps, nitems, delj, nullptr, nullptr, (cudaStream_t)stream);
 }
 
 // ------------------------------------------- parametric schedules (host)

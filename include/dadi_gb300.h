@@ -366,6 +366,37 @@ int dgb_batchnd_integrate(const dgb_itemnd *items, const int *nsteps, int nitems
                           const dgb_settings *settings, void *ws, size_t ws_bytes,
                           void *stream);
 
+/* The discrete adjoint of many N-dimensional integrations at once: the
+ * batched forms of dgb_integrate_table_states and dgb_adjoint_table_nd
+ * (the same per-step records, recomputation and transposed sweeps, every
+ * sweep launch over the lines of every integration still running; each
+ * integration's states, lambda and gpart are bitwise those of the
+ * one-at-a-time calls).  Items are HOST arrays here, nitems of them sorted
+ * longest first; each names its density (phi_all + phi_off: the initial
+ * density on entry of the forward, dJ/dphi_final on entry of the adjoint,
+ * dJ/dphi_initial on its exit), its table rows, its nsteps + 1 recorded
+ * densities (states_all + state_off) and its nsteps x
+ * dgb_adjoint_table_nd_gpart_doubles(ndim, L) partial rows (gpart_all +
+ * gpart_off, laid out as dgb_adjoint_table_nd's, each step's rows by axis).
+ * Thomas line solver; without the delj trick (DGB_ERR_UNSUPPORTED).
+ * ws: dgb_batchnd_adjoint_workspace_bytes (records, Thomas scratch, the
+ * recomputed sweep outputs: (ndim - 1) L^ndim doubles per item). */
+typedef struct {
+    long phi_off, row_off, state_off, gpart_off; /* in doubles / rows */
+    int nsteps;
+    int masks; /* frozen_mask | nomut_mask << 8 */
+} dgb_itemnd_adj;
+size_t dgb_batchnd_adjoint_workspace_bytes(int ndim, int L, int nitems,
+                                           const dgb_settings *settings);
+int dgb_batchnd_integrate_states(const dgb_itemnd_adj *items, int nitems, int ndim, int L,
+                                 const double *xx, double *phi_all, const double *table,
+                                 double *states_all, const dgb_settings *settings, void *ws,
+                                 size_t ws_bytes, void *stream);
+int dgb_batchnd_adjoint(const dgb_itemnd_adj *items, int nitems, int ndim, int L,
+                        const double *xx, double *lam_all, const double *table,
+                        const double *states_all, double *gpart_all,
+                        const dgb_settings *settings, void *ws, size_t ws_bytes, void *stream);
+
 /* One P-population integration (P = 1-5) in parametric form: the arguments
  * of Integration.one_pop .. five_pops (dadi/Integration.py:178-937) with
  * every parameter a dgb_pform; mig[k][j] is the rate into population k from
