@@ -630,18 +630,28 @@ def run_adjoint(a, obs):
     fs3, _ = m3.spectrum_ll(th0)
     obs3 = np.random.default_rng(0).poisson(1e4 * np.abs(fs3.cpu().numpy())).astype(float)
     d3 = torch.from_numpy(obs3).cuda()
-    m3.loglik_and_grad(sets[0], d3, 1e4)
+    m3.loglik_and_grad_batch(sets[:2], d3, 1e4)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    res = m3.loglik_and_grad_many(sets, d3, 1e4, workers=4)
+    res = m3.loglik_and_grad_batch(sets, d3, 1e4)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     finite = all(bool(torch.isfinite(g).all()) for _, g, _ in res)
+    t0 = time.perf_counter()
+    res4 = m3.loglik_and_grad_many(sets, d3, 1e4, workers=4)
+    torch.cuda.synchronize()
+    wall4 = time.perf_counter() - t0
+    same = all(torch.equal(a[1], b[1]) for a, b in zip(res, res4))
     out["growth3"] = {"sets": 32, "pts": 80, "ns": [20, 20, 20], "wall_s": wall,
                       "gradients_per_s": 32 / wall, "finite": finite,
-                      "note": "four sets at a time on their own streams; host wall clock "
-                              "(forward with every step's density kept, adjoint, table "
-                              "derivatives)"}
+                      "streams_wall_s": wall4, "streams_gradients_per_s": 32 / wall4,
+                      "bitwise_equal": same,
+                      "note": "host wall clock of loglik_and_grad_batch: the sets in groups "
+                              "whose recorded densities fit 48 GB, every sweep launch over "
+                              "all the sets of a group (forward recording every step's "
+                              "density, the loss tails, the adjoint, the table derivatives); "
+                              "streams_*: loglik_and_grad_many, four sets at a time on their "
+                              "own streams"}
     return out
 
 

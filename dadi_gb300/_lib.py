@@ -36,7 +36,8 @@ EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
            "dgb_adjoint_table_nd_gpart_doubles", "dgb_adjoint_table_nd",
            "dgb_batchnd_workspace_bytes", "dgb_batchnd_integrate", "dgb_schednd_host",
            "dgb_from_phi_nd_workspace_bytes", "dgb_from_phi_nd", "dgb_adjoint2d_traj_ws_bytes",
-           "dgb_adjoint2d_traj", "dgb_schednd_dual_host"]
+           "dgb_adjoint2d_traj", "dgb_schednd_dual_host", "dgb_batchnd_adjoint_workspace_bytes",
+           "dgb_batchnd_integrate_states", "dgb_batchnd_adjoint"]
 
 
 class PForm(ctypes.Structure):
@@ -71,6 +72,12 @@ class SeedND(ctypes.Structure):
 
 class ItemND(ctypes.Structure):
     _fields_ = [("phi_off", ctypes.c_long), ("row_off", ctypes.c_long),
+                ("nsteps", ctypes.c_int), ("masks", ctypes.c_int)]
+
+
+class ItemNDAdj(ctypes.Structure):
+    _fields_ = [("phi_off", ctypes.c_long), ("row_off", ctypes.c_long),
+                ("state_off", ctypes.c_long), ("gpart_off", ctypes.c_long),
                 ("nsteps", ctypes.c_int), ("masks", ctypes.c_int)]
 
 
@@ -135,6 +142,11 @@ def _declare(L):
         "dgb_schednd_host": (i, [_vp, i, ctypes.POINTER(Settings), lg, d, _vp, _vp, _vp, _vp]),
         "dgb_schednd_dual_host": (i, [_vp, _vp, i, ctypes.POINTER(Settings), lg, d, _vp, _vp,
                                       _vp, _vp]),
+        "dgb_batchnd_adjoint_workspace_bytes": (sz, [i, i, i, ctypes.POINTER(Settings)]),
+        "dgb_batchnd_integrate_states": (i, [_vp, i, i, i, _vp, _vp, _vp, _vp,
+                                             ctypes.POINTER(Settings), _vp, sz, _vp]),
+        "dgb_batchnd_adjoint": (i, [_vp, i, i, i, _vp, _vp, _vp, _vp, _vp,
+                                    ctypes.POINTER(Settings), _vp, sz, _vp]),
         "dgb_from_phi_nd_workspace_bytes": (sz, [i, i, _vp, i]),
         "dgb_from_phi_nd": (i, [_vp, i, i, i, _vp, _vp, _vp, _vp, _vp, _vp, sz, _vp]),
         "dgb_adjoint2d_traj_ws_bytes": (sz, [i, i]),

@@ -166,6 +166,17 @@ def schedule_dual(rec, seed, npar, xx, max_steps=10 ** 7):
     return table[:n.value], drows[:n.value]
 
 
+def _row_grads(torch, gpart, n, per, stride, drows):
+    """d J / d theta from one integration's per-step partial rows (n steps of
+    `per` doubles: the CTAs' rows, then the injection's dt and theta0 terms)
+    and the table's derivatives drows (n, stride, npar)."""
+    gp = gpart.view(n, per)
+    G = gp[:, :per - 2].reshape(n, -1, stride).sum(dim=1)
+    G[:, 0] += gp[:, per - 2]
+    G[:, 1] += gp[:, per - 1]
+    return torch.einsum("kj,kjp->p", G, _lib.to_device(torch, drows))
+
+
 class TableModel:
     """An N-population model run through parameter tables on the GPU, with
     the gradient of its Poisson log-likelihood by the discrete adjoint.
@@ -266,15 +277,102 @@ class TableModel:
                 _lib.dptr(lam), P, L, _lib.dptr(r["d_xx"]), _lib.dptr(r["d_tab"]), n, 0, 0,
                 _lib.dptr(r["states"]), _lib.dptr(gpart), _lib.dptr(ws), nws,
                 _lib.stream_handle(torch)), "dgb_adjoint_table_nd")
-            gp = gpart.view(n, per)
-            G = gp[:, :per - 2].reshape(n, -1, stride).sum(dim=1)
-            G[:, 0] += gp[:, per - 2]
-            G[:, 1] += gp[:, per - 1]
-            D = _lib.to_device(torch, r["drows"])
-            grad += torch.einsum("kj,kjp->p", G, D)
+            grad += _row_grads(torch, gpart, n, per, stride, r["drows"])
             r["states"] = None
         return ll.detach(), grad, fs.detach()
 
+
+    #: Bytes of recorded densities one batched gradient pass may hold; more
+    #: parameter sets are taken in groups of about equal size.
+    states_budget = 48 << 30
+
+    def loglik_and_grad_batch(self, thetas, data, scale=1.0):
+        """loglik_and_grad for many parameter sets at once: per grid one
+        batched forward recording every step's density
+        (dgb_batchnd_integrate_states), each set's loss tail by autograd, and
+        one batched adjoint (dgb_batchnd_adjoint), so that every sweep launch
+        carries the lines of all the sets.  Returns [(ll, grad, fs)] in the
+        order of thetas, each bitwise the one-at-a-time result."""
+        torch = self.torch
+        thetas = [np.asarray(t, dtype=np.float64) for t in thetas]
+        d = data if torch.is_tensor(data) else _lib.to_device(torch, data)
+        tabs = [[self.table(th, xx) for xx in self.xxs] for th in thetas]
+        nbytes = [sum(8 * (len(tabs[i][g][0]) + 1) * L ** self.P
+                      for g, L in enumerate(self.pts_l)) for i in range(len(thetas))]
+        ngroups = max(1, -(-sum(nbytes) // int(self.states_budget)))
+        bounds = np.searchsorted(np.cumsum(nbytes), np.arange(1, ngroups) * sum(nbytes) / ngroups)
+        out = [None] * len(thetas)
+        for grp in np.split(np.arange(len(thetas)), bounds):
+            if len(grp):
+                self._grad_group([int(i) for i in grp], tabs, d, scale, out)
+        return out
+
+    def _grad_group(self, grp, tabs, d, scale, out):
+        torch, lib = self.torch, _lib.lib()
+        P, m = self.P, len(grp)
+        st = _lib.settings_struct(*integration.current_settings())
+        sh = _lib.stream_handle(torch)
+        stride = integration.row_stride(P)
+        runs = []
+        for g, (L, xx) in enumerate(zip(self.pts_l, self.xxs)):
+            N = L ** P
+            steps = np.array([len(tabs[i][g][0]) for i in grp], dtype=np.int64)
+            order = np.argsort(-steps, kind="stable")
+            per = int(lib.dgb_adjoint_table_nd_gpart_doubles(P, L))
+            items = (_lib.ItemNDAdj * m)()
+            slot = np.empty(m, dtype=np.int64)   # set (position in grp) -> slot
+            row = state = gp = 0
+            for pos, j in enumerate(order):
+                it = items[pos]
+                it.phi_off, it.row_off, it.state_off, it.gpart_off = pos * N, row, state, gp
+                it.nsteps, it.masks = int(steps[j]), 0
+                slot[j] = pos
+                row += int(steps[j])
+                state += (int(steps[j]) + 1) * N
+                gp += int(steps[j]) * per
+            table = np.concatenate([tabs[grp[j]][g][0] for j in order] +
+                                   [np.zeros((1, stride))])
+            phi = _lib.to_device(torch, self.initial(xx)).reshape(1, N).expand(m, N).contiguous()
+            states = torch.empty(max(state, 1), dtype=torch.float64, device="cuda")
+            gpart = torch.empty(max(gp, 1), dtype=torch.float64, device="cuda")
+            d_xx, d_tab = _lib.to_device(torch, xx), _lib.to_device(torch, table)
+            ws, nws = _lib.workspace(torch, lib.dgb_batchnd_adjoint_workspace_bytes(
+                P, L, m, ctypes.byref(st)))
+            _lib.check(lib.dgb_batchnd_integrate_states(
+                ctypes.byref(items), m, P, L, _lib.dptr(d_xx), _lib.dptr(phi), _lib.dptr(d_tab),
+                _lib.dptr(states), ctypes.byref(st), _lib.dptr(ws), nws, sh),
+                "dgb_batchnd_integrate_states")
+            runs.append(dict(L=L, N=N, per=per, items=items, slot=slot, phi=phi, states=states,
+                             gpart=gpart, d_xx=d_xx, d_tab=d_tab, ws=ws, nws=nws,
+                             lam=torch.zeros_like(phi)))
+        for k, i in enumerate(grp):
+            phis = [r["phi"][r["slot"][k]].view((r["L"],) * P).detach().requires_grad_(True)
+                    for r in runs]
+            with torch.enable_grad():
+                fs, ll = self._tail(phis, d, scale)
+            lams = torch.autograd.grad(ll, phis, allow_unused=True)
+            for r, lam in zip(runs, lams):
+                if lam is not None:
+                    r["lam"][r["slot"][k]] = lam.reshape(-1)
+            out[i] = (ll.detach(), fs.detach())
+        for r in runs:
+            _lib.check(lib.dgb_batchnd_adjoint(
+                ctypes.byref(r["items"]), m, P, r["L"], _lib.dptr(r["d_xx"]),
+                _lib.dptr(r["lam"]), _lib.dptr(r["d_tab"]), _lib.dptr(r["states"]),
+                _lib.dptr(r["gpart"]), ctypes.byref(st), _lib.dptr(r["ws"]), r["nws"], sh),
+                "dgb_batchnd_adjoint")
+            r["states"] = None
+        for k, i in enumerate(grp):
+            grad = torch.zeros(self.npar, dtype=torch.float64, device="cuda")
+            for g, r in enumerate(runs):
+                n = len(tabs[i][g][0])
+                if n == 0:
+                    continue
+                it = r["items"][int(r["slot"][k])]
+                gpart = r["gpart"][it.gpart_off:it.gpart_off + n * r["per"]]
+                grad += _row_grads(torch, gpart, n, r["per"], stride, tabs[i][g][1])
+            ll, fs = out[i]
+            out[i] = (ll, grad, fs)
 
     def loglik_and_grad_many(self, thetas, data, scale=1.0, workers=4):
         """loglik_and_grad for several parameter sets, `workers` at a time on

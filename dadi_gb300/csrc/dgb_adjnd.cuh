@@ -19,16 +19,20 @@ struct ADNArgs {
     long rec_off;       // offset of this integration's records after the grid constants
 };
 
-__host__ __device__ inline size_t adn_smem_doubles(int L, int nt)
+// Shared memory of an adjoint sweep CTA: the forward sweep's (tile, gam
+// unless it sits in a workspace slice, grid constants, vectors), the
+// transposed vectors and four per-interval contraction factors.
+__host__ __device__ inline size_t adn_smem_doubles(int L, int nt, bool gsmem = true)
 {
-    return nd_smem_doubles(L, nt, false) + 5 * (size_t)L;
+    return (size_t)L * (nt + 1) + (gsmem ? (size_t)L * nt : 0) + 20 * (size_t)L;
 }
 
 // The transposed sweep and contraction of tile `tile_idx` (nt lines from
 // tile_idx * nt) of one integration: the body of k_adjoint_sweep_nd and of the
 // batched k_adjoint_sweep_batch.  Called by the whole CTA.
 __device__ __forceinline__ void adn_tile(const ADNArgs &A, long tile_idx, double *smem,
-                                         NDShared &Sh, double (*red)[8])
+                                         NDShared &Sh, double (*red)[8],
+                                         double *gam_slice = nullptr)
 {
     const NDArgs &N = A.nd;
     const int nt = blockDim.x, L = N.L, P = N.ndim, ax = N.axis, tid = threadIdx.x;
@@ -36,13 +40,31 @@ __device__ __forceinline__ void adn_tile(const ADNArgs &A, long tile_idx, double
     double *tile, *gam;
     GridVecs g;
     AxisVecs v, vt;
-    nd_carve(smem, L, nt, false, tile, gam, g, v);
+    if (gam_slice) {
+        // the Thomas scratch in this CTA's workspace slice: the shared
+        // memory holds the tile and the vectors only
+        tile = smem;
+        gam = gam_slice;
+        double *q = smem + (size_t)L * (nt + 1);
+        g.x = q; q += L;
+        g.xv = q; q += L;
+        g.dfac = q; q += L;
+        g.xInt = q; q += L;
+        g.ih = q; q += L;
+        g.dx = q; q += L;
+        nd_vecs_at(q, L, false, v);
+    } else {
+        nd_carve(smem, L, nt, false, tile, gam, g, v);
+    }
     double *p = v.B0 + L;
     vt.A1 = p; p += L;
     vt.A0 = p; p += L;
     vt.C1 = p; p += L;
     vt.C0 = p; p += L;
-    vt.B0 = p;
+    vt.B0 = p; p += L;
+    // per interval i, for the contraction below: cP, cQ (the nu terms), gS,
+    // hS (the selection terms' gamma and h factors)
+    double *cP = p, *cQ = p + L, *gS = p + 2 * L, *hS = p + 3 * L;
     if (A.coef) {
         // the grid constants and this step's record, in the carve order
         const double *rec = A.coef + nd_grid_doubles(L) + A.rec_off +
@@ -74,6 +96,17 @@ __device__ __forceinline__ void adn_tile(const ADNArgs &A, long tile_idx, double
         vt.C1[i] = (i < L - 1) ? v.A1[i + 1] : 0.0;
         vt.C0[i] = (i < L - 1) ? v.A0[i + 1] : 0.0;
         vt.B0[i] = v.B0[i];
+        if (i < L - 1) {
+            // with w = D_i (u_i + u_{i+1}) (twice D_i times the mean density):
+            // d/dnu: D_i (Q_i u_{i+1} - P_i u_i) / nu = D_i (cQ u_{i+1} - cP u_i);
+            // d/dgamma, d/dh of the selection term times D_i hp: w gS, w hS
+            const double inu = Sh.s.inv_nu, hh = Sh.s.h, gm = Sh.s.gamma;
+            const double xi = g.xInt[i], xx1 = xi * (1. - xi);
+            cP[i] = inu * inu * g.xv[i] * g.ih[i];
+            cQ[i] = inu * inu * g.xv[i + 1] * g.ih[i];
+            gS[i] = (hh + (1. - 2 * hh) * xi) * xx1;
+            hS[i] = gm * (1. - 2 * xi) * xx1;
+        }
     }
     const long l0 = tile_idx * nt;
     const int n = (int)min((long)nt, N.nlines - l0);
@@ -117,10 +150,11 @@ __device__ __forceinline__ void adn_tile(const ADNArgs &A, long tile_idx, double
         const double dt = s.dt, inu = s.inv_nu, gm = s.gamma, hh = s.h;
         const double inj0 = (n1 == 1 && k1 >= 0) ? Sh.inj[k1] : 0.0; // point 0 of this line
         const double inj1 = (n1 == 0) ? Sh.inj[ax] : 0.0;             // point 1 of this line
-        double smr = 0, smp = 0, snu = 0, sg = 0, sh = 0, sm[DGB_MAX_DIM];
-        for (int k = 0; k < P; k++)
-            sm[k] = 0;
+        // the migration terms D_i (x_k - xInt_i) hp of every other population
+        // k from two sums: s1 = sum w, s2 = sum w xInt_i
+        double smr = 0, smp = 0, snu = 0, sg = 0, sh = 0, s1 = 0, s2 = 0;
         double mi = tile[tid], ui = u[0];
+        double dmi = g.dfac[0] * mi;
         for (int i = 0; i < L; i++) {
             double ri = r[i * S];
             if (i == 0)
@@ -131,22 +165,22 @@ __device__ __forceinline__ void adn_tile(const ADNArgs &A, long tile_idx, double
             smp = fma(mi, ui, smp);
             if (i < L - 1) {
                 const double mn = tile[(i + 1) * tp + tid], un = u[(i + 1) * S];
-                const double xi = g.xInt[i];
-                const double Pi = inu * g.xv[i] * g.ih[i];
-                const double Qi = inu * g.xv[i + 1] * g.ih[i];
-                const double Di = g.dfac[i] * mi - g.dfac[i + 1] * mn;
-                const double hp = 0.5 * (ui + un);
-                const double xx1 = xi * (1. - xi);
-                snu = fma(Di, (Qi * un - Pi * ui) * inu, snu);
-                for (int k = 0; k < P; k++)
-                    if (k != ax)
-                        sm[k] = fma(Di * (oo[k] - xi), hp, sm[k]);
-                sg = fma(Di * (2 * (hh + (1. - 2 * hh) * xi) * xx1), hp, sg);
-                sh = fma(Di * (gm * 2 * (1. - 2 * xi) * xx1), hp, sh);
+                const double dmn = g.dfac[i + 1] * mn;
+                const double Di = dmi - dmn;
+                const double w = Di * (ui + un);
+                snu = fma(Di, fma(-cP[i], ui, cQ[i] * un), snu);
+                s1 += w;
+                s2 = fma(w, g.xInt[i], s2);
+                sg = fma(w, gS[i], sg);
+                sh = fma(w, hS[i], sh);
                 mi = mn;
                 ui = un;
+                dmi = dmn;
             }
         }
+        double sm[DGB_MAX_DIM];
+        for (int k = 0; k < P; k++)
+            sm[k] = 0.5 * fma(oo[k], s1, -s2);
         double bnu = 0, bg = 0, bh = 0, bmf = 0, bml = 0;
         if (bs != 0.0) {
             const double x0 = g.x[0], f = dt * 2. / g.dx[0], w = tile[tid] * u[0];

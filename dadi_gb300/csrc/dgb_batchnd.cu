@@ -25,7 +25,9 @@
 #include <algorithm>
 #include <cmath>
 
-#include "dgb_nd.cuh"
+#include <vector>
+
+#include "dgb_adjnd.cuh"
 
 namespace dgb {
 
@@ -795,6 +797,347 @@ extern "C" int dgb_batchnd_integrate(const dgb_itemnd *items, const int *nsteps,
     B.bpi = p.bpi;
     B.gam_glob = p.gsmem ? nullptr : (double *)ws + p.coef_doubles;
     return batch_loop(B, p, nsteps, nitems, delj, nullptr, nullptr, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------- the batched adjoint
+
+namespace dgb {
+
+// First and last unfrozen axis of an integration.
+__host__ __device__ inline int first_active(int frozen, int P)
+{
+    for (int a = 0; a < P; a++)
+        if (!(frozen >> a & 1))
+            return a;
+    return P;
+}
+__host__ __device__ inline int last_active(int frozen, int P)
+{
+    for (int a = P - 1; a >= 0; a--)
+        if (!(frozen >> a & 1))
+            return a;
+    return -1;
+}
+
+// The recomputation of step k's intermediate sweep outputs, per item in
+// its scratch slots (slot a = the density after the step's sweep of axis
+// a): slot[ax] = (ax == 0 ? states[k] : slot[ax - 1]) before the sweep of
+// axis ax is run on it in place (a frozen axis leaves the copy, so slot[a]
+// is always the output of the last unfrozen axis <= a).  blockIdx.y = item.
+__global__ void k_slot_copy(const dgb_itemnd_adj *items, const double *states_all,
+                            double *scratch, long slot_stride, long k, int ax, long N)
+{
+    const dgb_itemnd_adj I = items[blockIdx.y];
+    if (k >= I.nsteps)
+        return;
+    double *base = scratch + (long)blockIdx.y * slot_stride;
+    const double *src = ax ? base + (long)(ax - 1) * N : states_all + I.state_off + k * N;
+    double *dst = base + (long)ax * N;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+         i += (long)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+struct ADNBatch {
+    ADNArgs a; // shape, axis, step, records (coef, step0); per item below
+    const dgb_itemnd_adj *items;
+    double *lam_all;
+    const double *states_all, *scratch;
+    double *gpart_all;
+    double *gam; // per-CTA Thomas scratch slices of L x nt doubles
+    long N, slot_stride, item_coef, per_step;
+    int bpi, nb;
+};
+
+// The transposed sweep of axis a.nd.axis at step a.nd.step for the tiles of
+// every running integration: CTA b handles tile b % bpi of item b / bpi,
+// the per-line work of k_adjoint_sweep_nd on that item's lambda, recorded
+// and recomputed densities, records and partial rows.
+__global__ void k_adjoint_sweep_batch(ADNBatch B)
+{
+    extern __shared__ __align__(16) double smem[];
+    __shared__ NDShared Sh;
+    __shared__ double red[ADN_MAXQ][8];
+    const long it = blockIdx.x / B.bpi;
+    const long tl = blockIdx.x - it * B.bpi;
+    const dgb_itemnd_adj I = B.items[it];
+    const int P = B.a.nd.ndim, ax = B.a.nd.axis;
+    const long k = B.a.nd.step;
+    const int frozen = I.masks & 0xff;
+    if (k >= I.nsteps || (frozen >> ax & 1))
+        return;
+    ADNArgs A = B.a;
+    A.nd.phi = B.lam_all + I.phi_off;
+    const double *slots = B.scratch + it * B.slot_stride;
+    A.out = (ax == last_active(frozen, P)) ? B.states_all + I.state_off + (k + 1) * B.N
+                                           : slots + (long)ax * B.N;
+    A.rhs = (ax == first_active(frozen, P)) ? B.states_all + I.state_off + k * B.N
+                                            : slots + (long)(ax - 1) * B.N;
+    int j = 0; // this axis' place among the item's swept axes
+    for (int a = 0; a < ax; a++)
+        j += !(frozen >> a & 1);
+    A.gpart = B.gpart_all + I.gpart_off + k * B.per_step + (long)j * B.nb * row_stride(P);
+    A.rec_off = it * B.item_coef;
+    adn_tile(A, tl, smem, Sh, red,
+             B.gam + (size_t)blockIdx.x * B.a.nd.L * blockDim.x);
+}
+
+// The injection's terms of step k, one thread per running item.
+__global__ void k_adjoint_inject_batch(const dgb_itemnd_adj *items, int nact,
+                                       const double *lam_all, const double *xx,
+                                       const double *table, int P, int L, long k,
+                                       long per_step, long inj_at, double *gpart_all)
+{
+    const int it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= nact)
+        return;
+    const dgb_itemnd_adj I = items[it];
+    const int active = ((1 << P) - 1) & ~(I.masks & 0xff) & ~((I.masks >> 8) & 0xff);
+    if (k >= I.nsteps || !active)
+        return;
+    adn_inject_terms(lam_all + I.phi_off, xx, table + (I.row_off + k) * row_stride(P), P, L,
+                     active, gpart_all + I.gpart_off + k * per_step + inj_at);
+}
+
+// The Thomas plan of the batched forward and recomputation, and where the
+// pieces of the workspace sit: records, Thomas scratch, recomputed slots,
+// the device copies of the items (adjoint records, then plain items for the
+// forward and for each recomputed axis).
+struct AdjLayout {
+    BatchPlan p;
+    int nt, nb; // the transposed sweeps' lines per CTA and CTAs per item
+    size_t coef, gam, slots, gam_adj, items_adj, items_nd, total; // offsets in bytes
+};
+
+static int adj_layout(int ndim, int L, int nitems, const dgb_settings *settings, AdjLayout &w)
+{
+    dgb_settings st = *settings;
+    st.line_solver = 0;
+    if (st.use_delj_trick)
+        return DGB_ERR_UNSUPPORTED;
+    int rc = batch_plan(ndim, L, nitems, &st, w.p);
+    if (rc)
+        return rc;
+    const size_t N = (size_t)ipow(L, ndim);
+    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+    w.coef = 0;
+    w.gam = up(w.p.coef_doubles * sizeof(double));
+    w.slots = w.gam + up(w.p.gam_doubles * sizeof(double));
+    const long nlines = ipow(L, ndim - 1);
+    w.nt = nd_threads(L, nlines);
+    w.nb = (int)((nlines + w.nt - 1) / w.nt);
+    w.gam_adj = w.slots + up((size_t)nitems * (ndim > 1 ? ndim - 1 : 0) * N * sizeof(double));
+    w.items_adj = w.gam_adj + up((size_t)nitems * w.nb * w.nt * L * sizeof(double));
+    w.items_nd = w.items_adj + up((size_t)nitems * sizeof(dgb_itemnd_adj));
+    w.total = w.items_nd + up((size_t)(ndim + 1) * nitems * sizeof(dgb_itemnd));
+    return DGB_OK;
+}
+
+static bool adj_items_ok(const dgb_itemnd_adj *items, int nitems)
+{
+    for (int i = 0; i < nitems; i++)
+        if (items[i].nsteps < 0 || (i > 0 && items[i].nsteps > items[i - 1].nsteps) ||
+            items[i].phi_off < 0 || items[i].row_off < 0 || items[i].state_off < 0 ||
+            items[i].gpart_off < 0)
+            return false;
+    return true;
+}
+
+// The device copies of the items: the adjoint records, the plain items of
+// the forward (phi in phi_all) and, per axis a < ndim - 1, the plain items
+// whose density is the item's recomputation slot a.
+static int adj_upload(const dgb_itemnd_adj *items, int nitems, int ndim, long N,
+                      const AdjLayout &w, char *ws, cudaStream_t st)
+{
+    std::vector<dgb_itemnd> nd((size_t)(ndim + 1) * nitems);
+    const long slot_stride = (long)(ndim - 1) * N;
+    for (int i = 0; i < nitems; i++) {
+        for (int a = 0; a <= ndim; a++) {
+            dgb_itemnd &d = nd[(size_t)a * nitems + i];
+            d.phi_off = a == 0 ? items[i].phi_off : (long)i * slot_stride + (long)(a - 1) * N;
+            d.row_off = items[i].row_off;
+            d.nsteps = items[i].nsteps;
+            d.masks = items[i].masks;
+        }
+    }
+    // pageable sources: each copy returns once its source has been staged
+    if (cudaMemcpyAsync(ws + w.items_adj, items, (size_t)nitems * sizeof(dgb_itemnd_adj),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(ws + w.items_nd, nd.data(), nd.size() * sizeof(dgb_itemnd),
+                        cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return DGB_ERR_CUDA;
+    return DGB_OK;
+}
+
+static void adj_batch(NDBatch &B, const AdjLayout &w, int ndim, int L, const double *xx,
+                      double *phi_all, const double *table, char *ws)
+{
+    B = NDBatch{};
+    nd_fill(B.A, phi_all, ndim, L, 0, xx);
+    B.phi_all = phi_all;
+    B.table = table;
+    B.coef = (double *)(ws + w.coef);
+    B.chunk = w.p.chunk;
+    B.item_coef = (long)w.p.chunk * ndim * (long)nd_rec_doubles(L, false);
+    B.bpi = w.p.bpi;
+    B.gam_glob = w.p.gsmem ? nullptr : (double *)(ws + w.gam);
+}
+
+} // namespace dgb
+
+extern "C" size_t dgb_batchnd_adjoint_workspace_bytes(int ndim, int L, int nitems,
+                                                      const dgb_settings *settings)
+{
+    if (!shape_ok(ndim, L) || nitems < 1 || !settings)
+        return 0;
+    AdjLayout w;
+    if (adj_layout(ndim, L, nitems, settings, w))
+        return 0;
+    return w.total + 256;
+}
+
+extern "C" int dgb_batchnd_integrate_states(const dgb_itemnd_adj *items, int nitems, int ndim,
+                                            int L, const double *xx, double *phi_all,
+                                            const double *table, double *states_all,
+                                            const dgb_settings *settings, void *ws,
+                                            size_t ws_bytes, void *stream)
+{
+    if (!items || nitems < 1 || !xx || !phi_all || !table || !states_all || !settings ||
+        !shape_ok(ndim, L) || !adj_items_ok(items, nitems))
+        return DGB_ERR_ARG;
+    AdjLayout w;
+    int rc = adj_layout(ndim, L, nitems, settings, w);
+    if (rc)
+        return rc;
+    if (!ws || ws_bytes < w.total)
+        return DGB_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *wb = (char *)ws;
+    const long N = ipow(L, ndim);
+    rc = adj_upload(items, nitems, ndim, N, w, wb, st);
+    if (rc)
+        return rc;
+    std::vector<int> nsteps(nitems);
+    for (int i = 0; i < nitems; i++)
+        nsteps[i] = items[i].nsteps;
+    NDBatch B;
+    adj_batch(B, w, ndim, L, xx, phi_all, table, wb);
+    B.items = (const dgb_itemnd *)(wb + w.items_nd);
+    return batch_loop(B, w.p, nsteps.data(), nitems, false,
+                      (const dgb_itemnd_adj *)(wb + w.items_adj), states_all, st);
+}
+
+extern "C" int dgb_batchnd_adjoint(const dgb_itemnd_adj *items, int nitems, int ndim, int L,
+                                   const double *xx, double *lam_all, const double *table,
+                                   const double *states_all, double *gpart_all,
+                                   const dgb_settings *settings, void *ws, size_t ws_bytes,
+                                   void *stream)
+{
+    if (!items || nitems < 1 || !xx || !lam_all || !table || !states_all || !gpart_all ||
+        !settings || !shape_ok(ndim, L) || !adj_items_ok(items, nitems))
+        return DGB_ERR_ARG;
+    AdjLayout w;
+    int rc = adj_layout(ndim, L, nitems, settings, w);
+    if (rc)
+        return rc;
+    if (!ws || ws_bytes < w.total)
+        return DGB_ERR_WORKSPACE;
+    cudaStream_t st = (cudaStream_t)stream;
+    char *wb = (char *)ws;
+    const long N = ipow(L, ndim);
+    const long total = items[0].nsteps;
+    if (total == 0)
+        return DGB_OK;
+    rc = adj_upload(items, nitems, ndim, N, w, wb, st);
+    if (rc)
+        return rc;
+    const long per_step = (long)dgb_adjoint_table_nd_gpart_doubles(ndim, L);
+    for (int i = 0; i < nitems; i++)
+        if (items[i].nsteps &&
+            cudaMemsetAsync(gpart_all + items[i].gpart_off, 0,
+                            (size_t)items[i].nsteps * per_step * sizeof(double),
+                            st) != cudaSuccess)
+            return DGB_ERR_CUDA;
+    const dgb_itemnd *d_nd = (const dgb_itemnd *)(wb + w.items_nd);
+    const dgb_itemnd_adj *d_adj = (const dgb_itemnd_adj *)(wb + w.items_adj);
+    double *slots = (double *)(wb + w.slots);
+    const long slot_stride = (long)(ndim - 1) * N;
+    // the records (and the item list they are indexed by) and the
+    // recomputation sweeps: slot a of item i is phi_all' = slots, items
+    // d_nd + (a + 1) * nitems
+    NDBatch B;
+    adj_batch(B, w, ndim, L, xx, slots, table, wb);
+    B.items = d_nd;
+    size_t csmem;
+    if (batch_coef_prepare(false, csmem, L))
+        return DGB_ERR_CUDA;
+    // the transposed sweeps: the tiles of dgb_adjoint_table_nd, with the
+    // Thomas scratch in workspace slices (twice the CTAs per SM)
+    const int nt = w.nt, nb = w.nb;
+    ADNBatch AB = {};
+    nd_fill(AB.a.nd, nullptr, ndim, L, 0, xx);
+    AB.a.nd.table = table;
+    AB.a.coef = B.coef;
+    AB.items = d_adj;
+    AB.lam_all = lam_all;
+    AB.states_all = states_all;
+    AB.scratch = slots;
+    AB.gpart_all = gpart_all;
+    AB.gam = (double *)(wb + w.gam_adj);
+    AB.N = N;
+    AB.slot_stride = slot_stride;
+    AB.item_coef = B.item_coef;
+    AB.per_step = per_step;
+    AB.bpi = nb;
+    AB.nb = nb;
+    const size_t asmem = adn_smem_doubles(L, nt, false) * sizeof(double);
+    if (raise_smem_limit(k_adjoint_sweep_batch))
+        return DGB_ERR_CUDA;
+    const long inj_at = (long)ndim * nb * row_stride(ndim);
+    const unsigned cpx = (unsigned)std::min<long>((N + 255) / 256, 64);
+    long nact = 0, lo = -1;
+    for (long k = total - 1; k >= 0; k--) {
+        while (nact < nitems && items[nact].nsteps > k)
+            nact++;
+        if (lo < 0 || k < lo) {
+            lo = std::max(0L, k - w.p.chunk + 1);
+            long nrec = 0; // every item running at some step of the chunk
+            while (nrec < nitems && items[nrec].nsteps > lo)
+                nrec++;
+            B.step0 = lo;
+            const int nsl = (int)(k - lo + 1);
+            k_coef_batch<false><<<(unsigned)(nrec * nsl * ndim), 128, csmem, st>>>(B, nsl);
+            if (cudaGetLastError() != cudaSuccess)
+                return DGB_ERR_CUDA;
+        }
+        for (int ax = 0; ax < ndim - 1; ax++) {
+            k_slot_copy<<<dim3(cpx, (unsigned)nact), 256, 0, st>>>(d_adj, states_all, slots,
+                                                                 slot_stride, k, ax, N);
+            if (cudaGetLastError() != cudaSuccess)
+                return DGB_ERR_CUDA;
+            B.items = d_nd + (size_t)(ax + 1) * nitems;
+            batch_set_axis(B, ax);
+            rc = batch_sweep(B, w.p, nact, k, false, st);
+            if (rc)
+                return rc;
+        }
+        B.items = d_nd;
+        AB.a.step0 = lo;
+        for (int ax = ndim - 1; ax >= 0; ax--) {
+            AB.a.nd.axis = ax;
+            AB.a.nd.S = ipow(L, ndim - 1 - ax);
+            AB.a.nd.LS = AB.a.nd.S * L;
+            AB.a.nd.step = k;
+            k_adjoint_sweep_batch<<<(unsigned)(nact * nb), nt, asmem, st>>>(AB);
+            if (cudaGetLastError() != cudaSuccess)
+                return DGB_ERR_CUDA;
+        }
+        k_adjoint_inject_batch<<<(unsigned)((nact + 127) / 128), 128, 0, st>>>(
+            d_adj, (int)nact, lam_all, xx, table, ndim, L, k, per_step, inj_at, gpart_all);
+        if (cudaGetLastError() != cudaSuccess)
+            return DGB_ERR_CUDA;
+    }
+    return DGB_OK;
 }
 
 // ------------------------------------------- parametric schedules (host)

@@ -83,7 +83,8 @@ def test_record_dtypes_match_header(tmp_path, struct, dtype, cfields):
 
 @pytest.mark.parametrize("struct,ctype", [("dgb_settings", "Settings"), ("dgb_pform", "PForm"),
                                           ("dgb_instnd", "InstND"), ("dgb_itemnd", "ItemND"),
-                                          ("dgb_seednd", "SeedND")])
+                                          ("dgb_seednd", "SeedND"),
+                                          ("dgb_itemnd_adj", "ItemNDAdj")])
 def test_ctypes_structs_match_header(tmp_path, struct, ctype):
     """The ctypes structures passed by reference match the C structs (size
     and every field offset)."""
