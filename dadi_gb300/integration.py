@@ -69,12 +69,18 @@ def ensure_1arg_func(var):
 
 def _compute_dt(dx, nu, ms, gamma, h):
     """Timestep from the current parameters (dadi/Integration.py:147-176)."""
-    tsf, otsf, old, _ = current_settings()
+    return _dt_with(current_settings(), dx[0], nu, ms, gamma, h)
+
+
+def _dt_with(settings, dx0, nu, ms, gamma, h):
+    """_compute_dt with the settings read once by the caller (the same
+    arithmetic; abs of a float64 is exact, as numpy's is)."""
+    tsf, otsf, old, _ = settings
     if old:
-        return otsf * dx[0]
+        return otsf * dx0
     maxVM = max(0.25 / nu, sum(ms),
-                abs(gamma) * 2 * max(np.abs(h + (1 - 2 * h) * 0.5) * 0.5 * (1 - 0.5),
-                                     np.abs(h + (1 - 2 * h) * 0.25) * 0.25 * (1 - 0.25)))
+                abs(gamma) * 2 * max(abs(h + (1 - 2 * h) * 0.5) * 0.5 * (1 - 0.5),
+                                     abs(h + (1 - 2 * h) * 0.25) * 0.25 * (1 - 0.25)))
     dt = tsf / maxVM if maxVM > 0 else np.inf
     if dt == 0:
         raise ValueError('Timestep is zero. Values passed in are nu=%f, ms=%s,'
@@ -101,16 +107,18 @@ def build_table(P, xx, T, initial_t, nu_f, mig_f, gamma_f, h_f, theta0_f, beta_f
     h = [f(current_t) for f in h_f]
     offd = [(k, j) for k in range(P) for j in range(P) if j != k]
     mig = {kj: mig_f[kj[0]][kj[1]](current_t) for kj in offd}
-    dx = np.diff(xx)
+    dx0 = xx[1] - xx[0]
+    settings = current_settings()
     rows = []
     hist = [[0, list(nu), [mig[kj] for kj in offd]]]
     stride = row_stride(P)
+    into = [[kj for kj in offd if kj[0] == k] for k in range(P)]
     while current_t < T:
         if P == 1:
-            dt = _compute_dt(dx, nu[0], [0], gamma[0], h[0])
+            dt = _dt_with(settings, dx0, nu[0], [0], gamma[0], h[0])
         else:
-            dt = min(_compute_dt(dx, nu[k], [mig[(k, j)] for j in range(P) if j != k],
-                                 gamma[k], h[k]) for k in range(P))
+            dt = min(_dt_with(settings, dx0, nu[k], [mig[kj] for kj in into[k]], gamma[k], h[k])
+                     for k in range(P))
         this_dt = min(dt, T - current_t)
         next_t = current_t + this_dt
         nu = [f(next_t) for f in nu_f]
@@ -121,21 +129,13 @@ def build_table(P, xx, T, initial_t, nu_f, mig_f, gamma_f, h_f, theta0_f, beta_f
         theta0 = theta0_f(next_t)
         ms = [mig[kj] for kj in offd]
         hist.append([next_t, list(nu), ms])
-        if np.any(np.less([T] + nu + ms + [theta0], 0)):
+        if T < 0 or theta0 < 0 or any(v < 0 for v in nu) or any(v < 0 for v in ms):
             raise ValueError('A time, population size, migration rate, or '
                              'theta0 is < 0. Has the model been mis-specified?')
-        if np.any(np.equal(nu, 0)):
+        if any(v == 0 for v in nu):
             raise ValueError('A population size is 0. Has the model been '
                              'mis-specified?')
-        row = np.empty(stride)
-        row[0] = this_dt
-        row[1] = theta0
-        row[2:2 + P] = nu
-        row[2 + P:2 + 2 * P] = gamma
-        row[2 + 2 * P:2 + 3 * P] = h
-        row[2 + 3 * P] = beta
-        row[3 + 3 * P:] = ms
-        rows.append(row)
+        rows.append([this_dt, theta0] + nu + gamma + h + [beta] + ms)
         current_t = next_t
     table = np.array(rows, dtype=np.float64).reshape(len(rows), stride)
     return table, hist
