@@ -647,7 +647,8 @@ def run_adjoint(a, obs):
                       "streams_wall_s": wall4, "streams_gradients_per_s": 32 / wall4,
                       "bitwise_equal": same,
                       "note": "host wall clock of loglik_and_grad_batch: the sets in groups "
-                              "whose recorded densities fit 48 GB, every sweep launch over "
+                              "whose recorded densities fit half the free device memory "
+                              "(here one group), every sweep launch over "
                               "all the sets of a group (forward recording every step's "
                               "density, the loss tails, the adjoint, the table derivatives); "
                               "streams_*: loglik_and_grad_many, four sets at a time on their "
@@ -879,6 +880,14 @@ def run_profile_kernel(a):
             from dadi_gb300 import numerics, spectrum
             phis = torch.rand(32, 90, 90, 90, dtype=torch.float64, device="cuda")
             spectrum.from_phi_nd_batch(torch, phis, (20, 20, 20), numerics.default_grid(90))
+        elif a.profile == "adjointnd_batch":
+            # 8 three-population gradients at pts 32 as one batch (every
+            # step's density recorded: about 1.5 GB), every sweep launch over
+            # the lines of all 8 sets
+            m = adjoint_nd.Growth3((32,), (10, 10, 10))
+            sets = [adjoint_nd.Growth3.from_model_params(p) for p in growth3_sets(8)]
+            m.loglik_and_grad_batch(sets, torch.ones(11, 11, 11, dtype=torch.float64,
+                                                     device="cuda"), 1.0)
         elif a.profile == "adjointnd":
             m = adjoint_nd.Growth3((40,), (10, 10, 10))
             th = adjoint_nd.Growth3.from_model_params(models.GROWTH3_DEFAULT)
@@ -924,7 +933,7 @@ def main():
                          "steps, twice) for profiler captures, then exit")
     ap.add_argument("--profile", default=None,
                     choices=["epilogue", "sweep3d", "adjoint2d", "adjointnd", "batchnd",
-                             "fromphind", "thomas3d", "part3d"],
+                             "fromphind", "thomas3d", "part3d", "adjointnd_batch"],
                     help="run a small case of another kernel for profiler captures, then exit")
     ap.add_argument("--line-solvers", action="store_true",
                     help="time the batched N-D engine's line solvers on the growth model's "

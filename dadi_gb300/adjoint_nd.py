@@ -282,9 +282,10 @@ class TableModel:
         return ll.detach(), grad, fs.detach()
 
 
-    #: Bytes of recorded densities one batched gradient pass may hold; more
-    #: parameter sets are taken in groups of about equal size.
-    states_budget = 48 << 30
+    #: Bytes of recorded densities one batched gradient pass may hold (None:
+    #: half the device memory free at the call); more parameter sets are
+    #: taken in groups of about equal size.
+    states_budget = None
 
     def loglik_and_grad_batch(self, thetas, data, scale=1.0):
         """loglik_and_grad for many parameter sets at once: per grid one
@@ -299,7 +300,10 @@ class TableModel:
         tabs = [[self.table(th, xx) for xx in self.xxs] for th in thetas]
         nbytes = [sum(8 * (len(tabs[i][g][0]) + 1) * L ** self.P
                       for g, L in enumerate(self.pts_l)) for i in range(len(thetas))]
-        ngroups = max(1, -(-sum(nbytes) // int(self.states_budget)))
+        budget = self.states_budget
+        if budget is None:
+            budget = torch.cuda.mem_get_info()[0] // 2
+        ngroups = max(1, -(-sum(nbytes) // int(budget)))
         bounds = np.searchsorted(np.cumsum(nbytes), np.arange(1, ngroups) * sum(nbytes) / ngroups)
         out = [None] * len(thetas)
         for grp in np.split(np.arange(len(thetas)), bounds):

@@ -183,3 +183,69 @@ def tune_nd_line_solver(P, L, steps=8):
         choice = min(times, key=times.get)
         _nd_cache[key] = {"segments": int(choice), "ms": times}
         return _nd_cache[key]
+
+
+_c2_cache = {}
+
+
+def tune_2d_cluster(L, steps=16):
+    """CTAs of the cluster (0: the one-CTA Thomas path of
+    dgb_integrate_table) with which a lone 2-population integration on L
+    points runs fastest on this GPU: each candidate (2, 4, 8, 16 CTAs where
+    3 CTAs <= L <= 16 CTAs) integrates `steps` steps of a constant table,
+    timed with CUDA events, best of 3 after a warm-up.  A cluster size the
+    GPU cannot place is skipped.  Cached per (device, L); returns
+    {"ctas": c, "ms": {c: ms}}."""
+    import threading
+    import torch
+    from . import integration, numerics
+    global _nd_lock
+    if _nd_lock is None:
+        _nd_lock = threading.Lock()
+    key = (torch.cuda.get_device_name(torch.cuda.current_device()), int(L))
+    with _nd_lock:
+        if key in _c2_cache:
+            return _c2_cache[key]
+        lib = _lib.lib()
+        tab = np.zeros((steps, integration.row_stride(2)))
+        tab[:, 0] = 1e-4
+        tab[:, 1] = 1.0
+        tab[:, 2:4] = 1.0
+        tab[:, 6:8] = 0.5
+        tab[:, 8] = 1.0
+        tab[:, 9:] = 1.0
+        xx = numerics.default_grid(L)
+        d_xx, d_tab = _lib.to_device(torch, xx), _lib.to_device(torch, tab)
+        phi = torch.ones((L, L), dtype=torch.float64, device="cuda")
+        ws, nws = _lib.workspace(torch, lib.dgb_workspace_bytes(0, 2, L, 0))
+        sh = _lib.stream_handle(torch)
+
+        def run(c):
+            if c == 0:
+                return lib.dgb_integrate_table(_lib.dptr(phi), 2, L, _lib.dptr(d_xx),
+                                               _lib.dptr(d_tab), steps, 0, 0, 0, _lib.dptr(ws),
+                                               nws, sh)
+            return lib.dgb_integrate2d_cluster(_lib.dptr(phi), L, _lib.dptr(d_xx),
+                                               _lib.dptr(d_tab), steps, 0, 0, c, sh)
+        times = {}
+        for c in (0, 2, 4, 8, 16):
+            if c and not 3 * c <= L <= 16 * c:
+                continue
+            best = None
+            for rep in range(4):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                rc = run(c)
+                e1.record()
+                if rc != _lib.DGB_OK:
+                    break
+                torch.cuda.synchronize()
+                if rep:
+                    ms = e0.elapsed_time(e1)
+                    best = ms if best is None else min(best, ms)
+            if best is not None:
+                times[c] = best
+        choice = min(times, key=times.get)
+        _c2_cache[key] = {"ctas": int(choice), "ms": times}
+        return _c2_cache[key]

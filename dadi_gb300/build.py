@@ -13,7 +13,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libdadi_gb300.so")
 SOURCES = ["dgb_integrate2d.cu", "dgb_sweepnd.cu", "dgb_probe.cu", "dgb_adjoint2d.cu",
-           "dgb_fsepi.cu", "dgb_adjointnd.cu", "dgb_batchnd.cu"]
+           "dgb_fsepi.cu", "dgb_adjointnd.cu", "dgb_batchnd.cu", "dgb_cluster2d.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]

@@ -314,19 +314,26 @@ __global__ void __launch_bounds__(32 * PCR_LINES) k_sweep_batch_pcr(NDBatch B, l
 //   upward, j <= m-3: x_j = de_j - al_j x_0 - ga_j x_{m-1}
 //     (de_j -= ga_j de_{j+1}, al_j -= ga_j al_{j+1}, ga_j = -ga_j ga_{j+1});
 //   row 0 with x_1 substituted:  a_0 x_prev + (b_0 - c_0 al_1) x_0
-//                                - c_0 ga_1 x_{m-1} = d_0 - c_0 de_1;
+//                                - c_0 ga_1 x_{m-1} = d_0 - c_0 de_1,
+//     i.e. x_0 = D' - A' z_{q-1} - C' z_q with z_q = x_{m-1} of segment q;
 //   row m-1 as it stands:        al x_0 + x_{m-1} + ga x_next = de.
-// Those two rows of every segment form a tridiagonal system of 2 SEG
-// unknowns (the segments' end points), solved by one thread per line; then
-// x_j = de_j - al_j x_0 - ga_j x_{m-1} inside.  About 17 FP64 instructions
-// per row against 10 for Thomas.  Default delta_j only; segments of at least
-// three rows.
+// Putting x_0 of segments q and q+1 into row m-1 of segment q leaves a
+// tridiagonal system in the segments' last points z_0 .. z_{SEG-1},
+//     -al A'_q z_{q-1} + (1 - al C'_q - ga A'_{q+1}) z_q - ga C'_{q+1} z_{q+1}
+//         = de - al D'_q - ga D'_{q+1},
+// each row formed by its segment's thread, the SEG rows solved by one
+// thread per line; then x_0 and x_j = de_j - al_j x_0 - ga_j x_{m-1}
+// inside.  About 17 FP64 instructions per row against 10 for Thomas.
+// Default delta_j only; segments of at least three rows.
 constexpr int PART_LINES = 32;
+// Per (segment, line): A' C' D', then al ga de (replaced by the row of the
+// system in the last points, read only by the segment's own thread), then z.
+constexpr int PART_SLOTS = 8;
 
 __host__ __device__ inline size_t part_smem_doubles(int L, int seg)
 {
     return (size_t)6 * L + (size_t)L * (PART_LINES + 1) + (size_t)2 * L * PART_LINES +
-           (size_t)8 * seg * PART_LINES;
+           (size_t)PART_SLOTS * seg * PART_LINES;
 }
 
 template <int SEG>
@@ -352,7 +359,7 @@ __global__ void __launch_bounds__(32 * SEG) k_sweep_batch_part(NDBatch B, long s
     double *tile = gx + L;                    // d, then de, then x
     double *al = tile + (size_t)L * tp;       // al_j
     double *ga = al + (size_t)L * nt;         // ga_j
-    double *red = ga + (size_t)L * nt;        // 8 doubles per (segment, line)
+    double *red = ga + (size_t)L * nt;        // PART_SLOTS per (segment, line)
     const double *rec = B.coef + nd_grid_doubles(L) + it * B.item_coef +
                         ((size_t)(step - B.step0) * P + A.axis) * nd_rec_doubles(L, false);
     double *hp = reinterpret_cast<double *>(&H);
@@ -385,7 +392,7 @@ __global__ void __launch_bounds__(32 * SEG) k_sweep_batch_part(NDBatch B, long s
     AxisVecs v;
     nd_vecs_at(vv, L, false, v);
     const AxisScalars &s = H.s;
-    double *r8 = red + (size_t)q * 8 * nt + t; // this segment's reduced rows, stride nt
+    double *r8 = red + (size_t)q * PART_SLOTS * nt + t; // this segment's slots, stride nt
     if (t < n) {
         int coord[DGB_MAX_DIM];
         nd_line_base(A, l0 + t, coord);
@@ -443,9 +450,9 @@ __global__ void __launch_bounds__(32 * SEG) k_sweep_batch_part(NDBatch B, long s
             tile[p * tp + t] = dep;
         }
         // the segment's last row, as it stands
-        r8[4 * nt] = alp;
-        r8[5 * nt] = gap;
-        r8[6 * nt] = dep;
+        r8[3 * nt] = alp;
+        r8[4 * nt] = gap;
+        r8[5 * nt] = dep;
         // upward, from row m-3: ga_j now couples to x_{m-1}
         p = s0 + m - 2;
         double deu = tile[p * tp + t], alu = al[p * nt + t], gau = ga[p * nt + t];
@@ -458,53 +465,58 @@ __global__ void __launch_bounds__(32 * SEG) k_sweep_batch_part(NDBatch B, long s
             al[p * nt + t] = alu;
             ga[p * nt + t] = gau;
         }
-        // row 0 with x_1 substituted
+        // row 0 with x_1 substituted, solved for x_0
         const double c0 = crow(s0);
-        r8[0] = arow(s0);
-        r8[1 * nt] = fma(-c0, alu, brow(s0));
-        r8[2 * nt] = -c0 * gau;
-        r8[3 * nt] = fma(-c0, deu, tile[s0 * tp + t]);
-    }
-    __syncthreads();
-    if (q == 0 && t < n) {
-        // the 2 SEG end points: Thomas on rows (row 0, row m-1) of each
-        // segment in order; unknowns y_{2k} = x_first(k), y_{2k+1} = x_last(k)
-        double gm[2 * SEG], y[2 * SEG];
-        double g = 0, u = 0;
-#pragma unroll
-        for (int r = 0; r < 2 * SEG; r++) {
-            const double *rr = red + (size_t)(r >> 1) * 8 * nt + t;
-            double ra, rb, rc, rd;
-            if ((r & 1) == 0) {
-                ra = rr[0];
-                rb = rr[1 * nt];
-                rc = rr[2 * nt];
-                rd = rr[3 * nt];
-            } else {
-                ra = rr[4 * nt];
-                rb = 1.0;
-                rc = rr[5 * nt];
-                rd = rr[6 * nt];
-            }
-            const double bet = (r == 0) ? rb : fma(-ra, g, rb);
-            const double iv = rcp_full(bet);
-            u = ((r == 0) ? rd : fma(-ra, u, rd)) * iv;
-            g = rc * iv;
-            gm[r] = g;
-            y[r] = u;
-        }
-#pragma unroll
-        for (int r = 2 * SEG - 2; r >= 0; r--)
-            y[r] = fma(-gm[r], y[r + 1], y[r]);
-#pragma unroll
-        for (int k = 0; k < SEG; k++) {
-            red[(size_t)k * 8 * nt + 3 * nt + t] = y[2 * k];
-            red[(size_t)k * 8 * nt + 6 * nt + t] = y[2 * k + 1];
-        }
+        const double iB = rcp_full(fma(-c0, alu, brow(s0)));
+        r8[0] = arow(s0) * iB;
+        r8[1 * nt] = (-c0 * gau) * iB;
+        r8[2 * nt] = fma(-c0, deu, tile[s0 * tp + t]) * iB;
     }
     __syncthreads();
     if (t < n) {
-        const double xf = r8[3 * nt], xl = r8[6 * nt];
+        // this segment's row of the system in the last points
+        const double Ap = r8[0], Cp = r8[nt], Dp = r8[2 * nt];
+        const double alq = r8[3 * nt], gaq = r8[4 * nt], deq = r8[5 * nt];
+        double An = 0, Cn = 0, Dn = 0;
+        if (q + 1 < SEG) {
+            const double *rn = r8 + PART_SLOTS * nt;
+            An = rn[0];
+            Cn = rn[nt];
+            Dn = rn[2 * nt];
+        }
+        r8[3 * nt] = -alq * Ap;
+        r8[4 * nt] = fma(-gaq, An, fma(-alq, Cp, 1.0));
+        r8[5 * nt] = -gaq * Cn;
+        r8[6 * nt] = fma(-gaq, Dn, fma(-alq, Dp, deq));
+    }
+    __syncthreads();
+    if (q == 0 && t < n) {
+        // Thomas on the SEG rows: z_k = the last point of segment k
+        double gm[SEG], z[SEG];
+        double g = 0, u = 0;
+#pragma unroll
+        for (int k = 0; k < SEG; k++) {
+            const double *rr = red + (size_t)k * PART_SLOTS * nt + t;
+            const double ra = rr[3 * nt], rb = rr[4 * nt], rc = rr[5 * nt], rd = rr[6 * nt];
+            const double bet = (k == 0) ? rb : fma(-ra, g, rb);
+            const double iv = rcp_full(bet);
+            u = ((k == 0) ? rd : fma(-ra, u, rd)) * iv;
+            g = rc * iv;
+            gm[k] = g;
+            z[k] = u;
+        }
+#pragma unroll
+        for (int k = SEG - 2; k >= 0; k--)
+            z[k] = fma(-gm[k], z[k + 1], z[k]);
+#pragma unroll
+        for (int k = 0; k < SEG; k++)
+            red[(size_t)k * PART_SLOTS * nt + 7 * nt + t] = z[k];
+    }
+    __syncthreads();
+    if (t < n) {
+        const double xl = r8[7 * nt];
+        const double zp = q ? r8[7 * nt - PART_SLOTS * nt] : 0.0;
+        const double xf = fma(-r8[nt], xl, fma(-r8[0], zp, r8[2 * nt]));
         tile[s0 * tp + t] = xf;
         tile[(s0 + m - 1) * tp + t] = xl;
         for (int p = s0 + 1; p < s0 + m - 1; p++)

@@ -1,0 +1,447 @@
+// One 2-D integration spread over a thread-block cluster.
+//
+// GB300's FP64 pipe retires about 1.7 FMA lanes per clock per SM, so a lone
+// 2-D integration on one CTA (k_integrate2d) is bound by its one SM's pipe
+// (L = 120: about 88,000 clocks per sweep).  Here the S CTAs of a cluster
+// (S SMs) share the grid: CTA r holds rows R0 .. R0+m-1 of phi (all L
+// columns) in shared memory for the whole time loop, and every sweep is a
+// partitioned Thomas solve (the modified-Thomas form of the partition method,
+// as in k_sweep_batch_part):
+//
+// * x sweep (lines = columns, points = rows): each column is cut into the S
+//   CTAs' row blocks.  Each CTA's thread j runs the downward and upward
+//   passes over its rows and exports the two end rows of its segment
+//   (x_first = D' - A' z_prev - C' z, and al x_first + z + ga x_next = de);
+//   after a cluster barrier, the thread of column j in CTA j mod S reads the
+//   S segments' rows through distributed shared memory, solves the
+//   tridiagonal system in the segments' last points z_0 .. z_{S-1} and
+//   writes z_q, z_{q-1} into CTA q; after a second barrier each CTA
+//   finishes its interior points.
+// * y sweep (lines = rows, points = columns): the rows are local; each is
+//   cut into 8 segments on 8 threads of the CTA (so 16 rows fill its 128
+//   lanes) and solved the same way with CTA barriers.
+//
+// The rows, corner terms, injection and parameter rows are those of
+// k_integrate2d (Integration.two_pops, dadi/Integration.py:340-386, with
+// implicit_2Dx / implicit_2Dy, dadi/integration2D.c:19-160); the solves
+// agree with Thomas to rounding.  Default delta_j only; L <= 16 S and
+// segments of at least 3 rows (L >= 24, L >= 3 S).
+#include <algorithm>
+
+#include <cooperative_groups.h>
+
+#include "dgb_common.cuh"
+#include "dgb_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace dgb {
+
+constexpr int C2_THREADS = 128;
+constexpr int C2_ROWS = 16; // rows per CTA at most
+constexpr int C2_YSEG = 8;  // segments per row in the y sweep
+constexpr int C2_XROW = 6;  // exported values per column: A' C' D' al ga de
+constexpr int C2_YSLOT = 8; // per (row, segment): A' C' D', al ga de / z row, z
+
+struct C2Args {
+    double *phi;
+    const double *xx;
+    const double *table;
+    int L, nsteps, frozen, nomut;
+};
+
+struct C2Shared {
+    AxisScalars ax[2];
+    double inj;
+};
+
+__host__ __device__ inline int c2_pitch(int L) { return (L % 2) ? L : L + 1; }
+
+// Shared memory (doubles) of one CTA for grids of up to L points.
+__host__ __device__ inline size_t c2_smem_doubles(int L)
+{
+    return (size_t)C2_ROWS * c2_pitch(L) + 2 * (size_t)C2_ROWS * L + 16 * (size_t)L +
+           (size_t)C2_XROW * L + 2 * (size_t)L + (size_t)C2_YSLOT * C2_YSEG * C2_ROWS;
+}
+
+// Rows of CTA r of S over L points: [*r0, *r0 + *m).
+__device__ __forceinline__ void c2_rows(int L, int S, int r, int *r0, int *m)
+{
+    const int base = L / S, extra = L % S;
+    *r0 = r * base + min(r, extra);
+    *m = base + (r < extra ? 1 : 0);
+}
+
+__global__ void __launch_bounds__(C2_THREADS) k_integrate2d_cluster(C2Args A)
+{
+    extern __shared__ __align__(16) double smem[];
+    __shared__ C2Shared Sh;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int S = (int)cluster.num_blocks();
+    const int rank = (int)cluster.block_rank();
+    const int tid = threadIdx.x, L = A.L, pitch = c2_pitch(L);
+    int R0, m;
+    c2_rows(L, S, rank, &R0, &m);
+    double *blk = smem;                                  // m x pitch: rows R0 ..
+    double *al = blk + (size_t)C2_ROWS * pitch;          // x: [p][j]; y: [j][p]
+    double *ga = al + (size_t)C2_ROWS * L;
+    GridVecs g;
+    double *q0 = ga + (size_t)C2_ROWS * L;
+    g.x = q0;
+    g.xv = q0 + L;
+    g.dfac = q0 + 2 * L;
+    g.xInt = q0 + 3 * L;
+    g.ih = q0 + 4 * L;
+    g.dx = q0 + 5 * L;
+    AxisVecs v[2];
+    v[0].A1 = q0 + 6 * L;
+    v[0].A0 = q0 + 7 * L;
+    v[0].C1 = q0 + 8 * L;
+    v[0].C0 = q0 + 9 * L;
+    v[0].B0 = q0 + 10 * L;
+    v[1].A1 = q0 + 11 * L;
+    v[1].A0 = q0 + 12 * L;
+    v[1].C1 = q0 + 13 * L;
+    v[1].C0 = q0 + 14 * L;
+    v[1].B0 = q0 + 15 * L;
+    for (int a = 0; a < 2; a++)
+        v[a].G = v[a].Pv = v[a].Qv = v[a].VI = v[a].DF = nullptr;
+    double *xr = q0 + 16 * L;             // exported rows of the x segments, [k][j]
+    double *zin = xr + C2_XROW * L;       // z of this segment and of the one above, [2][j]
+    double *yr = zin + 2 * L;             // y sweep slots, [(q * C2_YSLOT + k) * C2_ROWS + p]
+
+    // grid constants and this CTA's rows of the initial density
+    for (int i = tid; i < L; i += C2_THREADS) {
+        const double x = A.xx[i];
+        g.x[i] = x;
+        g.xv[i] = x * (1. - x);
+        if (i < L - 1) {
+            const double d = A.xx[i + 1] - x;
+            g.dx[i] = d;
+            g.ih[i] = 1.0 / (2 * d);
+            g.xInt[i] = 0.5 * (A.xx[i + 1] + x);
+        }
+    }
+    for (int idx = tid; idx < m * L; idx += C2_THREADS) {
+        const int p = idx / L, c = idx - p * L;
+        blk[p * pitch + c] = A.phi[(size_t)(R0 + p) * L + c];
+    }
+    __syncthreads();
+    for (int i = tid; i < L; i += C2_THREADS)
+        g.dfac[i] = (i == 0)       ? 2. / g.dx[0]
+                    : (i == L - 1) ? 2. / g.dx[L - 2]
+                                   : 2. / (g.dx[i] + g.dx[i - 1]);
+    __syncthreads();
+    const int j0 = (g.x[0] == 0.0) ? 0 : -1;
+    const int j1 = (g.x[L - 1] == 1.0) ? L - 1 : -1;
+
+    for (int step = 0; step < A.nsteps; step++) {
+        const double *row = A.table + (size_t)step * 11;
+        if (tid < 2) {
+            AxisScalars &s = Sh.ax[tid];
+            const int a = tid;
+            const double dt = row[0];
+            s.dt = dt;
+            s.nu = row[row_nu(2, a)];
+            s.inv_nu = 1.0 / s.nu;
+            s.gamma = row[row_gamma(2, a)];
+            s.h = row[row_h(2, a)];
+            const double mg = row[row_mig(2, a, 1 - a)];
+            s.msum = mg;
+            s.mig[a] = 0;
+            s.mig[1 - a] = mg;
+            s.B1s = 0.5 * (dt * g.dfac[0]);
+            s.B1e = -0.5 * (dt * g.dfac[L - 1]);
+            corner_bc(2, a, s.mig, s.nu, s.gamma, s.h, g.x[0], g.x[L - 1], g.dx[0], g.dx[L - 2],
+                      dt, s.bcs, s.bce);
+        } else if (tid == 2) {
+            Sh.inj = inject_value(2, row[0], row[1], g.x[0], g.x[1], g.x[2]);
+        }
+        __syncthreads();
+        for (int t = tid; t < 2 * L; t += C2_THREADS) {
+            const int a = t >= L, i = t - a * L;
+            build_axis_entry(i, L, g, Sh.ax[a], 1.0, false, v[a]);
+        }
+        if (tid == 0 && rank == 0) {
+            // rows 0 and 1 are this CTA's (m >= 3)
+            if (!(A.frozen & 1) && !(A.nomut & 1))
+                blk[1 * pitch + 0] += Sh.inj;
+            if (!(A.frozen & 2) && !(A.nomut & 2))
+                blk[0 * pitch + 1] += Sh.inj;
+        }
+        __syncthreads();
+
+        // ---------------- x sweep: column j, points i = R0 + p
+        if (!(A.frozen & 1)) {
+            const AxisScalars &s = Sh.ax[0];
+            const AxisVecs &vv = v[0];
+            const int j = tid;
+            if (j < L) {
+                const double W = s.mig[1] * g.x[j];
+                auto arow = [&](int i) { return (i > 0) ? fma(W, vv.A1[i], vv.A0[i]) : 0.0; };
+                auto crow = [&](int i) { return (i < L - 1) ? fma(W, vv.C1[i], vv.C0[i]) : 0.0; };
+                auto brow = [&](int i) {
+                    if (i == 0)
+                        return fma(W, s.B1s, vv.B0[0]) + (j == j0 ? s.bcs : 0.0);
+                    if (i == L - 1)
+                        return fma(W, s.B1e, vv.B0[L - 1]) + (j == j1 ? s.bce : 0.0);
+                    return vv.B0[i];
+                };
+                int p = 1;
+                double aa = arow(R0 + p);
+                double inv = rcp_full(brow(R0 + p));
+                double alp = aa * inv, gap = crow(R0 + p) * inv, dep = blk[p * pitch + j] * inv;
+                al[p * L + j] = alp;
+                ga[p * L + j] = gap;
+                blk[p * pitch + j] = dep;
+                for (p = 2; p < m; p++) {
+                    aa = arow(R0 + p);
+                    inv = rcp_full(fma(-aa, gap, brow(R0 + p)));
+                    alp = -aa * alp * inv;
+                    gap = crow(R0 + p) * inv;
+                    dep = fma(-aa, dep, blk[p * pitch + j]) * inv;
+                    al[p * L + j] = alp;
+                    ga[p * L + j] = gap;
+                    blk[p * pitch + j] = dep;
+                }
+                xr[3 * L + j] = alp;
+                xr[4 * L + j] = gap;
+                xr[5 * L + j] = dep;
+                p = m - 2;
+                double deu = blk[p * pitch + j], alu = al[p * L + j], gau = ga[p * L + j];
+                for (p = m - 3; p >= 1; p--) {
+                    const double gg = ga[p * L + j];
+                    deu = fma(-gg, deu, blk[p * pitch + j]);
+                    alu = fma(-gg, alu, al[p * L + j]);
+                    gau = -gg * gau;
+                    blk[p * pitch + j] = deu;
+                    al[p * L + j] = alu;
+                    ga[p * L + j] = gau;
+                }
+                const double c0 = crow(R0);
+                const double iB = rcp_full(fma(-c0, alu, brow(R0)));
+                xr[0 * L + j] = arow(R0) * iB;
+                xr[1 * L + j] = (-c0 * gau) * iB;
+                xr[2 * L + j] = fma(-c0, deu, blk[j]) * iB;
+            }
+            cluster.sync();
+            if (j < L && j % S == rank) {
+                // column j's system in the segments' last points
+                double gm[C2_ROWS], z[C2_ROWS];
+                double gq = 0, u = 0;
+                for (int q = 0; q < S; q++) {
+                    const double *rq = cluster.map_shared_rank(xr, q);
+                    const double Ap = rq[j], Cp = rq[L + j], Dp = rq[2 * L + j];
+                    const double alq = rq[3 * L + j], gaq = rq[4 * L + j], deq = rq[5 * L + j];
+                    double An = 0, Cn = 0, Dn = 0;
+                    if (q + 1 < S) {
+                        const double *rn = cluster.map_shared_rank(xr, q + 1);
+                        An = rn[j];
+                        Cn = rn[L + j];
+                        Dn = rn[2 * L + j];
+                    }
+                    const double ra = -alq * Ap;
+                    const double rb = fma(-gaq, An, fma(-alq, Cp, 1.0));
+                    const double rc = -gaq * Cn;
+                    const double rd = fma(-gaq, Dn, fma(-alq, Dp, deq));
+                    const double bet = (q == 0) ? rb : fma(-ra, gq, rb);
+                    const double iv = rcp_full(bet);
+                    u = ((q == 0) ? rd : fma(-ra, u, rd)) * iv;
+                    gq = rc * iv;
+                    gm[q] = gq;
+                    z[q] = u;
+                }
+                for (int q = S - 2; q >= 0; q--)
+                    z[q] = fma(-gm[q], z[q + 1], z[q]);
+                for (int q = 0; q < S; q++) {
+                    double *zq = cluster.map_shared_rank(zin, q);
+                    zq[j] = z[q];
+                    zq[L + j] = q ? z[q - 1] : 0.0;
+                }
+            }
+            cluster.sync();
+            if (j < L) {
+                const double xl = zin[j], zp = zin[L + j];
+                const double xf = fma(-xr[L + j], xl, fma(-xr[j], zp, xr[2 * L + j]));
+                blk[j] = xf;
+                blk[(m - 1) * pitch + j] = xl;
+                for (int p = 1; p < m - 1; p++)
+                    blk[p * pitch + j] =
+                        fma(-ga[p * L + j], xl, fma(-al[p * L + j], xf, blk[p * pitch + j]));
+            }
+            __syncthreads();
+        }
+
+        // ---------------- y sweep: local row p (global R0 + p), 8 segments
+        if (!(A.frozen & 2)) {
+            const AxisScalars &s = Sh.ax[1];
+            const AxisVecs &vv = v[1];
+            const int p = tid % C2_ROWS, q = tid / C2_ROWS;
+            const int mlen = L / C2_YSEG, extra = L % C2_YSEG;
+            const int s0 = q * mlen + min(q, extra);
+            const int ml = mlen + (q < extra ? 1 : 0);
+            double *r8 = yr + (size_t)q * C2_YSLOT * C2_ROWS + p;
+            double *ph = blk + (size_t)p * pitch;
+            const bool live = p < m;
+            if (live) {
+                const int i = R0 + p;
+                const double W = s.mig[0] * g.x[i];
+                auto arow = [&](int c) { return (c > 0) ? fma(W, vv.A1[c], vv.A0[c]) : 0.0; };
+                auto crow = [&](int c) { return (c < L - 1) ? fma(W, vv.C1[c], vv.C0[c]) : 0.0; };
+                auto brow = [&](int c) {
+                    if (c == 0)
+                        return fma(W, s.B1s, vv.B0[0]) + (i == j0 ? s.bcs : 0.0);
+                    if (c == L - 1)
+                        return fma(W, s.B1e, vv.B0[L - 1]) + (i == j1 ? s.bce : 0.0);
+                    return vv.B0[c];
+                };
+                int c = s0 + 1;
+                double aa = arow(c);
+                double inv = rcp_full(brow(c));
+                double alp = aa * inv, gap = crow(c) * inv, dep = ph[c] * inv;
+                al[c * C2_ROWS + p] = alp;
+                ga[c * C2_ROWS + p] = gap;
+                ph[c] = dep;
+                for (c = s0 + 2; c < s0 + ml; c++) {
+                    aa = arow(c);
+                    inv = rcp_full(fma(-aa, gap, brow(c)));
+                    alp = -aa * alp * inv;
+                    gap = crow(c) * inv;
+                    dep = fma(-aa, dep, ph[c]) * inv;
+                    al[c * C2_ROWS + p] = alp;
+                    ga[c * C2_ROWS + p] = gap;
+                    ph[c] = dep;
+                }
+                r8[3 * C2_ROWS] = alp;
+                r8[4 * C2_ROWS] = gap;
+                r8[5 * C2_ROWS] = dep;
+                c = s0 + ml - 2;
+                double deu = ph[c], alu = al[c * C2_ROWS + p], gau = ga[c * C2_ROWS + p];
+                for (c = s0 + ml - 3; c >= s0 + 1; c--) {
+                    const double gg = ga[c * C2_ROWS + p];
+                    deu = fma(-gg, deu, ph[c]);
+                    alu = fma(-gg, alu, al[c * C2_ROWS + p]);
+                    gau = -gg * gau;
+                    ph[c] = deu;
+                    al[c * C2_ROWS + p] = alu;
+                    ga[c * C2_ROWS + p] = gau;
+                }
+                const double c0 = crow(s0);
+                const double iB = rcp_full(fma(-c0, alu, brow(s0)));
+                r8[0] = arow(s0) * iB;
+                r8[1 * C2_ROWS] = (-c0 * gau) * iB;
+                r8[2 * C2_ROWS] = fma(-c0, deu, ph[s0]) * iB;
+            }
+            __syncthreads();
+            if (live) {
+                const double Ap = r8[0], Cp = r8[C2_ROWS], Dp = r8[2 * C2_ROWS];
+                const double alq = r8[3 * C2_ROWS], gaq = r8[4 * C2_ROWS], deq = r8[5 * C2_ROWS];
+                double An = 0, Cn = 0, Dn = 0;
+                if (q + 1 < C2_YSEG) {
+                    const double *rn = r8 + C2_YSLOT * C2_ROWS;
+                    An = rn[0];
+                    Cn = rn[C2_ROWS];
+                    Dn = rn[2 * C2_ROWS];
+                }
+                r8[3 * C2_ROWS] = -alq * Ap;
+                r8[4 * C2_ROWS] = fma(-gaq, An, fma(-alq, Cp, 1.0));
+                r8[5 * C2_ROWS] = -gaq * Cn;
+                r8[6 * C2_ROWS] = fma(-gaq, Dn, fma(-alq, Dp, deq));
+            }
+            __syncthreads();
+            if (live && q == 0) {
+                double gm[C2_YSEG], z[C2_YSEG];
+                double gq = 0, u = 0;
+#pragma unroll
+                for (int k = 0; k < C2_YSEG; k++) {
+                    const double *rr = yr + (size_t)k * C2_YSLOT * C2_ROWS + p;
+                    const double ra = rr[3 * C2_ROWS], rb = rr[4 * C2_ROWS];
+                    const double rc = rr[5 * C2_ROWS], rd = rr[6 * C2_ROWS];
+                    const double bet = (k == 0) ? rb : fma(-ra, gq, rb);
+                    const double iv = rcp_full(bet);
+                    u = ((k == 0) ? rd : fma(-ra, u, rd)) * iv;
+                    gq = rc * iv;
+                    gm[k] = gq;
+                    z[k] = u;
+                }
+#pragma unroll
+                for (int k = C2_YSEG - 2; k >= 0; k--)
+                    z[k] = fma(-gm[k], z[k + 1], z[k]);
+#pragma unroll
+                for (int k = 0; k < C2_YSEG; k++)
+                    yr[((size_t)k * C2_YSLOT + 7) * C2_ROWS + p] = z[k];
+            }
+            __syncthreads();
+            if (live) {
+                const double xl = r8[7 * C2_ROWS];
+                const double zp = q ? r8[7 * C2_ROWS - C2_YSLOT * C2_ROWS] : 0.0;
+                const double xf = fma(-r8[C2_ROWS], xl, fma(-r8[0], zp, r8[2 * C2_ROWS]));
+                ph[s0] = xf;
+                ph[s0 + ml - 1] = xl;
+                for (int c = s0 + 1; c < s0 + ml - 1; c++)
+                    ph[c] = fma(-ga[c * C2_ROWS + p], xl, fma(-al[c * C2_ROWS + p], xf, ph[c]));
+            }
+            __syncthreads();
+        }
+    }
+    for (int idx = tid; idx < m * L; idx += C2_THREADS) {
+        const int p = idx / L, c = idx - p * L;
+        A.phi[(size_t)(R0 + p) * L + c] = blk[p * pitch + c];
+    }
+    // no CTA may leave while another may still read its shared memory
+    cluster.sync();
+}
+
+} // namespace dgb
+
+using namespace dgb;
+
+extern "C" int dgb_integrate2d_cluster(double *phi, int L, const double *xx, const double *table,
+                                       int nsteps, int frozen_mask, int nomut_mask, int cluster,
+                                       void *stream)
+{
+    if (!phi || !xx || !table || nsteps < 0 || L < 3)
+        return DGB_ERR_ARG;
+    if (cluster != 2 && cluster != 4 && cluster != 8 && cluster != 16)
+        return DGB_ERR_ARG;
+    if (L > C2_ROWS * cluster || L > C2_THREADS || L < 3 * cluster || L < 3 * C2_YSEG)
+        return DGB_ERR_UNSUPPORTED;
+    if (nsteps == 0)
+        return DGB_OK;
+    // at least 116 KB per CTA, so that no two CTAs of the cluster share an
+    // SM (and its FP64 pipe)
+    const size_t smem = std::max(c2_smem_doubles(L) * sizeof(double), (size_t)116 << 10);
+    if (raise_smem_limit(k_integrate2d_cluster))
+        return DGB_ERR_CUDA;
+    if (cluster > 8 && cudaFuncSetAttribute(k_integrate2d_cluster,
+                                            cudaFuncAttributeNonPortableClusterSizeAllowed,
+                                            1) != cudaSuccess) {
+        cudaGetLastError();
+        return DGB_ERR_UNSUPPORTED;
+    }
+    C2Args A;
+    A.phi = phi;
+    A.xx = xx;
+    A.table = table;
+    A.L = L;
+    A.nsteps = nsteps;
+    A.frozen = frozen_mask;
+    A.nomut = nomut_mask;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)cluster, 1, 1);
+    cfg.blockDim = dim3(C2_THREADS, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = (cudaStream_t)stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cudaLaunchKernelEx(&cfg, k_integrate2d_cluster, A) != cudaSuccess) {
+        cudaGetLastError();
+        return DGB_ERR_CUDA;
+    }
+    return DGB_OK;
+}

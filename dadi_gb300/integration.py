@@ -41,6 +41,14 @@ old_timescale_factor = 0.1
 nd_line_solver = "auto"
 nd_segments = 0
 
+#: Solver of the lone 2-population integrations: "thomas" (one CTA,
+#: dgb_integrate_table), "cluster" (dgb_integrate2d_cluster over
+#: cluster_ctas CTAs, or by the autotuner when 0) or "auto" (the autotuner
+#: times both once per grid size).  The results agree to rounding; "thomas"
+#: keeps them bitwise those of the batched engine.
+line_solver_2d = "auto"
+cluster_ctas = 0
+
 
 def current_settings():
     """(timescale_factor, old_timescale_factor, use_old_timestep, use_delj_trick)."""
@@ -193,6 +201,20 @@ def partition_segments(P, L, delj=False):
     return seg if seg and L >= 3 * seg else 0
 
 
+def cluster_size_2d(L, delj=False):
+    """CTAs of the cluster for a lone 2-population grid of L points under
+    line_solver_2d, or 0 for the one-CTA Thomas path."""
+    mode = line_solver_2d
+    if mode not in ("auto", "thomas", "cluster"):
+        raise ValueError("line_solver_2d must be 'auto', 'thomas' or 'cluster'")
+    if delj or mode == "thomas" or not 24 <= L <= 128:
+        return 0
+    if mode == "cluster" and cluster_ctas:
+        return int(cluster_ctas)
+    from . import autotune
+    return autotune.tune_2d_cluster(L)["ctas"]
+
+
 _engines = {}
 
 
@@ -221,7 +243,16 @@ def run_table(phi, xx, table, frozen_mask=0, nomut_mask=0):
     if len(table) == 0:
         return _copy_in(phi)
     d_phi, dev = _device_phi(torch, phi)
-    seg = partition_segments(P, L, current_settings()[3])
+    delj = current_settings()[3]
+    ctas = cluster_size_2d(L, delj) if P == 2 else 0
+    if ctas:
+        d_xx, d_tab = _lib.to_device(torch, xx), _lib.to_device(torch, table)
+        _lib.check(_lib.lib().dgb_integrate2d_cluster(
+            _lib.dptr(d_phi), L, _lib.dptr(d_xx), _lib.dptr(d_tab), len(table),
+            int(frozen_mask), int(nomut_mask), ctas, _lib.stream_handle(torch)),
+            "dgb_integrate2d_cluster")
+        return d_phi if dev else _lib.to_host(torch, d_phi)
+    seg = partition_segments(P, L, delj)
     if seg:
         out = _partition_engine(P, L, xx, seg).integrate(
             d_phi, [np.asarray(table, dtype=np.float64)],

@@ -142,6 +142,19 @@ int dgb_integrate_table(double *phi, int ndim, int L, const double *xx,
                         int nomut_mask, int use_delj_trick,
                         void *ws, size_t ws_bytes, void *stream);
 
+/* dgb_integrate_table for one 2-population integration spread over a
+ * thread-block cluster of `cluster` CTAs (2, 4, 8 or 16), one SM each: each
+ * CTA holds a block of rows of phi in shared memory, the x sweep is a
+ * partitioned Thomas solve across the cluster (segment end rows exchanged
+ * through distributed shared memory), the y sweep one within each CTA.  For
+ * a lone integration, whose one CTA would be bound by one SM's FP64 pipe.
+ * Agrees with dgb_integrate_table to rounding; default delta_j only (no
+ * use_delj_trick argument); 24 <= L <= 128, 3 cluster <= L <= 16 cluster
+ * (else DGB_ERR_UNSUPPORTED).  No workspace. */
+int dgb_integrate2d_cluster(double *phi, int L, const double *xx, const double *table,
+                            int nsteps, int frozen_mask, int nomut_mask, int cluster,
+                            void *stream);
+
 /* A whole constant-coefficient time loop: abc holds 3*ndim arrays of L^ndim
  * doubles (a_0, b_0, c_0, a_1, ...; b without 1/dt, as built by
  * dadi/Integration.py:1057-1095, 1145-1222); dts (device) the nsteps step
