@@ -880,6 +880,17 @@ def run_profile_kernel(a):
             from dadi_gb300 import numerics, spectrum
             phis = torch.rand(32, 90, 90, 90, dtype=torch.float64, device="cuda")
             spectrum.from_phi_nd_batch(torch, phis, (20, 20, 20), numerics.default_grid(90))
+        elif a.profile == "cluster2d":
+            # one IM integration (seed-0 draw 1, 2648 steps) at L = 120 through
+            # the drop-in on a cluster of 8 CTAs, then of 16
+            from dadi_gb300 import integration, models
+            saved = integration.line_solver_2d, integration.cluster_ctas
+            try:
+                for c in (8, 16):
+                    integration.line_solver_2d, integration.cluster_ctas = "cluster", c
+                    models.IM(im_draws(2, 0)[1], (40, 40), 120)
+            finally:
+                integration.line_solver_2d, integration.cluster_ctas = saved
         elif a.profile == "adjointnd_batch":
             # 8 three-population gradients at pts 32 as one batch (every
             # step's density recorded: about 1.5 GB), every sweep launch over
@@ -933,7 +944,8 @@ def main():
                          "steps, twice) for profiler captures, then exit")
     ap.add_argument("--profile", default=None,
                     choices=["epilogue", "sweep3d", "adjoint2d", "adjointnd", "batchnd",
-                             "fromphind", "thomas3d", "part3d", "adjointnd_batch"],
+                             "fromphind", "thomas3d", "part3d", "adjointnd_batch",
+                             "cluster2d"],
                     help="run a small case of another kernel for profiler captures, then exit")
     ap.add_argument("--line-solvers", action="store_true",
                     help="time the batched N-D engine's line solvers on the growth model's "

@@ -48,6 +48,11 @@ struct C2Args {
     const double *xx;
     const double *table;
     int L, nsteps, frozen, nomut;
+    // a list of work items, one cluster each (null: the one integration above)
+    const dgb_item2d *items;
+    const long *row_off; // first table row of each schedule
+    const int *row_cnt;  // rows of each schedule
+    int Lmin, Lmax;      // the grid sizes the launch was checked for
 };
 
 struct C2Shared {
@@ -79,7 +84,24 @@ __global__ void __launch_bounds__(C2_THREADS) k_integrate2d_cluster(C2Args A)
     cg::cluster_group cluster = cg::this_cluster();
     const int S = (int)cluster.num_blocks();
     const int rank = (int)cluster.block_rank();
-    const int tid = threadIdx.x, L = A.L, pitch = c2_pitch(L);
+    double *phi_g = A.phi;
+    const double *xx = A.xx, *table = A.table;
+    int L = A.L, nsteps = A.nsteps, frozen = A.frozen, nomut = A.nomut;
+    if (A.items) {
+        // this cluster's work item; every CTA of the cluster reads the same
+        // one, so a skipped item is skipped by the whole cluster
+        const dgb_item2d it = A.items[blockIdx.x / S];
+        if (it.L < A.Lmin || it.L > A.Lmax)
+            return;
+        L = it.L;
+        xx = A.xx + it.xx_off;
+        phi_g = A.phi + it.out_off;
+        table = A.table + A.row_off[it.sched] * 11;
+        nsteps = A.row_cnt[it.sched];
+        frozen = it.masks & 0xff;
+        nomut = it.masks >> 8 & 0xff;
+    }
+    const int tid = threadIdx.x, pitch = c2_pitch(L);
     int R0, m;
     c2_rows(L, S, rank, &R0, &m);
     double *blk = smem;                                  // m x pitch: rows R0 ..
@@ -112,19 +134,19 @@ __global__ void __launch_bounds__(C2_THREADS) k_integrate2d_cluster(C2Args A)
 
     // grid constants and this CTA's rows of the initial density
     for (int i = tid; i < L; i += C2_THREADS) {
-        const double x = A.xx[i];
+        const double x = xx[i];
         g.x[i] = x;
         g.xv[i] = x * (1. - x);
         if (i < L - 1) {
-            const double d = A.xx[i + 1] - x;
+            const double d = xx[i + 1] - x;
             g.dx[i] = d;
             g.ih[i] = 1.0 / (2 * d);
-            g.xInt[i] = 0.5 * (A.xx[i + 1] + x);
+            g.xInt[i] = 0.5 * (xx[i + 1] + x);
         }
     }
     for (int idx = tid; idx < m * L; idx += C2_THREADS) {
         const int p = idx / L, c = idx - p * L;
-        blk[p * pitch + c] = A.phi[(size_t)(R0 + p) * L + c];
+        blk[p * pitch + c] = phi_g[(size_t)(R0 + p) * L + c];
     }
     __syncthreads();
     for (int i = tid; i < L; i += C2_THREADS)
@@ -135,8 +157,8 @@ __global__ void __launch_bounds__(C2_THREADS) k_integrate2d_cluster(C2Args A)
     const int j0 = (g.x[0] == 0.0) ? 0 : -1;
     const int j1 = (g.x[L - 1] == 1.0) ? L - 1 : -1;
 
-    for (int step = 0; step < A.nsteps; step++) {
-        const double *row = A.table + (size_t)step * 11;
+    for (int step = 0; step < nsteps; step++) {
+        const double *row = table + (size_t)step * 11;
         if (tid < 2) {
             AxisScalars &s = Sh.ax[tid];
             const int a = tid;
@@ -164,15 +186,15 @@ __global__ void __launch_bounds__(C2_THREADS) k_integrate2d_cluster(C2Args A)
         }
         if (tid == 0 && rank == 0) {
             // rows 0 and 1 are this CTA's (m >= 3)
-            if (!(A.frozen & 1) && !(A.nomut & 1))
+            if (!(frozen & 1) && !(nomut & 1))
                 blk[1 * pitch + 0] += Sh.inj;
-            if (!(A.frozen & 2) && !(A.nomut & 2))
+            if (!(frozen & 2) && !(nomut & 2))
                 blk[0 * pitch + 1] += Sh.inj;
         }
         __syncthreads();
 
         // ---------------- x sweep: column j, points i = R0 + p
-        if (!(A.frozen & 1)) {
+        if (!(frozen & 1)) {
             const AxisScalars &s = Sh.ax[0];
             const AxisVecs &vv = v[0];
             const int j = tid;
@@ -273,7 +295,7 @@ __global__ void __launch_bounds__(C2_THREADS) k_integrate2d_cluster(C2Args A)
         }
 
         // ---------------- y sweep: local row p (global R0 + p), 8 segments
-        if (!(A.frozen & 2)) {
+        if (!(frozen & 2)) {
             const AxisScalars &s = Sh.ax[1];
             const AxisVecs &vv = v[1];
             const int p = tid % C2_ROWS, q = tid / C2_ROWS;
@@ -386,7 +408,7 @@ __global__ void __launch_bounds__(C2_THREADS) k_integrate2d_cluster(C2Args A)
     }
     for (int idx = tid; idx < m * L; idx += C2_THREADS) {
         const int p = idx / L, c = idx - p * L;
-        A.phi[(size_t)(R0 + p) * L + c] = blk[p * pitch + c];
+        phi_g[(size_t)(R0 + p) * L + c] = blk[p * pitch + c];
     }
     // no CTA may leave while another may still read its shared memory
     cluster.sync();
@@ -396,21 +418,18 @@ __global__ void __launch_bounds__(C2_THREADS) k_integrate2d_cluster(C2Args A)
 
 using namespace dgb;
 
-extern "C" int dgb_integrate2d_cluster(double *phi, int L, const double *xx, const double *table,
-                                       int nsteps, int frozen_mask, int nomut_mask, int cluster,
-                                       void *stream)
+namespace dgb {
+
+static bool c2_fits(int L, int cluster)
 {
-    if (!phi || !xx || !table || nsteps < 0 || L < 3)
-        return DGB_ERR_ARG;
-    if (cluster != 2 && cluster != 4 && cluster != 8 && cluster != 16)
-        return DGB_ERR_ARG;
-    if (L > C2_ROWS * cluster || L > C2_THREADS || L < 3 * cluster || L < 3 * C2_YSEG)
-        return DGB_ERR_UNSUPPORTED;
-    if (nsteps == 0)
-        return DGB_OK;
-    // at least 116 KB per CTA, so that no two CTAs of the cluster share an
-    // SM (and its FP64 pipe)
-    const size_t smem = std::max(c2_smem_doubles(L) * sizeof(double), (size_t)116 << 10);
+    return L >= 3 * C2_YSEG && L <= C2_THREADS && L >= 3 * cluster && L <= C2_ROWS * cluster;
+}
+
+static int c2_launch(const C2Args &A, int nclusters, int cluster, int Lmax, cudaStream_t st)
+{
+    // at least 116 KB per CTA, so that no two CTAs of a cluster share an SM
+    // (and its FP64 pipe)
+    const size_t smem = std::max(c2_smem_doubles(Lmax) * sizeof(double), (size_t)116 << 10);
     if (raise_smem_limit(k_integrate2d_cluster))
         return DGB_ERR_CUDA;
     if (cluster > 8 && cudaFuncSetAttribute(k_integrate2d_cluster,
@@ -419,19 +438,11 @@ extern "C" int dgb_integrate2d_cluster(double *phi, int L, const double *xx, con
         cudaGetLastError();
         return DGB_ERR_UNSUPPORTED;
     }
-    C2Args A;
-    A.phi = phi;
-    A.xx = xx;
-    A.table = table;
-    A.L = L;
-    A.nsteps = nsteps;
-    A.frozen = frozen_mask;
-    A.nomut = nomut_mask;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)cluster, 1, 1);
+    cfg.gridDim = dim3((unsigned)(cluster * nclusters), 1, 1);
     cfg.blockDim = dim3(C2_THREADS, 1, 1);
     cfg.dynamicSmemBytes = smem;
-    cfg.stream = (cudaStream_t)stream;
+    cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned)cluster;
@@ -444,4 +455,55 @@ extern "C" int dgb_integrate2d_cluster(double *phi, int L, const double *xx, con
         return DGB_ERR_CUDA;
     }
     return DGB_OK;
+}
+
+} // namespace dgb
+
+extern "C" int dgb_integrate2d_cluster(double *phi, int L, const double *xx, const double *table,
+                                       int nsteps, int frozen_mask, int nomut_mask, int cluster,
+                                       void *stream)
+{
+    if (!phi || !xx || !table || nsteps < 0 || L < 3)
+        return DGB_ERR_ARG;
+    if (cluster != 2 && cluster != 4 && cluster != 8 && cluster != 16)
+        return DGB_ERR_ARG;
+    if (!c2_fits(L, cluster))
+        return DGB_ERR_UNSUPPORTED;
+    if (nsteps == 0)
+        return DGB_OK;
+    C2Args A = {};
+    A.phi = phi;
+    A.xx = xx;
+    A.table = table;
+    A.L = L;
+    A.nsteps = nsteps;
+    A.frozen = frozen_mask;
+    A.nomut = nomut_mask;
+    return c2_launch(A, 1, cluster, L, (cudaStream_t)stream);
+}
+
+extern "C" int dgb_items2d_integrate_cluster(const dgb_item2d *items, int nitems, int Lmin,
+                                             int Lmax, const double *xx_all, double *phi_out,
+                                             const double *table, const long *row_off,
+                                             const int *row_cnt, int cluster, void *stream)
+{
+    if (!items || nitems < 0 || !xx_all || !phi_out || !table || !row_off || !row_cnt ||
+        Lmin > Lmax)
+        return DGB_ERR_ARG;
+    if (cluster != 2 && cluster != 4 && cluster != 8 && cluster != 16)
+        return DGB_ERR_ARG;
+    if (!c2_fits(Lmin, cluster) || !c2_fits(Lmax, cluster))
+        return DGB_ERR_UNSUPPORTED;
+    if (nitems == 0)
+        return DGB_OK;
+    C2Args A = {};
+    A.phi = phi_out;
+    A.xx = xx_all;
+    A.table = table;
+    A.items = items;
+    A.row_off = row_off;
+    A.row_cnt = row_cnt;
+    A.Lmin = Lmin;
+    A.Lmax = Lmax;
+    return c2_launch(A, nitems, cluster, Lmax, (cudaStream_t)stream);
 }

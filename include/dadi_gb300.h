@@ -302,6 +302,18 @@ int dgb_items2d_integrate(const dgb_item2d *items, int nitems, int Lmax, const d
                           const int *row_cnt, const int *order, const dgb_settings *settings,
                           int one_per_cta, void *ws, size_t ws_bytes, void *stream);
 
+/* dgb_items2d_integrate with one thread-block cluster of `cluster` CTAs per
+ * item (the kernel of dgb_integrate2d_cluster): for a few items, which one
+ * CTA each would leave bound by one SM's FP64 pipe.  Lmin / Lmax (host)
+ * bound every item's L and must satisfy dgb_integrate2d_cluster's range
+ * (else DGB_ERR_UNSUPPORTED); an item outside them is skipped.  Default
+ * delta_j only; no order, settings or workspace.  Results agree with
+ * dgb_items2d_integrate to rounding. */
+int dgb_items2d_integrate_cluster(const dgb_item2d *items, int nitems, int Lmin, int Lmax,
+                                  const double *xx_all, double *phi_out, const double *table,
+                                  const long *row_off, const int *row_cnt, int cluster,
+                                  void *stream);
+
 /* dgb_sched2d evaluated in C on the host (all arrays HOST): table == NULL
  * counts rows into row_cnt; otherwise writes the rows at table +
  * row_off[i]*11 and ORs status bits into status[i].  One schedule per

@@ -93,3 +93,55 @@ def test_dropin_auto_2d_is_tuned_per_grid(cuda_lib):
     assert integration.cluster_size_2d(100) == t["ctas"]
     assert integration.cluster_size_2d(100, delj=True) == 0
     assert integration.cluster_size_2d(20) == 0
+
+
+def test_items_on_clusters_match_one_cta_per_item(cuda_lib):
+    """dgb_items2d_integrate_cluster (one cluster of 8 CTAs per work item,
+    grids of 40-120 points, own schedules and masks) against
+    dgb_items2d_integrate (one CTA per item): 1e-12 relative; an item
+    outside the checked grid range is left untouched."""
+    import ctypes
+    import torch
+    from dadi_gb300 import _lib, batch
+    lib = cuda_lib
+    Ls = [40, 64, 120, 100, 33]
+    xx_h = [cases.grid("default", L) for L in Ls]
+    xx_off = np.cumsum([0] + Ls[:-1])
+    tabs = [table_rows(2, n, 700 + k) for k, n in enumerate([30, 12, 25, 1, 5])]
+    roff = np.cumsum([0] + [len(t) for t in tabs[:-1]]).astype(np.int64)
+    cnt = np.array([len(t) for t in tabs], dtype=np.int32)
+    items = np.zeros(5, dtype=batch.ITEM2D_DTYPE)
+    phi0, off = [], 0
+    for k, L in enumerate(Ls):
+        items["L"][k], items["xx_off"][k], items["out_off"][k] = L, xx_off[k], off
+        items["sched"][k], items["masks"][k] = k, [0, 1, 0, 2 << 8, 0][k]
+        phi0.append((np.abs(cases.initial_phi(30 + k, (L, L))) + 1e-3).reshape(-1))
+        off += L * L
+    d_items = _lib.to_device(torch, items.view(np.uint8), np.uint8)
+    d_xx = torch.from_numpy(np.concatenate(xx_h)).cuda()
+    d_tab = torch.from_numpy(np.concatenate(tabs)).cuda()
+    d_roff = torch.from_numpy(roff).cuda()
+    d_cnt = torch.from_numpy(cnt).cuda()
+    sh = _lib.stream_handle(torch)
+    ref = torch.from_numpy(np.concatenate(phi0)).cuda()
+    st = _lib.settings_struct()
+    ws, nws = _lib.workspace(torch, lib.dgb_workspace_bytes(3, 2, 120, 5))
+    _lib.check(lib.dgb_items2d_integrate(_lib.dptr(d_items), 5, 120, _lib.dptr(d_xx),
+                                         _lib.dptr(ref), _lib.dptr(d_tab), _lib.dptr(d_roff),
+                                         _lib.dptr(d_cnt), None, ctypes.byref(st), 1,
+                                         _lib.dptr(ws), nws, sh), "dgb_items2d_integrate")
+    out = torch.from_numpy(np.concatenate(phi0)).cuda()
+    _lib.check(lib.dgb_items2d_integrate_cluster(_lib.dptr(d_items), 5, 40, 120, _lib.dptr(d_xx),
+                                                 _lib.dptr(out), _lib.dptr(d_tab),
+                                                 _lib.dptr(d_roff), _lib.dptr(d_cnt), 8, sh),
+               "dgb_items2d_integrate_cluster")
+    ref, out = ref.cpu().numpy(), out.cpu().numpy()
+    off = 0
+    for k, L in enumerate(Ls):
+        a, b = out[off:off + L * L], ref[off:off + L * L]
+        if L < 40:   # outside [Lmin, Lmax]: skipped
+            assert np.array_equal(a, phi0[k])
+        else:
+            rel = np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-12 * np.abs(b).max()))
+            assert rel < 1e-12, (k, rel)
+        off += L * L

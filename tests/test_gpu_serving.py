@@ -1,10 +1,15 @@
 """The serving loop: a mixed request stream (2-D IM at assorted grid and
 sample sizes, DFE-style IM with selection, 3-D growth, four populations,
 gradient requests) arriving over time is served with continuous batching;
-every result equals the same request served alone (bitwise: each request's
-work is the same kernels on the same data, only its neighbours differ); the
-2-D results match the oracle (the reference's algorithm on the CPU) and the
-3-D / 4-D ones the one-at-a-time drop-in, within the spectrum bar."""
+every result equals the same request served alone -- bitwise for 3-D / 4-D
+spectra and gradients (the same kernels on the same data, only the
+neighbours differ), to 1e-10 relative for 2-D spectra (a small wave runs
+each work item on a cluster of CTAs, a large one on one CTA: the same
+equations solved in another order, whose last-bit differences accumulate
+over up to 19,546 steps and grow through the extrapolation: measured up to
+2.2e-11) -- the 2-D results match the oracle
+(the reference's algorithm on the CPU) and the 3-D / 4-D ones the
+one-at-a-time drop-in, within the spectrum bar."""
 import copy
 import multiprocessing as mp
 import os
@@ -48,7 +53,12 @@ def test_serving_mix_equals_alone_and_reference(cuda_lib):
     # each request alone, through a fresh server
     for r in reqs[:12]:
         alone = serving.Server(hbm_budget=8 << 30).run([copy.copy(r)])[0]
-        assert np.array_equal(alone.fs, by_id[r.rid].fs), r.kind
+        if r.kind in ("im", "im_sel"):
+            a, b = alone.fs, by_id[r.rid].fs
+            rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-12 * np.abs(b).max())
+            assert float(rel.max()) <= 1e-10, (r.kind, float(rel.max()))
+        else:
+            assert np.array_equal(alone.fs, by_id[r.rid].fs), r.kind
         if r.want_grad:
             assert np.array_equal(alone.grad, by_id[r.rid].grad)
     # 2-D results against the oracle (a spawn pool: this process uses CUDA)
