@@ -38,7 +38,7 @@ EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
            "dgb_from_phi_nd_workspace_bytes", "dgb_from_phi_nd", "dgb_adjoint2d_traj_ws_bytes",
            "dgb_adjoint2d_traj", "dgb_schednd_dual_host", "dgb_batchnd_adjoint_workspace_bytes",
            "dgb_batchnd_integrate_states", "dgb_batchnd_adjoint", "dgb_integrate2d_cluster",
-           "dgb_items2d_integrate_cluster"]
+           "dgb_items2d_integrate_cluster", "dgb_adjoint2d_part", "dgb_preload"]
 
 
 class PForm(ctypes.Structure):
@@ -106,6 +106,7 @@ def _declare(L):
     i, d, sz, lg = ctypes.c_int, ctypes.c_double, ctypes.c_size_t, ctypes.c_long
     sig = {
         "dgb_abi_version": (i, []),
+        "dgb_preload": (i, []),
         "dgb_status_string": (ctypes.c_char_p, [i]),
         "dgb_workspace_bytes": (sz, [i, i, i, lg]),
         "dgb_tridiag_batch": (i, [_vp, _vp, _vp, _vp, _vp, i, i, _vp, sz, _vp]),
@@ -156,6 +157,9 @@ def _declare(L):
         "dgb_adjoint2d_traj": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp,
                                    _vp, _vp, _vp, i, _vp, _vp, _vp, _vp, _vp, _vp,
                                    ctypes.POINTER(Settings), _vp, sz, _vp]),
+        "dgb_adjoint2d_part": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp,
+                                   _vp, _vp, _vp, i, _vp, _vp, _vp, _vp, _vp, _vp, i, i,
+                                   ctypes.POINTER(Settings), _vp, sz, _vp]),
         "dgb_adjoint2d": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp, _vp,
                               _vp, _vp, i, _vp, _vp, _vp, ctypes.POINTER(Settings), _vp, sz,
                               _vp]),
@@ -194,12 +198,22 @@ def check(status, what):
 
 # ---------------------------------------------------------------- devices
 
+_preloaded = set()
+
+
 def require_cuda():
-    """torch with a visible CUDA device, or a RuntimeError (no CPU fallback)."""
+    """torch with a visible CUDA device, or a RuntimeError (no CPU fallback).
+    The first call on a device loads every kernel of the library there
+    (dgb_preload), so that no kernel's first launch waits for the device to
+    go idle while other streams have work in flight."""
     import torch
     if not torch.cuda.is_available():
         raise RuntimeError("dadi_gb300 needs a CUDA device; none is visible")
-    lib()
+    L = lib()
+    dev = torch.cuda.current_device()
+    if dev not in _preloaded:
+        check(L.dgb_preload(), "dgb_preload")
+        _preloaded.add(dev)
     return torch
 
 

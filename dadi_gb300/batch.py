@@ -540,8 +540,12 @@ class Batch2D:
         """d(sum_i grad_ll[i] * ll_i)/d(params) by the discrete adjoint: (n, 6).
         trajectory: recompute every checkpoint segment at once into a stored
         trajectory first (True), each work item's segments in turn (False),
-        or the first when it fits traj_budget (None); the gradients are the
-        same bit for bit."""
+        or (None) the first for as many of the longest work items as
+        traj_budget holds -- all of them when it holds the whole trajectory
+        -- and the second for the rest, the two on their own streams at once:
+        the longest items' serial backward walks lose their recomputation,
+        which bounds a batch with a few long integrations.  The gradients are
+        the same bit for bit whichever way."""
         torch = self.torch
         lib = _lib.lib()
         phis = ctx["phis"]
@@ -566,12 +570,18 @@ class Batch2D:
             per_sm = max(1, min(4, per_sm))
         nblocks = min(n * ng, nsm * per_sm)
         st = ctx["st"]
-        if trajectory is None:
-            trajectory = self.trajectory_bytes(ctx) <= self.traj_budget
         common = (_lib.dptr(ctx["masks"]), n, self.Ls, ng, _lib.dptr(self.d_xx),
                   _lib.dptr(ctx["table"]), _lib.dptr(ctx["drows"]), _lib.dptr(ctx["off"]),
                   _lib.dptr(ctx["cnt"]), _lib.dptr(ctx["ckpt"]), _lib.dptr(ctx["ck_off"]), C)
-        if trajectory:
+        if trajectory is None:
+            if self.trajectory_bytes(ctx) <= self.traj_budget:
+                trajectory = True
+            else:
+                self._adjoint_hybrid(ctx, lam, part, common, nblocks, nsm, Lmax)
+                trajectory = "hybrid"
+        if trajectory == "hybrid":
+            pass
+        elif trajectory:
             steps = self._work_steps(ctx).reshape(-1)
             Lsq = np.tile(np.array([L * L for L in self.pts_l], dtype=np.int64), n)
             size = (2 * steps + 1) * Lsq
@@ -599,6 +609,52 @@ class Batch2D:
         for gi in range(1, ng):
             grad += part[:, gi]
         return grad
+
+    def _adjoint_hybrid(self, ctx, lam, part, common, nblocks, nsm, Lmax):
+        """The longest work items (while their trajectory fits traj_budget)
+        in trajectory mode on the current stream, one CTA each, and the rest
+        with per-CTA segment recomputation on a side stream on the other
+        CTAs (dgb_adjoint2d_part twice)."""
+        torch = self.torch
+        lib = _lib.lib()
+        n, ng, C, st = ctx["n"], len(self.pts_l), ctx["C"], ctx["st"]
+        steps = self._work_steps(ctx).reshape(-1)
+        Lsq = np.tile(np.array([L * L for L in self.pts_l], dtype=np.int64), n)
+        order = np.argsort(-(steps * Lsq), kind="stable").astype(np.int32)
+        size = (2 * steps + 1) * Lsq * 8
+        k = int(np.searchsorted(np.cumsum(size[order]), self.traj_budget, side="right"))
+        k = max(1, min(k, len(order) - 1))
+        tset = order[:k]
+        t_off = np.zeros(n * ng, dtype=np.int64)
+        t_off[tset] = np.concatenate([[0], np.cumsum(size[tset] // 8)[:-1]])
+        nseg = np.zeros(n * ng, dtype=np.int64)
+        nseg[tset] = (steps[tset] + C - 1) // C
+        seg_off = np.zeros(n * ng + 1, dtype=np.int64)
+        np.cumsum(nseg, out=seg_off[1:])
+        traj = torch.empty(max(int(size[tset].sum() // 8), 1), dtype=torch.float64,
+                           device="cuda")
+        d_toff = _lib.to_device(torch, t_off, np.int64)
+        d_soff = _lib.to_device(torch, seg_off, np.int64)
+        d_order = _lib.to_device(torch, order, np.int32)
+        ws_t, nws_t = _lib.workspace(torch, lib.dgb_adjoint2d_traj_ws_bytes(Lmax, 2 * nsm))
+        rest = max(1, nblocks - k)
+        ws_s, nws_s = _lib.workspace(torch, 256 + lib.dgb_adjoint2d_scratch_bytes(Lmax, C, 1)
+                                     * rest)
+        main = torch.cuda.current_stream()
+        side = torch.cuda.Stream()
+        side.wait_stream(main)
+        _lib.check(lib.dgb_adjoint2d_part(
+            *common, _lib.dptr(traj), _lib.dptr(d_toff), _lib.dptr(d_soff), _lib.dptr(lam),
+            _lib.dptr(part), _lib.dptr(d_order), k, k, ctypes.byref(st), _lib.dptr(ws_t), nws_t,
+            _lib.stream_handle(torch)), "dgb_adjoint2d_part(trajectory)")
+        with torch.cuda.stream(side):
+            _lib.check(lib.dgb_adjoint2d_part(
+                *common, None, None, None, _lib.dptr(lam), _lib.dptr(part),
+                _lib.dptr(d_order[k:]), len(order) - k, rest, ctypes.byref(st),
+                _lib.dptr(ws_s), nws_s, _lib.stream_handle(torch)), "dgb_adjoint2d_part")
+        main.wait_stream(side)
+        for t in (traj, d_toff, d_soff, d_order, ws_t, ws_s):
+            t.record_stream(side)
 
     def spectra(self, phis):
         """Per-grid raw spectra (n, n1+1, n2+1) on the device."""

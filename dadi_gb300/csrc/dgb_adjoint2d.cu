@@ -807,18 +807,21 @@ extern "C" size_t dgb_adjoint2d_scratch_bytes(int Lmax, int ckpt_every, int nblo
     return (size_t)nblocks * (2 * ckpt_every + 3) * Lmax * Lmax * sizeof(double);
 }
 
+// norder: the work items of `order` to walk (<= 0: all ninst x ngrids);
+// max_blocks: most CTAs of the backward walk (<= 0: as many as the workspace
+// and the items allow).
 static int adjoint2d_run(const int *masks, int ninst, const int *Ls, int ngrids,
                          const double *xx_all, const double *table, const double *drows,
                          const long *row_off, const int *row_cnt, const double *ckpt,
                          const long *ckpt_off, int ckpt_every, double *lam, double *grad,
-                         const int *order, const dgb_settings *settings, double *traj,
-                         const long *traj_off, const long *seg_off, void *ws, size_t ws_bytes,
-                         void *stream)
+                         const int *order, int norder, int max_blocks,
+                         const dgb_settings *settings, double *traj, const long *traj_off,
+                         const long *seg_off, void *ws, size_t ws_bytes, void *stream)
 {
     using namespace dgb;
     if (!Ls || !xx_all || !table || !drows || !row_off || !row_cnt || !ckpt || !ckpt_off ||
         ckpt_every < 1 || !lam || !grad || !order || !settings || ngrids < 1 ||
-        ngrids > AD_MAXG || ninst < 1)
+        ngrids > AD_MAXG || ninst < 1 || norder > ninst * ngrids)
         return DGB_ERR_ARG;
     if (settings->use_delj_trick)
         return DGB_ERR_UNSUPPORTED;
@@ -862,7 +865,12 @@ static int adjoint2d_run(const int *masks, int ninst, const int *Ls, int ngrids,
     long nblocks = (long)((ws_bytes - 256) / per_cta);
     if (nblocks < 1)
         return DGB_ERR_WORKSPACE;
-    nblocks = std::min<long>(nblocks, A.nwork);
+    // the walk covers the first norder entries of `order`; the trajectory's
+    // recomputation (every work id with segments in seg_off) sees them all
+    const int nwalk = norder > 0 ? norder : A.nwork;
+    nblocks = std::min<long>(nblocks, nwalk);
+    if (max_blocks > 0)
+        nblocks = std::min<long>(nblocks, max_blocks);
     A.scratch = (double *)((char *)ws + 256);
     size_t smem = (size_t)AD_VEC_DOUBLES * Lmax * sizeof(double);
     {
@@ -896,6 +904,7 @@ static int adjoint2d_run(const int *masks, int ninst, const int *Ls, int ngrids,
     }
     if (cudaMemsetAsync(A.counter, 0, sizeof(int), (cudaStream_t)stream) != cudaSuccess)
         return DGB_ERR_CUDA;
+    A.nwork = nwalk;
     if (traj)
         k_adjoint2d<true><<<(unsigned)nblocks, AD_THREADS, smem, (cudaStream_t)stream>>>(A);
     else
@@ -911,8 +920,8 @@ extern "C" int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngr
                              size_t ws_bytes, void *stream)
 {
     return adjoint2d_run(masks, ninst, Ls, ngrids, xx_all, table, drows, row_off, row_cnt, ckpt,
-                         ckpt_off, ckpt_every, lam, grad, order, settings, nullptr, nullptr,
-                         nullptr, ws, ws_bytes, stream);
+                         ckpt_off, ckpt_every, lam, grad, order, 0, 0, settings, nullptr,
+                         nullptr, nullptr, ws, ws_bytes, stream);
 }
 
 extern "C" size_t dgb_adjoint2d_traj_ws_bytes(int Lmax, int nblocks)
@@ -932,6 +941,30 @@ extern "C" int dgb_adjoint2d_traj(const int *masks, int ninst, const int *Ls, in
     if (!traj || !traj_off || !seg_off)
         return DGB_ERR_ARG;
     return adjoint2d_run(masks, ninst, Ls, ngrids, xx_all, table, drows, row_off, row_cnt, ckpt,
-                         ckpt_off, ckpt_every, lam, grad, order, settings, traj, traj_off,
+                         ckpt_off, ckpt_every, lam, grad, order, 0, 0, settings, traj, traj_off,
                          seg_off, ws, ws_bytes, stream);
 }
+
+extern "C" int dgb_adjoint2d_part(const int *masks, int ninst, const int *Ls, int ngrids,
+                                  const double *xx_all, const double *table,
+                                  const double *drows, const long *row_off, const int *row_cnt,
+                                  const double *ckpt, const long *ckpt_off, int ckpt_every,
+                                  double *traj, const long *traj_off, const long *seg_off,
+                                  double *lam, double *grad, const int *order, int norder,
+                                  int max_blocks, const dgb_settings *settings, void *ws,
+                                  size_t ws_bytes, void *stream)
+{
+    if (norder < 1 || (traj && (!traj_off || !seg_off)))
+        return DGB_ERR_ARG;
+    return adjoint2d_run(masks, ninst, Ls, ngrids, xx_all, table, drows, row_off, row_cnt, ckpt,
+                         ckpt_off, ckpt_every, lam, grad, order, norder, max_blocks, settings,
+                         traj, traj_off, seg_off, ws, ws_bytes, stream);
+}
+
+namespace dgb {
+int preload_adjoint2d()
+{
+    return preload(k_sched2d_dual) + preload(k_adjoint2d<false>) + preload(k_adjoint2d<true>) +
+           preload(k_adjoint2d_traj);
+}
+} // namespace dgb

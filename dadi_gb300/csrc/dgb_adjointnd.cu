@@ -208,3 +208,7 @@ extern "C" int dgb_adjoint_table_nd(double *lam, int ndim, int L, const double *
     }
     return DGB_OK;
 }
+
+namespace dgb {
+int preload_adjointnd() { return preload(k_adjoint_sweep_nd) + preload(k_adjoint_inject_nd); }
+} // namespace dgb

@@ -1478,3 +1478,16 @@ extern "C" int dgb_schednd_dual_host(const dgb_instnd *inst, const dgb_seednd *s
         *status |= err;
     return DGB_OK;
 }
+
+namespace dgb {
+int preload_batchnd()
+{
+    return preload(k_coef_batch<false>) + preload(k_coef_batch<true>) +
+           preload(k_sweep_batch<false, false>) + preload(k_sweep_batch<false, true>) +
+           preload(k_sweep_batch<true, false>) + preload(k_sweep_batch<true, true>) +
+           preload(k_sweep_batch_pcr) + preload(k_sweep_batch_part<2>) +
+           preload(k_sweep_batch_part<4>) + preload(k_sweep_batch_part<8>) +
+           preload(k_store_states) + preload(k_slot_copy) + preload(k_adjoint_sweep_batch) +
+           preload(k_adjoint_inject_batch);
+}
+} // namespace dgb

@@ -507,3 +507,19 @@ extern "C" int dgb_items2d_integrate_cluster(const dgb_item2d *items, int nitems
     A.Lmax = Lmax;
     return c2_launch(A, nitems, cluster, Lmax, (cudaStream_t)stream);
 }
+
+namespace dgb {
+int preload_cluster2d() { return preload(k_integrate2d_cluster); }
+} // namespace dgb
+
+extern "C" int dgb_preload(void)
+{
+    const int bad = preload_integrate2d() + preload_sweepnd() + preload_probe() +
+                    preload_adjoint2d() + preload_fsepi() + preload_adjointnd() +
+                    preload_batchnd() + preload_cluster2d();
+    if (bad) {
+        cudaGetLastError();
+        return DGB_ERR_CUDA;
+    }
+    return DGB_OK;
+}

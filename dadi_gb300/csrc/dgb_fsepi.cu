@@ -418,3 +418,10 @@ extern "C" int dgb_extrap_ll(const dgb_extrap_item *items, int nitems, double fa
     k_extrap_ll<<<(unsigned)nitems, FS_THREADS, 0, (cudaStream_t)stream>>>(items, fail_mag);
     return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
 }
+
+namespace dgb {
+int preload_fsepi()
+{
+    return preload(k_from_phi2d) + preload(k_extrap_ll) + preload(k_contract_last);
+}
+} // namespace dgb

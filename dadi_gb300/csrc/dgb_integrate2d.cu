@@ -1102,3 +1102,11 @@ extern "C" int dgb_sched2d_host(const dgb_inst2d *insts, int ninst,
     }
     return DGB_OK;
 }
+
+namespace dgb {
+int preload_integrate2d()
+{
+    return preload(k_integrate2d<false>) + preload(k_integrate2d<true>) +
+           preload(k_integrate2d_pair) + preload(k_sched2d);
+}
+} // namespace dgb

@@ -56,6 +56,26 @@ template <typename Kernel> inline int raise_smem_limit(Kernel kernel)
 {
     return raise_smem_limit_ptr((const void *)kernel);
 }
+
+// Load a kernel now (1 if it cannot be).  Under lazy module loading a
+// kernel is loaded at its first launch, and loading can wait for the device
+// to go idle: a first launch on one stream then serialises behind the work
+// other streams have in flight.
+template <typename Kernel> inline int preload(Kernel kernel)
+{
+    cudaFuncAttributes fa;
+    return cudaFuncGetAttributes(&fa, (const void *)kernel) == cudaSuccess ? 0 : 1;
+}
+
+// Each translation unit's kernels (dgb_preload loads them all).
+int preload_integrate2d();
+int preload_sweepnd();
+int preload_probe();
+int preload_adjoint2d();
+int preload_fsepi();
+int preload_adjointnd();
+int preload_batchnd();
+int preload_cluster2d();
 } // namespace dgb
 
 namespace dgb {

@@ -3,6 +3,7 @@
 // FP64 pipe, whose rate is not in the machine's measured peaks).  Eight
 // independent FMA chains per thread; the launch shape is the caller's.
 #include "dgb_common.cuh"
+#include "dgb_internal.h"
 
 namespace dgb {
 __global__ void k_fp64_fma(double *out, int iters, int active_lanes)
@@ -51,3 +52,7 @@ extern "C" int dgb_probe_rcp(const double *x, double *out, int n, void *stream)
     dgb::k_rcp<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(x, out, n);
     return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
 }
+
+namespace dgb {
+int preload_probe() { return preload(k_fp64_fma) + preload(k_rcp); }
+} // namespace dgb

@@ -489,3 +489,12 @@ extern "C" int dgb_integrate_precalc(double *phi, int ndim, int L, const double 
     }
     return DGB_OK;
 }
+
+namespace dgb {
+int preload_sweepnd()
+{
+    return preload(k_sweep_nd<false>) + preload(k_sweep_nd<true>) + preload(k_coef_nd<false>) +
+           preload(k_coef_nd<true>) + preload(k_sweep_nd_rec<false>) +
+           preload(k_sweep_nd_rec<true>) + preload(k_precalc_nd) + preload(k_tridiag_batch);
+}
+} // namespace dgb

@@ -91,6 +91,13 @@ typedef struct {
 int dgb_abi_version(void);
 const char *dgb_status_string(int status);
 
+/* Load every kernel of the library on the current device now.  CUDA loads a
+ * kernel at its first launch by default, and that load can wait for the
+ * device to go idle, so a first launch on one stream would serialise behind
+ * work in flight on others; call this once before concurrent use
+ * (DGB_ERR_CUDA if a kernel cannot be loaded). */
+int dgb_preload(void);
+
 /* Scratch bytes needed by a call.  kind: 0 = dgb_integrate_table /
  * dgb_integrate_table_states / dgb_integrate_precalc / the single sweeps
  * (for 3-5 populations and 2-D grids too large for shared memory: per-step
@@ -272,6 +279,22 @@ int dgb_adjoint2d_traj(const int *masks, int ninst, const int *Ls, int ngrids,
                        const long *row_off, const int *row_cnt, const double *ckpt,
                        const long *ckpt_off, int ckpt_every, double *traj, const long *traj_off,
                        const long *seg_off, double *lam, double *grad, const int *order,
+                       const dgb_settings *settings, void *ws, size_t ws_bytes, void *stream);
+
+/* dgb_adjoint2d / dgb_adjoint2d_traj over part of the work items: the walk
+ * covers order[0 .. norder) (work ids inst * ngrids + grid) on at most
+ * max_blocks CTAs (<= 0: no cap), so that two calls on two streams share
+ * the GPU -- e.g. the longest items in trajectory mode (traj non-null;
+ * seg_off over all ninst * ngrids work ids, zero segments for the others)
+ * and the rest with per-CTA segment recomputation (traj null: ws as for
+ * dgb_adjoint2d).  Each item's lambda and gradient part are those of the
+ * whole-batch calls, bit for bit. */
+int dgb_adjoint2d_part(const int *masks, int ninst, const int *Ls, int ngrids,
+                       const double *xx_all, const double *table, const double *drows,
+                       const long *row_off, const int *row_cnt, const double *ckpt,
+                       const long *ckpt_off, int ckpt_every, double *traj,
+                       const long *traj_off, const long *seg_off, double *lam, double *grad,
+                       const int *order, int norder, int max_blocks,
                        const dgb_settings *settings, void *ws, size_t ws_bytes, void *stream);
 
 /* One work item of dgb_items2d_integrate: a 2-D integration on grid

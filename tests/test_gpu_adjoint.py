@@ -130,3 +130,25 @@ def test_adjoint_trajectory_mode_is_bitwise(cuda_lib, golden):
         _, g_traj, _ = eng.loglik_and_grad(draws[sel], data, scale=1e4, ckpt_every=C,
                                            trajectory=True)
         assert np.array_equal(g_seg.cpu().numpy(), g_traj.cpu().numpy()), C
+
+
+def test_adjoint_hybrid_mode_is_bitwise(cuda_lib, golden):
+    """With a trajectory budget that holds only the longest work items, those
+    walk back from a stored trajectory on the current stream while the rest
+    recompute their segments on a side stream (dgb_adjoint2d_part twice);
+    the gradients are the segment-by-segment adjoint's bit for bit."""
+    from dadi_gb300 import batch
+    draws = cases.im_draws(4096)
+    steps = batch.count_steps(batch.im_instances(draws))
+    sel = [i for i in range(64) if 30 <= steps[i] <= 1500][:6]
+    data = golden["grad"]["grad_data"]
+    eng = _engine()
+    _, g_seg, _ = eng.loglik_and_grad(draws[sel], data, scale=1e4, ckpt_every=7,
+                                      trajectory=False)
+    ll, ctx = eng.forward_for_adjoint(draws[sel], data, scale=1e4, ckpt_every=7)
+    eng.traj_budget = eng.trajectory_bytes(ctx) // 3   # about a third of the items
+    try:
+        _, g_hyb, _ = eng.loglik_and_grad(draws[sel], data, scale=1e4, ckpt_every=7)
+    finally:
+        eng.traj_budget = batch.Batch2D.traj_budget
+    assert np.array_equal(g_seg.cpu().numpy(), g_hyb.cpu().numpy())

@@ -17,12 +17,14 @@ def _alone(phi0, xx, table, masks, delj=False):
     """The drop-in's one-at-a-time integration with the Thomas solve
     (dgb_integrate_table)."""
     from dadi_gb300 import integration
-    saved = integration.use_delj_trick, integration.nd_line_solver
+    saved = integration.use_delj_trick, integration.nd_line_solver, integration.line_solver_2d
     integration.use_delj_trick, integration.nd_line_solver = delj, "thomas"
+    integration.line_solver_2d = "thomas"
     try:
         return integration.run_table(phi0, xx, table, masks & 0xff, masks >> 8)
     finally:
-        integration.use_delj_trick, integration.nd_line_solver = saved
+        (integration.use_delj_trick, integration.nd_line_solver,
+         integration.line_solver_2d) = saved
 
 
 @pytest.mark.parametrize("P,L,gam,threads,delj", [
