@@ -559,9 +559,11 @@ def run_serving(a, obs):
     from dadi_gb300 import serving
     srv = serving.Server(hbm_budget=a.serve_budget << 30)
     srv.prepare(range(40, 121), [(20, 20), (40, 40)])
-    # warm-up stream: library handles, worker engines
-    srv.run(serving.config5_stream(max(8, a.serve // 20), seed=1, rate=a.serve_rate,
-                                   obs=obs))
+    # warm-up: a stream of the same size (another seed), so that the measured
+    # burst meets the server in its steady state -- worker engines built, and
+    # the allocator's per-stream memory pools grown (the first burst a server
+    # sees pays device allocations in its waves: p50 5.5 s against 1.1 s)
+    srv.run(serving.config5_stream(a.serve, seed=1, rate=a.serve_rate, obs=obs))
     summ = _serve_stream(srv, a.serve, a.serve_rate, obs, a.serve_budget)
     if a.serve_sustained > 0:
         # the same mix at a rate the server keeps up with: latency without

@@ -152,6 +152,7 @@ class Server:
         self.cluster_items = int(cluster_items)
         self.workers = workers
         self.max_nd_group = int(max_nd_group)
+        self._streams = None
         self._used = 0
         self._lock = threading.Lock()
         self._grids = {}
@@ -394,8 +395,13 @@ class Server:
         waiting2d, inflight, futures = [], [], []
         # integrations at the lowest priority, spectra at the highest (torch
         # clamps to the device's range)
-        free_streams = [torch.cuda.Stream(priority=0) for _ in range(self.max_inflight)]
-        tail = torch.cuda.Stream(priority=-8)
+        # the server's own streams, kept across runs: the caching allocator
+        # keeps a memory pool per stream, and a burst on fresh streams pays
+        # device allocations (which stall the device) in its first waves
+        if self._streams is None:
+            self._streams = ([torch.cuda.Stream(priority=0) for _ in range(self.max_inflight)],
+                             torch.cuda.Stream(priority=-8))
+        free_streams, tail = list(self._streams[0]), self._streams[1]
         pool = ThreadPoolExecutor(max_workers=self.workers)
         gpool = ThreadPoolExecutor(max_workers=self.workers)
         # the scheduling loop must get the interpreter back quickly from
