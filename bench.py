@@ -565,6 +565,7 @@ def run_serving(a, obs):
     # sees pays device allocations in its waves: p50 5.5 s against 1.1 s)
     srv.run(serving.config5_stream(a.serve, seed=1, rate=a.serve_rate, obs=obs))
     summ = _serve_stream(srv, a.serve, a.serve_rate, obs, a.serve_budget)
+    summ["warmup"] = "a %d-request stream of the same mix (seed 1) served first" % a.serve
     if a.serve_sustained > 0:
         # the same mix at a rate the server keeps up with: latency without
         # the backlog of a burst
