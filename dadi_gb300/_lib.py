@@ -38,7 +38,8 @@ EXPORTS = ["dgb_abi_version", "dgb_status_string", "dgb_workspace_bytes",
            "dgb_from_phi_nd_workspace_bytes", "dgb_from_phi_nd", "dgb_adjoint2d_traj_ws_bytes",
            "dgb_adjoint2d_traj", "dgb_schednd_dual_host", "dgb_batchnd_adjoint_workspace_bytes",
            "dgb_batchnd_integrate_states", "dgb_batchnd_adjoint", "dgb_integrate2d_cluster",
-           "dgb_items2d_integrate_cluster", "dgb_adjoint2d_part", "dgb_preload"]
+           "dgb_items2d_integrate_cluster", "dgb_adjoint2d_part", "dgb_preload",
+           "dgb_batch2d_integrate_ckpt_part"]
 
 
 class PForm(ctypes.Structure):
@@ -146,7 +147,12 @@ def _declare(L):
                                       _vp, _vp]),
         "dgb_batchnd_adjoint_workspace_bytes": (sz, [i, i, i, ctypes.POINTER(Settings)]),
         "dgb_integrate2d_cluster": (i, [_vp, i, _vp, _vp, i, i, i, i, _vp]),
-        "dgb_items2d_integrate_cluster": (i, [_vp, i, i, i, _vp, _vp, _vp, _vp, _vp, i, _vp]),
+        "dgb_items2d_integrate_cluster": (i, [_vp, i, i, i, _vp, _vp, _vp, _vp, _vp, i, _vp,
+                                              _vp, i, _vp]),
+        "dgb_batch2d_integrate_ckpt_part": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp,
+                                                _vp, _vp, _vp, _vp, _vp, _vp, i, i,
+                                                ctypes.POINTER(Settings), _vp, _vp, i, _vp, sz,
+                                                _vp]),
         "dgb_batchnd_integrate_states": (i, [_vp, i, i, i, _vp, _vp, _vp, _vp,
                                              ctypes.POINTER(Settings), _vp, sz, _vp]),
         "dgb_batchnd_adjoint": (i, [_vp, i, i, i, _vp, _vp, _vp, _vp, _vp,

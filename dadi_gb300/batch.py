@@ -489,11 +489,17 @@ class Batch2D:
         d_out = torch.empty(total, dtype=torch.float64, device="cuda")
         nws = lib.dgb_workspace_bytes(1, 2, max(self.pts_l), n * ng)
         ws, nws = _lib.workspace(torch, nws)
-        _lib.check(lib.dgb_batch2d_integrate_ckpt(
-            _lib.dptr(d_masks), n, self.Ls, ng, _lib.dptr(self.d_xx), _lib.dptr(self.d_phi0),
-            _lib.dptr(d_out), _lib.dptr(table), _lib.dptr(off), _lib.dptr(cnt), _lib.dptr(d_order),
-            ctypes.byref(st), _lib.dptr(ckpt), _lib.dptr(ck_off), C, _lib.dptr(ws), nws, sh),
-            "dgb_batch2d_integrate_ckpt")
+        common = (_lib.dptr(d_masks), n, self.Ls, ng, _lib.dptr(self.d_xx),
+                  _lib.dptr(self.d_phi0), _lib.dptr(d_out), _lib.dptr(table), _lib.dptr(off),
+                  _lib.dptr(cnt))
+        longest = self._cluster_work(cnt, masks, st) if self.cluster_forward else None
+        if longest is None:
+            _lib.check(lib.dgb_batch2d_integrate_ckpt(
+                *common, _lib.dptr(d_order), ctypes.byref(st), _lib.dptr(ckpt), _lib.dptr(ck_off),
+                C, _lib.dptr(ws), nws, sh), "dgb_batch2d_integrate_ckpt")
+        else:
+            self._forward_split(longest, common, d_out, ckpt, ck_off, C, table, off, cnt, st, ws,
+                                nws)
         phis, o = [], 0
         for L in self.pts_l:
             phis.append(d_out[o:o + n * L * L].view(n, L, L).detach().requires_grad_(True))
@@ -514,6 +520,84 @@ class Batch2D:
         ctx = dict(phis=phis, ll=ll, fs=fs.detach(), table=table, off=off, cnt=cnt, drows=drows, ckpt=ckpt,
                    ck_off=ck_off, C=C, masks=d_masks, order=d_order, status=status, n=n, st=st)
         return ll, ctx
+
+    #: Run the forward of a few integrations on thread-block clusters (8
+    #: CTAs each; see _cluster_work).
+    cluster_forward = True
+
+    def _cluster_work(self, cnt, masks, st):
+        """The work items to run on clusters in the forward: all of them when
+        each can have a cluster of 8 CTAs (a few integrations, each bound by
+        one SM's FP64 pipe on one CTA: the longest seed-0 request's forward
+        3.48 -> 2.14 s), else none -- a larger batch has a tail of long items
+        too many for clusters, and SMs reserved for a few of them slow the
+        rest (256 sets: 3.09 -> 3.36 s with its 9 longest items on
+        clusters).  Grids of 24-128 points, default delta_j."""
+        torch = self.torch
+        if st.use_delj_trick or not all(24 <= L <= 128 for L in self.pts_l):
+            return None
+        ng = len(self.pts_l)
+        steps = _lib.to_host(torch, cnt).astype(np.int64)
+        steps = steps.reshape(-1, ng) if st.use_old_timestep else \
+            np.repeat(steps.reshape(-1, 1), ng, axis=1)
+        n = steps.shape[0]
+        nsm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        if n * ng * 8 > nsm:
+            return None
+        Lsq = np.array([L * L for L in self.pts_l], dtype=np.int64)
+        order = np.argsort(-(steps * Lsq[None, :]).reshape(-1), kind="stable")
+        return dict(order=order.astype(np.int32), pick=[int(w) for w in order], steps=steps,
+                    n=n, masks=np.asarray(masks, dtype=np.int32))
+
+    def _forward_split(self, longest, common, d_out, ckpt, ck_off, C, table, off, cnt, st, ws,
+                       nws):
+        """The forward with checkpoints with its longest work items on
+        clusters (dgb_items2d_integrate_cluster, the current stream) and the
+        rest through dgb_batch2d_integrate_ckpt_part on a side stream,
+        leaving the clusters their SMs."""
+        torch = self.torch
+        lib = _lib.lib()
+        ng = len(self.pts_l)
+        n, pick, order = longest["n"], longest["pick"], longest["order"]
+        xo = np.concatenate([[0], np.cumsum(self.pts_l)[:-1]]).astype(np.int64)
+        go = np.concatenate([[0], np.cumsum([n * L * L for L in self.pts_l])[:-1]])
+        po = np.concatenate([[0], np.cumsum([L * L for L in self.pts_l])[:-1]])
+        items = np.zeros(len(pick), dtype=ITEM2D_DTYPE)
+        ck_h = _lib.to_host(torch, ck_off)
+        for k, w in enumerate(pick):
+            inst, g = divmod(w, ng)
+            L = self.pts_l[g]
+            items["L"][k], items["xx_off"][k] = L, xo[g]
+            items["out_off"][k] = go[g] + inst * L * L
+            items["sched"][k] = w if st.use_old_timestep else inst
+            items["masks"][k] = longest["masks"][inst]
+            # the initial density, integrated in place in its output slot
+            d_out[items["out_off"][k]:items["out_off"][k] + L * L].copy_(
+                self.d_phi0[po[g]:po[g] + L * L])
+        d_items = _lib.to_device(torch, items.view(np.uint8), np.uint8)
+        d_ckoff = _lib.to_device(torch, ck_h[pick].astype(np.int64), np.int64)
+        picked = set(pick)
+        rest = np.array([w for w in order if w not in picked], dtype=np.int32)
+        d_rest = _lib.to_device(torch, rest, np.int32) if len(rest) else None
+        main = torch.cuda.current_stream()
+        side = torch.cuda.Stream()
+        side.wait_stream(main)
+        Ls = [self.pts_l[w % ng] for w in pick]
+        _lib.check(lib.dgb_items2d_integrate_cluster(
+            _lib.dptr(d_items), len(pick), min(Ls), max(Ls), _lib.dptr(self.d_xx),
+            _lib.dptr(d_out), _lib.dptr(table), _lib.dptr(off), _lib.dptr(cnt), 8,
+            _lib.dptr(ckpt), _lib.dptr(d_ckoff), C, _lib.stream_handle(torch)),
+            "dgb_items2d_integrate_cluster")
+        if d_rest is not None:
+            with torch.cuda.stream(side):
+                _lib.check(lib.dgb_batch2d_integrate_ckpt_part(
+                    *common, _lib.dptr(d_rest), len(rest), 8 * len(pick), ctypes.byref(st),
+                    _lib.dptr(ckpt), _lib.dptr(ck_off), C, _lib.dptr(ws), nws,
+                    _lib.stream_handle(torch)), "dgb_batch2d_integrate_ckpt_part")
+            main.wait_stream(side)
+            for t in (d_rest, ws):
+                t.record_stream(side)
+        self._split_keep = (d_items, d_ckoff, d_rest)
 
     #: Largest trajectory (bytes) the adjoint stores so that every checkpoint
     #: segment is recomputed at once (dgb_adjoint2d_traj); beyond it each

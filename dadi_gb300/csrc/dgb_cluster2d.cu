@@ -53,6 +53,11 @@ struct C2Args {
     const long *row_off; // first table row of each schedule
     const int *row_cnt;  // rows of each schedule
     int Lmin, Lmax;      // the grid sizes the launch was checked for
+    // optional: phi before every ckpt_every-th step, row-major, item i's
+    // checkpoints from ckpt + ckpt_off[i] (the forward of the adjoint)
+    double *ckpt;
+    const long *ckpt_off;
+    int ckpt_every;
 };
 
 struct C2Shared {
@@ -87,6 +92,7 @@ __global__ void __launch_bounds__(C2_THREADS) k_integrate2d_cluster(C2Args A)
     double *phi_g = A.phi;
     const double *xx = A.xx, *table = A.table;
     int L = A.L, nsteps = A.nsteps, frozen = A.frozen, nomut = A.nomut;
+    double *ck = nullptr;
     if (A.items) {
         // this cluster's work item; every CTA of the cluster reads the same
         // one, so a skipped item is skipped by the whole cluster
@@ -100,6 +106,8 @@ __global__ void __launch_bounds__(C2_THREADS) k_integrate2d_cluster(C2Args A)
         nsteps = A.row_cnt[it.sched];
         frozen = it.masks & 0xff;
         nomut = it.masks >> 8 & 0xff;
+        if (A.ckpt)
+            ck = A.ckpt + A.ckpt_off[blockIdx.x / S];
     }
     const int tid = threadIdx.x, pitch = c2_pitch(L);
     int R0, m;
@@ -159,6 +167,14 @@ __global__ void __launch_bounds__(C2_THREADS) k_integrate2d_cluster(C2Args A)
 
     for (int step = 0; step < nsteps; step++) {
         const double *row = table + (size_t)step * 11;
+        if (ck && step % A.ckpt_every == 0) {
+            // this CTA's rows of phi before the step
+            double *c = ck + (size_t)(step / A.ckpt_every) * L * L + (size_t)R0 * L;
+            for (int idx = tid; idx < m * L; idx += C2_THREADS) {
+                const int p = idx / L, q = idx - p * L;
+                c[idx] = blk[p * pitch + q];
+            }
+        }
         if (tid < 2) {
             AxisScalars &s = Sh.ax[tid];
             const int a = tid;
@@ -485,10 +501,11 @@ extern "C" int dgb_integrate2d_cluster(double *phi, int L, const double *xx, con
 extern "C" int dgb_items2d_integrate_cluster(const dgb_item2d *items, int nitems, int Lmin,
                                              int Lmax, const double *xx_all, double *phi_out,
                                              const double *table, const long *row_off,
-                                             const int *row_cnt, int cluster, void *stream)
+                                             const int *row_cnt, int cluster, double *ckpt,
+                                             const long *ckpt_off, int ckpt_every, void *stream)
 {
     if (!items || nitems < 0 || !xx_all || !phi_out || !table || !row_off || !row_cnt ||
-        Lmin > Lmax)
+        Lmin > Lmax || (ckpt && (!ckpt_off || ckpt_every < 1)))
         return DGB_ERR_ARG;
     if (cluster != 2 && cluster != 4 && cluster != 8 && cluster != 16)
         return DGB_ERR_ARG;
@@ -505,6 +522,9 @@ extern "C" int dgb_items2d_integrate_cluster(const dgb_item2d *items, int nitems
     A.row_cnt = row_cnt;
     A.Lmin = Lmin;
     A.Lmax = Lmax;
+    A.ckpt = ckpt;
+    A.ckpt_off = ckpt_off;
+    A.ckpt_every = ckpt_every;
     return c2_launch(A, nitems, cluster, Lmax, (cudaStream_t)stream);
 }
 

@@ -755,11 +755,15 @@ size_t k2_batch_ws_bytes(int Lmax, long nwork)
     return 256 + (size_t)k2_num_sms() * 4 * Lmax * Lmax * sizeof(double);
 }
 
+// norder: integrate only the work items order[0 .. norder) (<= 0: all);
+// reserve_sms: SMs to leave to launches running at the same time (the CTAs
+// are capped at (SMs - reserve_sms) x CTAs per SM).
 int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const double *xx_all,
              const double *phi0_all, double *phi_out, const double *table, const long *row_off,
              const int *row_cnt, int sched_per_grid, const int *order,
              const dgb_settings *settings, void *ws, size_t ws_bytes, cudaStream_t st,
-             double *ckpt = nullptr, const long *ckpt_off = nullptr, int ckpt_every = 0)
+             double *ckpt = nullptr, const long *ckpt_off = nullptr, int ckpt_every = 0,
+             int norder = 0, int reserve_sms = 0)
 {
     if (ngrids < 1 || ngrids > K2_MAXG || ninst < 1)
         return DGB_ERR_ARG;
@@ -788,7 +792,7 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     A.sched_per_grid = sched_per_grid;
     A.masks = masks;
     A.order = order;
-    A.nwork = ninst * ngrids;
+    A.nwork = (norder > 0 && norder < ninst * ngrids) ? norder : ninst * ngrids;
     A.Lmax = Lmax;
     A.use_delj = settings->use_delj_trick;
     A.ckpt = ckpt;
@@ -870,6 +874,10 @@ int k2_batch(int ninst, const int *masks, const int *Ls, int ngrids, const doubl
     if (nblocks < 1)
         return DGB_ERR_WORKSPACE;
     nblocks = std::min(nblocks, A.nwork);
+    if (reserve_sms > 0) {
+        const int occ = use_s ? occ_s : occ_g;
+        nblocks = std::min(nblocks, std::max(1, (nsm - reserve_sms) * occ));
+    }
     if (cudaMemsetAsync(A.counter, 0, sizeof(int), st) != cudaSuccess)
         return DGB_ERR_CUDA;
     return k2_launch(A, nblocks, smem, st, threads);
@@ -1006,6 +1014,23 @@ extern "C" int dgb_batch2d_integrate_ckpt(const int *masks, int ninst, const int
     return dgb::k2_batch(ninst, masks, Ls, ngrids, xx_all, phi0_all, phi_out, table, row_off,
                          row_cnt, settings->use_old_timestep ? 1 : 0, order, settings, ws,
                          ws_bytes, (cudaStream_t)stream, ckpt, ckpt_off, ckpt_every);
+}
+
+extern "C" int dgb_batch2d_integrate_ckpt_part(
+    const int *masks, int ninst, const int *Ls, int ngrids, const double *xx_all,
+    const double *phi0_all, double *phi_out, const double *table, const long *row_off,
+    const int *row_cnt, const int *order, int norder, int reserve_sms,
+    const dgb_settings *settings, double *ckpt, const long *ckpt_off, int ckpt_every, void *ws,
+    size_t ws_bytes, void *stream)
+{
+    if (!Ls || !xx_all || !phi0_all || !phi_out || !table || !row_off || !row_cnt || !order ||
+        !settings || !ckpt || !ckpt_off || ckpt_every < 1 || norder < 1 ||
+        norder > ninst * ngrids)
+        return DGB_ERR_ARG;
+    return dgb::k2_batch(ninst, masks, Ls, ngrids, xx_all, phi0_all, phi_out, table, row_off,
+                         row_cnt, settings->use_old_timestep ? 1 : 0, order, settings, ws,
+                         ws_bytes, (cudaStream_t)stream, ckpt, ckpt_off, ckpt_every, norder,
+                         reserve_sms);
 }
 
 extern "C" int dgb_items2d_integrate(const dgb_item2d *items, int nitems, int Lmax,

@@ -281,7 +281,7 @@ class Server:
                 _lib.check(lib.dgb_items2d_integrate_cluster(
                     _lib.dptr(d_items), len(items), Lmin, Lmax, _lib.dptr(d_xx),
                     _lib.dptr(w.d_phi), _lib.dptr(table), _lib.dptr(roff), _lib.dptr(cnt), 8,
-                    sh), "dgb_items2d_integrate_cluster")
+                    None, None, 0, sh), "dgb_items2d_integrate_cluster")
             else:
                 ws, nws = _lib.workspace(torch, lib.dgb_workspace_bytes(3, 2, Lmax, len(items)))
                 _lib.check(lib.dgb_items2d_integrate(

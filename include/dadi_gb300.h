@@ -245,6 +245,18 @@ int dgb_batch2d_integrate_ckpt(const int *masks, int ninst, const int *Ls, int n
                                const long *ckpt_off, int ckpt_every, void *ws, size_t ws_bytes,
                                void *stream);
 
+/* dgb_batch2d_integrate_ckpt over the work items order[0 .. norder) only,
+ * leaving reserve_sms SMs to other launches: the rest of a batch whose
+ * longest items run at the same time on clusters
+ * (dgb_items2d_integrate_cluster with checkpoints). */
+int dgb_batch2d_integrate_ckpt_part(const int *masks, int ninst, const int *Ls, int ngrids,
+                                    const double *xx_all, const double *phi0_all,
+                                    double *phi_out, const double *table, const long *row_off,
+                                    const int *row_cnt, const int *order, int norder,
+                                    int reserve_sms, const dgb_settings *settings, double *ckpt,
+                                    const long *ckpt_off, int ckpt_every, void *ws,
+                                    size_t ws_bytes, void *stream);
+
 /* Discrete adjoint of those integrations.  lam (device, phi_out layout) holds
  * dJ/dphi_final on entry and is overwritten; grad (device, ninst x ngrids x
  * DGB_AD_NPAR) receives each (instance, grid) work item's part of
@@ -329,12 +341,16 @@ int dgb_items2d_integrate(const dgb_item2d *items, int nitems, int Lmax, const d
  * item (the kernel of dgb_integrate2d_cluster): for a few items, which one
  * CTA each would leave bound by one SM's FP64 pipe.  Lmin / Lmax (host)
  * bound every item's L and must satisfy dgb_integrate2d_cluster's range
- * (else DGB_ERR_UNSUPPORTED); an item outside them is skipped.  Default
- * delta_j only; no order, settings or workspace.  Results agree with
+ * (else DGB_ERR_UNSUPPORTED); an item outside them is skipped.  With ckpt
+ * (device, optional) the density before every ckpt_every-th step is stored,
+ * row-major, from ckpt + ckpt_off[i] for item i (ckpt_off: device, nitems
+ * longs; the checkpoints of dgb_batch2d_integrate_ckpt).  Default delta_j
+ * only; no order, settings or workspace.  Results agree with
  * dgb_items2d_integrate to rounding. */
 int dgb_items2d_integrate_cluster(const dgb_item2d *items, int nitems, int Lmin, int Lmax,
                                   const double *xx_all, double *phi_out, const double *table,
                                   const long *row_off, const int *row_cnt, int cluster,
+                                  double *ckpt, const long *ckpt_off, int ckpt_every,
                                   void *stream);
 
 /* dgb_sched2d evaluated in C on the host (all arrays HOST): table == NULL

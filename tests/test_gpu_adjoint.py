@@ -152,3 +152,26 @@ def test_adjoint_hybrid_mode_is_bitwise(cuda_lib, golden):
     finally:
         eng.traj_budget = batch.Batch2D.traj_budget
     assert np.array_equal(g_seg.cpu().numpy(), g_hyb.cpu().numpy())
+
+
+def test_forward_of_few_items_on_clusters(cuda_lib, golden):
+    """The gradient's forward of a few integrations on thread-block clusters
+    (with checkpoints) gives the one-CTA forward's likelihoods to 1e-12 and
+    gradients to 1e-9 (the cluster's partitioned solves round
+    differently)."""
+    from dadi_gb300 import batch
+    draws = cases.im_draws(4096)
+    steps = batch.count_steps(batch.im_instances(draws))
+    sel = [i for i in range(64) if 30 <= steps[i] <= 1500][:4]
+    data = golden["grad"]["grad_data"]
+    eng = batch.Batch2D((30, 40, 50), NS)
+    eng.cluster_forward = False
+    ll0, g0, _ = eng.loglik_and_grad(draws[sel], data, scale=1e4)
+    eng.cluster_forward = True
+    eng._split_keep = None
+    ll1, g1, st = eng.loglik_and_grad(draws[sel], data, scale=1e4)
+    assert eng._split_keep is not None and int(st.abs().sum()) == 0
+    ll0, ll1 = ll0.cpu().numpy(), ll1.cpu().numpy()
+    assert np.max(np.abs(ll1 - ll0) / np.abs(ll0)) < 1e-12
+    g0, g1 = g0.cpu().numpy(), g1.cpu().numpy()
+    assert float(np.max(np.abs(g1 - g0)) / np.max(np.abs(g0))) < 1e-9

@@ -133,7 +133,8 @@ def test_items_on_clusters_match_one_cta_per_item(cuda_lib):
     out = torch.from_numpy(np.concatenate(phi0)).cuda()
     _lib.check(lib.dgb_items2d_integrate_cluster(_lib.dptr(d_items), 5, 40, 120, _lib.dptr(d_xx),
                                                  _lib.dptr(out), _lib.dptr(d_tab),
-                                                 _lib.dptr(d_roff), _lib.dptr(d_cnt), 8, sh),
+                                                 _lib.dptr(d_roff), _lib.dptr(d_cnt), 8,
+                                                 None, None, 0, sh),
                "dgb_items2d_integrate_cluster")
     ref, out = ref.cpu().numpy(), out.cpu().numpy()
     off = 0
