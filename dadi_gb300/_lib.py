@@ -164,7 +164,7 @@ def _declare(L):
                                    _vp, _vp, _vp, i, _vp, _vp, _vp, _vp, _vp, _vp,
                                    ctypes.POINTER(Settings), _vp, sz, _vp]),
         "dgb_adjoint2d_part": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp,
-                                   _vp, _vp, _vp, i, _vp, _vp, _vp, _vp, _vp, _vp, i, i,
+                                   _vp, _vp, _vp, i, _vp, _vp, _vp, _vp, _vp, _vp, i, i, i,
                                    ctypes.POINTER(Settings), _vp, sz, _vp]),
         "dgb_adjoint2d": (i, [_vp, i, ctypes.POINTER(ctypes.c_int), i, _vp, _vp, _vp, _vp, _vp,
                               _vp, _vp, i, _vp, _vp, _vp, ctypes.POINTER(Settings), _vp, sz,

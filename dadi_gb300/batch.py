@@ -600,9 +600,19 @@ class Batch2D:
         self._split_keep = (d_items, d_ckoff, d_rest)
 
     #: Largest trajectory (bytes) the adjoint stores so that every checkpoint
-    #: segment is recomputed at once (dgb_adjoint2d_traj); beyond it each
-    #: work item's CTA recomputes its segments in turn (dgb_adjoint2d).
-    traj_budget = 24 << 30
+    #: segment is recomputed at once (dgb_adjoint2d_traj); beyond it the
+    #: longest items that fit are walked from a stored trajectory and the
+    #: rest recompute their segments in turn (the hybrid).  256 sets at pts
+    #: 100/110/120: 7.13 s at 24 GB, 6.16 s at 48, 5.80 s at 64, 5.84 s at 80.
+    traj_budget = 64 << 30
+
+    def _traj_limit(self):
+        """traj_budget, but at most half the device memory free now (the
+        driver's free bytes plus what torch's allocator holds unused)."""
+        torch = self.torch
+        free, _ = torch.cuda.mem_get_info()
+        idle = torch.cuda.memory_reserved() - torch.cuda.memory_allocated()
+        return min(self.traj_budget, (free + idle) // 2)
 
     def trajectory_bytes(self, ctx):
         """Bytes of the adjoint's full trajectory for a forward context:
@@ -658,14 +668,15 @@ class Batch2D:
                   _lib.dptr(ctx["table"]), _lib.dptr(ctx["drows"]), _lib.dptr(ctx["off"]),
                   _lib.dptr(ctx["cnt"]), _lib.dptr(ctx["ckpt"]), _lib.dptr(ctx["ck_off"]), C)
         if trajectory is None:
-            if self.trajectory_bytes(ctx) <= self.traj_budget:
+            if self.trajectory_bytes(ctx) <= self._traj_limit():
                 trajectory = True
             else:
-                self._adjoint_hybrid(ctx, lam, part, common, nblocks, nsm, Lmax)
+                self._adjoint_hybrid(ctx, lam, part, common, nblocks, nsm, per_sm, Lmax)
                 trajectory = "hybrid"
         if trajectory == "hybrid":
             pass
         elif trajectory:
+            ctas = self._cluster_adjoint_ctas(ctx, nsm)
             steps = self._work_steps(ctx).reshape(-1)
             Lsq = np.tile(np.array([L * L for L in self.pts_l], dtype=np.int64), n)
             size = (2 * steps + 1) * Lsq
@@ -678,10 +689,17 @@ class Batch2D:
             d_soff = _lib.to_device(torch, seg_off, np.int64)
             ws, nws = _lib.workspace(torch, lib.dgb_adjoint2d_traj_ws_bytes(
                 Lmax, max(nblocks, 2 * nsm)))
-            _lib.check(lib.dgb_adjoint2d_traj(
-                *common, _lib.dptr(traj), _lib.dptr(d_toff), _lib.dptr(d_soff), _lib.dptr(lam),
-                _lib.dptr(part), _lib.dptr(ctx["order"]), ctypes.byref(st), _lib.dptr(ws), nws,
-                _lib.stream_handle(torch)), "dgb_adjoint2d_traj")
+            if ctas:
+                _lib.check(lib.dgb_adjoint2d_part(
+                    *common, _lib.dptr(traj), _lib.dptr(d_toff), _lib.dptr(d_soff),
+                    _lib.dptr(lam), _lib.dptr(part), _lib.dptr(ctx["order"]), n * ng, 0, ctas,
+                    ctypes.byref(st), _lib.dptr(ws), nws, _lib.stream_handle(torch)),
+                    "dgb_adjoint2d_part(cluster)")
+            else:
+                _lib.check(lib.dgb_adjoint2d_traj(
+                    *common, _lib.dptr(traj), _lib.dptr(d_toff), _lib.dptr(d_soff),
+                    _lib.dptr(lam), _lib.dptr(part), _lib.dptr(ctx["order"]), ctypes.byref(st),
+                    _lib.dptr(ws), nws, _lib.stream_handle(torch)), "dgb_adjoint2d_traj")
         else:
             per_cta = lib.dgb_adjoint2d_scratch_bytes(Lmax, C, 1)
             ws, nws = _lib.workspace(torch, 256 + per_cta * nblocks)
@@ -694,11 +712,39 @@ class Batch2D:
             grad += part[:, gi]
         return grad
 
-    def _adjoint_hybrid(self, ctx, lam, part, common, nblocks, nsm, Lmax):
+    #: CTAs of the thread-block cluster that walks each work item's adjoint
+    #: in trajectory mode when there are few items (2, 4, 8 or 16; 0: one
+    #: CTA per item always; see _cluster_adjoint_ctas).
+    cluster_adjoint = 8
+
+    def _cluster_adjoint_ctas(self, ctx, nsm):
+        """CTAs per work item of the trajectory-mode backward walk:
+        cluster_adjoint (a cluster per item, dgb_adjoint2d_part) when every
+        item can have its cluster at once and every grid has 3-16 rows per
+        CTA within 24-128 points, else 0 (one CTA per item).  A single
+        item's walk on one CTA is bound by one SM's FP64 pipe."""
+        c = self.cluster_adjoint
+        if not c or ctx["st"].use_delj_trick:
+            return 0
+        if not all(max(24, 3 * c) <= L <= min(128, 16 * c) for L in self.pts_l):
+            return 0
+        return c if ctx["n"] * len(self.pts_l) * c <= nsm else 0
+
+    #: In the hybrid adjoint, walk the longest (at most this many)
+    #: trajectory-mode items on clusters of cluster_adjoint CTAs, within a
+    #: quarter of the SMs (0: none).  Off by default: the hybrid's bound is
+    #: the segment-mode walk of the other items, which the clusters' SMs
+    #: slow (256 sets at pts 100/110/120: 5.81 s with none, 6.32 s with 2,
+    #: 7.15 s with 4).
+    hybrid_cluster_items = 0
+
+    def _adjoint_hybrid(self, ctx, lam, part, common, nblocks, nsm, per_sm, Lmax):
         """The longest work items (while their trajectory fits traj_budget)
-        in trajectory mode on the current stream, one CTA each, and the rest
-        with per-CTA segment recomputation on a side stream on the other
-        CTAs (dgb_adjoint2d_part twice)."""
+        in trajectory mode -- the longest hybrid_cluster_items of them on
+        clusters on the current stream, the others one CTA each on a side
+        stream -- and the rest with per-CTA segment recomputation on another
+        side stream on the remaining CTAs (dgb_adjoint2d_part up to three
+        times, each trajectory call recomputing its own items' segments)."""
         torch = self.torch
         lib = _lib.lib()
         n, ng, C, st = ctx["n"], len(self.pts_l), ctx["C"], ctx["st"]
@@ -706,39 +752,66 @@ class Batch2D:
         Lsq = np.tile(np.array([L * L for L in self.pts_l], dtype=np.int64), n)
         order = np.argsort(-(steps * Lsq), kind="stable").astype(np.int32)
         size = (2 * steps + 1) * Lsq * 8
-        k = int(np.searchsorted(np.cumsum(size[order]), self.traj_budget, side="right"))
+        k = int(np.searchsorted(np.cumsum(size[order]), self._traj_limit(), side="right"))
         k = max(1, min(k, len(order) - 1))
+        c = self.cluster_adjoint
+        if not c or not all(max(24, 3 * c) <= L <= min(128, 16 * c) for L in self.pts_l):
+            c = 0
+        j = min(k, self.hybrid_cluster_items, nsm // (4 * c)) if c else 0
         tset = order[:k]
         t_off = np.zeros(n * ng, dtype=np.int64)
         t_off[tset] = np.concatenate([[0], np.cumsum(size[tset] // 8)[:-1]])
-        nseg = np.zeros(n * ng, dtype=np.int64)
-        nseg[tset] = (steps[tset] + C - 1) // C
-        seg_off = np.zeros(n * ng + 1, dtype=np.int64)
-        np.cumsum(nseg, out=seg_off[1:])
         traj = torch.empty(max(int(size[tset].sum() // 8), 1), dtype=torch.float64,
                            device="cuda")
         d_toff = _lib.to_device(torch, t_off, np.int64)
-        d_soff = _lib.to_device(torch, seg_off, np.int64)
         d_order = _lib.to_device(torch, order, np.int32)
-        ws_t, nws_t = _lib.workspace(torch, lib.dgb_adjoint2d_traj_ws_bytes(Lmax, 2 * nsm))
-        rest = max(1, nblocks - k)
+        keep = [traj, d_toff, d_order]
+        # (first, count, CTAs, cluster) of each trajectory-mode call
+        calls = [(0, j, j, c), (j, k - j, k - j, 0)]
+        # the segment-mode walk on the SMs left, but never fewer than a
+        # quarter of the device's CTAs
+        rest = min(len(order) - k, max(nsm * per_sm // 4, (nsm - j * c) * per_sm - (k - j)))
         ws_s, nws_s = _lib.workspace(torch, 256 + lib.dgb_adjoint2d_scratch_bytes(Lmax, C, 1)
                                      * rest)
+        keep.append(ws_s)
+        # every upload on the current stream before the side streams wait on it
+        args = []
+        for first, cnt, ctas, cl in calls:
+            if cnt < 1:
+                args.append(None)
+                continue
+            nseg = np.zeros(n * ng, dtype=np.int64)
+            ids = order[first:first + cnt]
+            nseg[ids] = (steps[ids] + C - 1) // C
+            seg_off = np.zeros(n * ng + 1, dtype=np.int64)
+            np.cumsum(nseg, out=seg_off[1:])
+            d_soff = _lib.to_device(torch, seg_off, np.int64)
+            ws_t, nws_t = _lib.workspace(torch, lib.dgb_adjoint2d_traj_ws_bytes(Lmax, 2 * nsm))
+            keep += [d_soff, ws_t]
+            args.append((d_soff, ws_t, nws_t))
         main = torch.cuda.current_stream()
-        side = torch.cuda.Stream()
-        side.wait_stream(main)
-        _lib.check(lib.dgb_adjoint2d_part(
-            *common, _lib.dptr(traj), _lib.dptr(d_toff), _lib.dptr(d_soff), _lib.dptr(lam),
-            _lib.dptr(part), _lib.dptr(d_order), k, k, ctypes.byref(st), _lib.dptr(ws_t), nws_t,
-            _lib.stream_handle(torch)), "dgb_adjoint2d_part(trajectory)")
-        with torch.cuda.stream(side):
+        sides = [torch.cuda.Stream(), torch.cuda.Stream()]
+        for sd in sides:
+            sd.wait_stream(main)
+        for (first, cnt, ctas, cl), a, strm in zip(calls, args, (main, sides[0])):
+            if a is None:
+                continue
+            d_soff, ws_t, nws_t = a
+            with torch.cuda.stream(strm):
+                _lib.check(lib.dgb_adjoint2d_part(
+                    *common, _lib.dptr(traj), _lib.dptr(d_toff), _lib.dptr(d_soff),
+                    _lib.dptr(lam), _lib.dptr(part), _lib.dptr(d_order[first:]), cnt, ctas, cl,
+                    ctypes.byref(st), _lib.dptr(ws_t), nws_t, _lib.stream_handle(torch)),
+                    "dgb_adjoint2d_part(trajectory)")
+        with torch.cuda.stream(sides[1]):
             _lib.check(lib.dgb_adjoint2d_part(
                 *common, None, None, None, _lib.dptr(lam), _lib.dptr(part),
-                _lib.dptr(d_order[k:]), len(order) - k, rest, ctypes.byref(st),
+                _lib.dptr(d_order[k:]), len(order) - k, rest, 0, ctypes.byref(st),
                 _lib.dptr(ws_s), nws_s, _lib.stream_handle(torch)), "dgb_adjoint2d_part")
-        main.wait_stream(side)
-        for t in (traj, d_toff, d_soff, d_order, ws_t, ws_s):
-            t.record_stream(side)
+        for sd in sides:
+            main.wait_stream(sd)
+            for t in keep:
+                t.record_stream(sd)
 
     def spectra(self, phis):
         """Per-grid raw spectra (n, n1+1, n2+1) on the device."""

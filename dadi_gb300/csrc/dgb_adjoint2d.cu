@@ -27,6 +27,9 @@
 // slices), so any grid size runs.
 #include <algorithm>
 
+#include <cooperative_groups.h>
+
+#include "dgb_cluster.cuh"
 #include "dgb_common.cuh"
 #include "dgb_internal.h"
 
@@ -807,14 +810,289 @@ extern "C" size_t dgb_adjoint2d_scratch_bytes(int Lmax, int ckpt_every, int nblo
     return (size_t)nblocks * (2 * ckpt_every + 3) * Lmax * Lmax * sizeof(double);
 }
 
+namespace dgb {
+
+// The backward walk of one work item on a thread-block cluster (trajectory
+// mode: phi_k and chi_k read from the stored trajectory): the transposed
+// solves of k_adjoint2d partitioned as k_integrate2d_cluster partitions the
+// forward (c2_sweep_x / c2_sweep_y with the transposed vectors), CTA r
+// holding rows R0 .. R0+m-1 of the adjoint.  The contraction of each sweep
+// is split over the threads that hold the points: its sums run over points
+// and over the intervals (i, i+1) whose lower point a thread holds, so they
+// add up; an interval across two CTAs' row blocks reads the next CTA's first
+// adjoint row (exported after the x solve).  Per-CTA partial gradients are
+// summed through distributed shared memory.  Cluster b walks order[b].
+constexpr int AC_THREADS = C2_THREADS;
+
+__host__ __device__ inline size_t adc_smem_doubles(int L)
+{
+    return (size_t)AD_VEC_DOUBLES * L + (size_t)C2_ROWS * c2_pitch(L) +
+           2 * (size_t)C2_ROWS * L + (size_t)C2_XROW * L + 3 * (size_t)L +
+           (size_t)C2_YSLOT * C2_YSEG * C2_ROWS + NPAR;
+}
+
+__global__ void __launch_bounds__(AC_THREADS) k_adjoint2d_cluster(ADArgs A)
+{
+    extern __shared__ __align__(16) double smem[];
+    __shared__ ADShared S;
+    __shared__ double red[AC_THREADS / 32][NPAR];
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int NS = (int)cluster.num_blocks();
+    const int rank = (int)cluster.block_rank();
+    const int tid = threadIdx.x;
+    const int w = blockIdx.x / NS;
+    if (w >= A.nwork)
+        return; // the whole cluster
+    const int wid = A.order[w];
+    const int inst = wid / A.ngrids;
+    const int gi = wid - inst * A.ngrids;
+    const int L = A.L[gi];
+    const size_t LL = (size_t)L * L;
+    const int pitch = c2_pitch(L);
+    int R0, m;
+    c2_rows(L, NS, rank, &R0, &m);
+    GridVecs g;
+    ADVecs V;
+    ad_carve(smem, L, g, V);
+    double *blk = smem + (size_t)AD_VEC_DOUBLES * L; // this CTA's rows of lambda
+    double *al = blk + (size_t)C2_ROWS * pitch;
+    double *ga = al + (size_t)C2_ROWS * L;
+    double *xr = ga + (size_t)C2_ROWS * L;
+    double *zin = xr + (size_t)C2_XROW * L;
+    double *hx = zin + 2 * (size_t)L;                // exported first row of lambda
+    double *yr = hx + L;
+    double *part = yr + (size_t)C2_YSLOT * C2_YSEG * C2_ROWS; // this CTA's gradient
+
+    const double *xx = A.xx_all + A.xx_off[gi];
+    double *lam_g = A.lam + A.out_off[gi] + (size_t)inst * LL;
+    const int sidx = A.sched_per_grid ? wid : inst;
+    const double *rows = A.table + A.row_off[sidx] * 11;
+    const double *drows = A.drows + A.row_off[sidx] * NQ * NPAR;
+    const int n = A.row_cnt[sidx];
+    const int frozen = A.masks ? (A.masks[inst] & 0xff) : 0;
+    const int nomut = A.masks ? (A.masks[inst] >> 8 & 0xff) : 0;
+    const bool injx = !(frozen & 1) && !(nomut & 1), injy = !(frozen & 2) && !(nomut & 2);
+    const double *tphi = A.traj + A.traj_off[wid];
+    const double *tchi = tphi + (size_t)(n + 1) * LL;
+
+    for (int i = tid; i < L; i += AC_THREADS) {
+        const double x = xx[i];
+        g.x[i] = x;
+        g.xv[i] = x * (1. - x);
+        if (i < L - 1) {
+            const double d = xx[i + 1] - x;
+            g.dx[i] = d;
+            g.ih[i] = 1.0 / (2 * d);
+            g.xInt[i] = 0.5 * (xx[i + 1] + x);
+        }
+    }
+    for (int idx = tid; idx < m * L; idx += AC_THREADS) {
+        const int p = idx / L, c = idx - p * L;
+        blk[p * pitch + c] = lam_g[(size_t)(R0 + p) * L + c];
+    }
+    __syncthreads();
+    for (int i = tid; i < L; i += AC_THREADS)
+        g.dfac[i] = (i == 0)       ? 2. / g.dx[0]
+                    : (i == L - 1) ? 2. / g.dx[L - 2]
+                                   : 2. / (g.dx[i] + g.dx[i - 1]);
+    __syncthreads();
+    const int j0 = (g.x[0] == 0.0) ? 0 : -1;
+    const int j1 = (g.x[L - 1] == 1.0) ? L - 1 : -1;
+    double acc[NPAR];
+#pragma unroll
+    for (int p = 0; p < NPAR; p++)
+        acc[p] = 0;
+
+    for (int k = n - 1; k >= 0; k--) {
+        ad_step_setup(S, V, g, L, rows + (size_t)k * 11, drows + (size_t)k * NQ * NPAR, true);
+        const double *phin = tphi + (size_t)(k + 1) * LL; // Y^{-1} chi_k
+        const double *chi = tchi + (size_t)k * LL;        // X^{-1} psi_k
+        const double *phik = tphi + (size_t)k * LL;       // psi_k - injection
+        double G[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; q++)
+            G[q] = 0;
+        // ---- y: mu = Y^{-T} lambda on the CTA's rows, contracted with
+        // phi_{k+1} (the sweep's output) and chi_k (its input)
+        if (!(frozen & 2)) {
+            c2_sweep_y(blk, pitch, L, R0, m, al, ga, yr, V.t[1], S.ax[1], g, j0, j1);
+            const int p = tid % C2_ROWS, q = tid / C2_ROWS;
+            if (p < m) {
+                const int mlen = L / C2_YSEG, extra = L % C2_YSEG;
+                const int s0 = q * mlen + min(q, extra);
+                const int e0 = s0 + mlen + (q < extra ? 1 : 0); // points [s0, e0)
+                const int line = R0 + p;
+                const AxisScalars &s = S.ax[1];
+                const ADCVecs &cv = V.c[1];
+                const double *mr = blk + (size_t)p * pitch;
+                const double *pr = phin + (size_t)line * L, *rr = chi + (size_t)line * L;
+                const double o = g.x[line], inu = s.inv_nu, dt = s.dt;
+                double smr = 0, smp = 0, snu = 0, sm = 0, sg = 0, sh = 0;
+                double mi = mr[s0], pi = pr[s0];
+                for (int i = s0; i < e0; i++) {
+                    smr = fma(mi, rr[i], smr);
+                    smp = fma(mi, pi, smp);
+                    if (i < L - 1) {
+                        const double mn = mr[i + 1], pn = pr[i + 1];
+                        const double Di = g.dfac[i] * mi - g.dfac[i + 1] * mn;
+                        const double hp = 0.5 * (pi + pn);
+                        snu = fma(Di, (cv.Q[i] * pn - cv.P[i] * pi) * inu, snu);
+                        sm = fma(Di * (o - g.xInt[i]), hp, sm);
+                        sg = fma(Di * cv.FG[i], hp, sg);
+                        sh = fma(Di * cv.FH[i], hp, sh);
+                        mi = mn;
+                        pi = pn;
+                    }
+                }
+                double bnu = 0, bm = 0, bg = 0, bh = 0;
+                const double hh = s.h, gam = s.gamma;
+                if (s0 == 0 && line == j0 && s.bcs != 0.0) {
+                    const double x0 = g.x[0], f = dt * 2. / g.dx[0], w0 = mr[0] * pr[0];
+                    bnu += w0 * f * (-0.5 * inu * inu);
+                    bm += w0 * f * x0;
+                    bg -= w0 * f * (2 * (hh + (1. - 2 * hh) * x0) * x0 * (1. - x0));
+                    bh -= w0 * f * (gam * 2 * (1. - 2 * x0) * x0 * (1. - x0));
+                }
+                if (e0 == L && line == j1 && s.bce != 0.0) {
+                    const double xl = g.x[L - 1], f = dt * 2. / g.dx[L - 2];
+                    const double w1 = mr[L - 1] * pr[L - 1];
+                    bnu += w1 * f * (-0.5 * inu * inu);
+                    bm += w1 * f * (1. - xl);
+                    bg += w1 * f * (2 * (hh + (1. - 2 * hh) * xl) * xl * (1. - xl));
+                    bh += w1 * f * (gam * 2 * (1. - 2 * xl) * xl * (1. - xl));
+                }
+                G[Q_DT] -= (smr - smp) / dt;
+                G[Q_NU1] -= dt * snu + bnu;
+                G[Q_M10] -= dt * sm + bm;
+                G[Q_G1] -= dt * sg + bg;
+                G[Q_H1] -= dt * sh + bh;
+            }
+            __syncthreads();
+        }
+        // ---- x: nu = X^{-T} mu across the cluster, contracted with chi_k
+        // (the sweep's output) and psi_k (its input)
+        if (!(frozen & 1)) {
+            c2_sweep_x(cluster, NS, rank, blk, pitch, L, R0, m, al, ga, xr, zin, V.t[0],
+                       S.ax[0], g, j0, j1);
+            for (int j = tid; j < L; j += AC_THREADS)
+                hx[j] = blk[j];
+            cluster.sync();
+            const int j = tid;
+            if (j < L) {
+                // nu at row R0 + m, the next CTA's first row
+                const double mnext =
+                    (rank + 1 < NS) ? cluster.map_shared_rank(hx, rank + 1)[j] : 0.0;
+                const AxisScalars &s = S.ax[0];
+                const ADCVecs &cv = V.c[0];
+                const double o = g.x[j], inu = s.inv_nu, dt = s.dt;
+                double smr = 0, smp = 0, snu = 0, sm = 0, sg = 0, sh = 0;
+                double mi = blk[j], pi = chi[(size_t)R0 * L + j];
+                for (int p = 0; p < m; p++) {
+                    const int i = R0 + p;
+                    double ri = phik[(size_t)i * L + j];
+                    if (i == 1 && j == 0 && injx)
+                        ri += S.inj;
+                    if (i == 0 && j == 1 && injy)
+                        ri += S.inj;
+                    smr = fma(mi, ri, smr);
+                    smp = fma(mi, pi, smp);
+                    if (i < L - 1) {
+                        const double mn = (p + 1 < m) ? blk[(p + 1) * pitch + j] : mnext;
+                        const double pn = chi[(size_t)(i + 1) * L + j];
+                        const double Di = g.dfac[i] * mi - g.dfac[i + 1] * mn;
+                        const double hp = 0.5 * (pi + pn);
+                        snu = fma(Di, (cv.Q[i] * pn - cv.P[i] * pi) * inu, snu);
+                        sm = fma(Di * (o - g.xInt[i]), hp, sm);
+                        sg = fma(Di * cv.FG[i], hp, sg);
+                        sh = fma(Di * cv.FH[i], hp, sh);
+                        mi = mn;
+                        pi = pn;
+                    }
+                }
+                double bnu = 0, bm = 0, bg = 0, bh = 0;
+                const double hh = s.h, gam = s.gamma;
+                if (R0 == 0 && j == j0 && s.bcs != 0.0) {
+                    const double x0 = g.x[0], f = dt * 2. / g.dx[0], w0 = blk[j] * chi[j];
+                    bnu += w0 * f * (-0.5 * inu * inu);
+                    bm += w0 * f * x0;
+                    bg -= w0 * f * (2 * (hh + (1. - 2 * hh) * x0) * x0 * (1. - x0));
+                    bh -= w0 * f * (gam * 2 * (1. - 2 * x0) * x0 * (1. - x0));
+                }
+                if (R0 + m == L && j == j1 && s.bce != 0.0) {
+                    const double xl = g.x[L - 1], f = dt * 2. / g.dx[L - 2];
+                    const double w1 = blk[(m - 1) * pitch + j] * chi[(size_t)(L - 1) * L + j];
+                    bnu += w1 * f * (-0.5 * inu * inu);
+                    bm += w1 * f * (1. - xl);
+                    bg += w1 * f * (2 * (hh + (1. - 2 * hh) * xl) * xl * (1. - xl));
+                    bh += w1 * f * (gam * 2 * (1. - 2 * xl) * xl * (1. - xl));
+                }
+                G[Q_DT] -= (smr - smp) / dt;
+                G[Q_NU0] -= dt * snu + bnu;
+                G[Q_M01] -= dt * sm + bm;
+                G[Q_G0] -= dt * sg + bg;
+                G[Q_H0] -= dt * sh + bh;
+            }
+        }
+        // injection: d psi(1,0), psi(0,1) / d(dt, theta0), rows 0 and 1 of
+        // the first CTA
+        if (rank == 0 && tid == 0) {
+            const double lin = (injx ? blk[1 * pitch + 0] : 0.0) + (injy ? blk[0 * pitch + 1] : 0.0);
+            G[Q_DT] += lin * S.dinj_dt;
+            G[Q_TH] += lin * S.dinj_th;
+        }
+#pragma unroll
+        for (int p = 0; p < NPAR; p++) {
+            double sacc = acc[p];
+#pragma unroll
+            for (int q = 0; q < NQ; q++)
+                sacc = fma(G[q], S.D[q * NPAR + p], sacc);
+            acc[p] = sacc;
+        }
+        __syncthreads();
+    }
+    for (int idx = tid; idx < m * L; idx += AC_THREADS) {
+        const int p = idx / L, c = idx - p * L;
+        lam_g[(size_t)(R0 + p) * L + c] = blk[p * pitch + c];
+    }
+#pragma unroll
+    for (int p = 0; p < NPAR; p++) {
+        double v = acc[p];
+        for (int off = 16; off > 0; off >>= 1)
+            v += __shfl_down_sync(0xffffffffu, v, off);
+        if ((tid & 31) == 0)
+            red[tid >> 5][p] = v;
+    }
+    __syncthreads();
+    if (tid < NPAR) {
+        double v = 0;
+        for (int wv = 0; wv < AC_THREADS / 32; wv++)
+            v += red[wv][tid];
+        part[tid] = v;
+    }
+    cluster.sync();
+    if (rank == 0 && tid < NPAR) {
+        double v = 0;
+        for (int q = 0; q < NS; q++)
+            v += cluster.map_shared_rank(part, q)[tid];
+        A.grad[((size_t)inst * A.ngrids + gi) * NPAR + tid] = v;
+    }
+    // no CTA may leave while the first still reads its partial gradient
+    cluster.sync();
+}
+
+} // namespace dgb
+
 // norder: the work items of `order` to walk (<= 0: all ninst x ngrids);
 // max_blocks: most CTAs of the backward walk (<= 0: as many as the workspace
-// and the items allow).
+// and the items allow); cluster: in trajectory mode, walk each item on a
+// thread-block cluster of that many CTAs (k_adjoint2d_cluster; 0: one CTA
+// per item).
 static int adjoint2d_run(const int *masks, int ninst, const int *Ls, int ngrids,
                          const double *xx_all, const double *table, const double *drows,
                          const long *row_off, const int *row_cnt, const double *ckpt,
                          const long *ckpt_off, int ckpt_every, double *lam, double *grad,
-                         const int *order, int norder, int max_blocks,
+                         const int *order, int norder, int max_blocks, int cluster,
                          const dgb_settings *settings, double *traj, const long *traj_off,
                          const long *seg_off, void *ws, size_t ws_bytes, void *stream)
 {
@@ -825,6 +1103,15 @@ static int adjoint2d_run(const int *masks, int ninst, const int *Ls, int ngrids,
         return DGB_ERR_ARG;
     if (settings->use_delj_trick)
         return DGB_ERR_UNSUPPORTED;
+    if (cluster) {
+        // every grid within the partitioned sweeps' range, in trajectory mode
+        if (!traj || (cluster != 2 && cluster != 4 && cluster != 8 && cluster != 16))
+            return DGB_ERR_ARG;
+        for (int gi = 0; gi < ngrids; gi++)
+            if (Ls[gi] < 3 * C2_YSEG || Ls[gi] > C2_THREADS || Ls[gi] < 3 * cluster ||
+                Ls[gi] > C2_ROWS * cluster)
+                return DGB_ERR_UNSUPPORTED;
+    }
     ADArgs A = {};
     A.ngrids = ngrids;
     long xo = 0, oo = 0;
@@ -905,6 +1192,35 @@ static int adjoint2d_run(const int *masks, int ninst, const int *Ls, int ngrids,
     if (cudaMemsetAsync(A.counter, 0, sizeof(int), (cudaStream_t)stream) != cudaSuccess)
         return DGB_ERR_CUDA;
     A.nwork = nwalk;
+    if (traj && cluster > 0) {
+        const size_t csmem =
+            std::max(adc_smem_doubles(Lmax) * sizeof(double), (size_t)116 << 10);
+        if (raise_smem_limit(k_adjoint2d_cluster))
+            return DGB_ERR_CUDA;
+        if (cluster > 8 && cudaFuncSetAttribute(k_adjoint2d_cluster,
+                                                cudaFuncAttributeNonPortableClusterSizeAllowed,
+                                                1) != cudaSuccess) {
+            cudaGetLastError();
+            return DGB_ERR_UNSUPPORTED;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)(cluster * nwalk), 1, 1);
+        cfg.blockDim = dim3(AC_THREADS, 1, 1);
+        cfg.dynamicSmemBytes = csmem;
+        cfg.stream = (cudaStream_t)stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)cluster;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        if (cudaLaunchKernelEx(&cfg, k_adjoint2d_cluster, A) != cudaSuccess) {
+            cudaGetLastError();
+            return DGB_ERR_CUDA;
+        }
+        return DGB_OK;
+    }
     if (traj)
         k_adjoint2d<true><<<(unsigned)nblocks, AD_THREADS, smem, (cudaStream_t)stream>>>(A);
     else
@@ -920,7 +1236,7 @@ extern "C" int dgb_adjoint2d(const int *masks, int ninst, const int *Ls, int ngr
                              size_t ws_bytes, void *stream)
 {
     return adjoint2d_run(masks, ninst, Ls, ngrids, xx_all, table, drows, row_off, row_cnt, ckpt,
-                         ckpt_off, ckpt_every, lam, grad, order, 0, 0, settings, nullptr,
+                         ckpt_off, ckpt_every, lam, grad, order, 0, 0, 0, settings, nullptr,
                          nullptr, nullptr, ws, ws_bytes, stream);
 }
 
@@ -941,8 +1257,8 @@ extern "C" int dgb_adjoint2d_traj(const int *masks, int ninst, const int *Ls, in
     if (!traj || !traj_off || !seg_off)
         return DGB_ERR_ARG;
     return adjoint2d_run(masks, ninst, Ls, ngrids, xx_all, table, drows, row_off, row_cnt, ckpt,
-                         ckpt_off, ckpt_every, lam, grad, order, 0, 0, settings, traj, traj_off,
-                         seg_off, ws, ws_bytes, stream);
+                         ckpt_off, ckpt_every, lam, grad, order, 0, 0, 0, settings, traj,
+                         traj_off, seg_off, ws, ws_bytes, stream);
 }
 
 extern "C" int dgb_adjoint2d_part(const int *masks, int ninst, const int *Ls, int ngrids,
@@ -951,20 +1267,20 @@ extern "C" int dgb_adjoint2d_part(const int *masks, int ninst, const int *Ls, in
                                   const double *ckpt, const long *ckpt_off, int ckpt_every,
                                   double *traj, const long *traj_off, const long *seg_off,
                                   double *lam, double *grad, const int *order, int norder,
-                                  int max_blocks, const dgb_settings *settings, void *ws,
-                                  size_t ws_bytes, void *stream)
+                                  int max_blocks, int cluster, const dgb_settings *settings,
+                                  void *ws, size_t ws_bytes, void *stream)
 {
     if (norder < 1 || (traj && (!traj_off || !seg_off)))
         return DGB_ERR_ARG;
     return adjoint2d_run(masks, ninst, Ls, ngrids, xx_all, table, drows, row_off, row_cnt, ckpt,
-                         ckpt_off, ckpt_every, lam, grad, order, norder, max_blocks, settings,
-                         traj, traj_off, seg_off, ws, ws_bytes, stream);
+                         ckpt_off, ckpt_every, lam, grad, order, norder, max_blocks, cluster,
+                         settings, traj, traj_off, seg_off, ws, ws_bytes, stream);
 }
 
 namespace dgb {
 int preload_adjoint2d()
 {
     return preload(k_sched2d_dual) + preload(k_adjoint2d<false>) + preload(k_adjoint2d<true>) +
-           preload(k_adjoint2d_traj);
+           preload(k_adjoint2d_traj) + preload(k_adjoint2d_cluster);
 }
 } // namespace dgb

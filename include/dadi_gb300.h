@@ -300,13 +300,19 @@ int dgb_adjoint2d_traj(const int *masks, int ninst, const int *Ls, int ngrids,
  * seg_off over all ninst * ngrids work ids, zero segments for the others)
  * and the rest with per-CTA segment recomputation (traj null: ws as for
  * dgb_adjoint2d).  Each item's lambda and gradient part are those of the
- * whole-batch calls, bit for bit. */
+ * whole-batch calls, bit for bit.  cluster (trajectory mode only): walk
+ * each item on a thread-block cluster of that many CTAs (2, 4, 8, 16), the
+ * transposed solves partitioned across them as dgb_integrate2d_cluster
+ * partitions the forward -- for a few long items, whose walk on one CTA is
+ * bound by one SM's FP64 pipe; every grid within that function's range (else
+ * DGB_ERR_UNSUPPORTED); lambda and gradients then agree with the one-CTA
+ * walk to rounding. */
 int dgb_adjoint2d_part(const int *masks, int ninst, const int *Ls, int ngrids,
                        const double *xx_all, const double *table, const double *drows,
                        const long *row_off, const int *row_cnt, const double *ckpt,
                        const long *ckpt_off, int ckpt_every, double *traj,
                        const long *traj_off, const long *seg_off, double *lam, double *grad,
-                       const int *order, int norder, int max_blocks,
+                       const int *order, int norder, int max_blocks, int cluster,
                        const dgb_settings *settings, void *ws, size_t ws_bytes, void *stream);
 
 /* One work item of dgb_items2d_integrate: a 2-D integration on grid

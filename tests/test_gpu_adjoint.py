@@ -124,6 +124,7 @@ def test_adjoint_trajectory_mode_is_bitwise(cuda_lib, golden):
     sel = [i for i in range(64) if 30 <= steps[i] <= 1500][:5]
     data = golden["grad"]["grad_data"]
     eng = _engine()
+    eng.cluster_adjoint = 0
     for C in (None, 7):
         _, g_seg, _ = eng.loglik_and_grad(draws[sel], data, scale=1e4, ckpt_every=C,
                                           trajectory=False)
@@ -166,6 +167,7 @@ def test_forward_of_few_items_on_clusters(cuda_lib, golden):
     data = golden["grad"]["grad_data"]
     eng = batch.Batch2D((30, 40, 50), NS)
     eng.cluster_forward = False
+    eng.cluster_adjoint = 0
     ll0, g0, _ = eng.loglik_and_grad(draws[sel], data, scale=1e4)
     eng.cluster_forward = True
     eng._split_keep = None
@@ -175,3 +177,59 @@ def test_forward_of_few_items_on_clusters(cuda_lib, golden):
     assert np.max(np.abs(ll1 - ll0) / np.abs(ll0)) < 1e-12
     g0, g1 = g0.cpu().numpy(), g1.cpu().numpy()
     assert float(np.max(np.abs(g1 - g0)) / np.max(np.abs(g0))) < 1e-9
+
+
+@pytest.mark.parametrize("pts,ctas", [((30,), 2), ((30, 40, 50), 4), ((30, 40, 50), 8),
+                                      ((50, 60), 16)])
+def test_adjoint_on_clusters_matches_one_cta(cuda_lib, golden, pts, ctas):
+    """The trajectory-mode backward walk on thread-block clusters of 2-16
+    CTAs (dgb_adjoint2d_part with a cluster size) against the one-CTA walk
+    on the same forward: gradients within 1e-10 (max-norm relative; the
+    partitioned solves and the split contraction sums round differently),
+    also with a frozen or a mutation-free population (the masks set on the
+    context, the same for both walks)."""
+    import torch
+    from dadi_gb300 import batch
+    draws = cases.im_draws(4096)
+    steps = batch.count_steps(batch.im_instances(draws))
+    sel = [i for i in range(64) if 30 <= steps[i] <= 1500][:2]
+    data = golden["grad"]["grad_data"]
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    eng = batch.Batch2D(pts, NS)
+    eng.cluster_forward = False
+    for mask in (0, 1, 2, 1 << 8, 2 << 8):
+        out = []
+        for c in (0, ctas):
+            eng.cluster_adjoint = c
+            ll, ctx = eng.forward_for_adjoint(draws[sel], data, scale=1e4, ckpt_every=7)
+            ctx["masks"].fill_(mask)
+            assert eng._cluster_adjoint_ctas(ctx, nsm) == c
+            out.append(eng.adjoint(ctx, torch.ones_like(ll), trajectory=True).cpu().numpy())
+        assert np.all(np.isfinite(out[1]))
+        assert _close(out[1], out[0]) < 1e-10, (mask, _close(out[1], out[0]))
+
+
+def test_hybrid_adjoint_with_clusters(cuda_lib, golden):
+    """The hybrid adjoint with its longest trajectory-mode items walked on
+    clusters of 8 CTAs, the other trajectory items on one CTA each and the
+    rest in segment mode, on three streams: the segment-mode gradients
+    within 1e-10."""
+    from dadi_gb300 import batch
+    draws = cases.im_draws(4096)
+    steps = batch.count_steps(batch.im_instances(draws))
+    sel = [i for i in range(64) if 30 <= steps[i] <= 1500][:6]
+    data = golden["grad"]["grad_data"]
+    eng = batch.Batch2D((30, 40, 50), NS)
+    eng.cluster_forward = False
+    eng.hybrid_cluster_items = 4
+    _, g_seg, _ = eng.loglik_and_grad(draws[sel], data, scale=1e4, ckpt_every=7,
+                                      trajectory=False)
+    ll, ctx = eng.forward_for_adjoint(draws[sel], data, scale=1e4, ckpt_every=7)
+    eng.traj_budget = eng.trajectory_bytes(ctx) // 3
+    try:
+        _, g_hyb, st = eng.loglik_and_grad(draws[sel], data, scale=1e4, ckpt_every=7)
+    finally:
+        eng.traj_budget = batch.Batch2D.traj_budget
+    g_seg, g_hyb = g_seg.cpu().numpy(), g_hyb.cpu().numpy()
+    assert int(st.abs().sum()) == 0 and np.all(np.isfinite(g_hyb))
+    assert _close(g_hyb, g_seg) < 1e-10
