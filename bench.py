@@ -624,6 +624,29 @@ def run_adjoint(a, obs):
                     "gradients_per_s": 256 / (fwd + adj),
                     "failed_instances": int((ctx["status"] != 0).sum()),
                     "finite": bool(torch.isfinite(grad).all())}}
+    del ll, ctx, grad
+    # one gradient request: the longest of the first 4096 seed-0 draws
+    # (19,546 steps), each grid's forward and backward walk on a cluster of 8
+    # CTAs (the default for a few items), then on one CTA per grid
+    d4 = im_draws(NINST, 0)
+    i = int(np.argmax(batch.count_steps(batch.im_instances(d4))))
+    single = {}
+    for name, cf, ca in (("clusters", True, 8), ("one_cta", False, 0)):
+        eng.cluster_forward, eng.cluster_adjoint = cf, ca
+        e0.record()
+        ll, ctx = eng.forward_for_adjoint(d4[i:i + 1], d_obs, scale=5e4)
+        e1.record()
+        g1 = eng.adjoint(ctx, torch.ones_like(ll))
+        e2.record()
+        torch.cuda.synchronize()
+        single[name] = {"forward_s": e0.elapsed_time(e1) / 1e3,
+                        "adjoint_s": e1.elapsed_time(e2) / 1e3,
+                        "finite": bool(torch.isfinite(g1).all())}
+        del ll, ctx
+    eng.cluster_forward, eng.cluster_adjoint = batch.Batch2D.cluster_forward, \
+        batch.Batch2D.cluster_adjoint
+    single["steps"] = int(batch.count_steps(batch.im_instances(d4[i:i + 1]))[0])
+    out["im2d"]["single_request"] = single
     # three populations: 32 sets of the growth model's parameters, each
     # scaled by exp(U(log .5, log 2)) (seed 0), at pts 80, ns (20,20,20)
     from dadi_gb300 import adjoint_nd, models
@@ -894,6 +917,14 @@ def run_profile_kernel(a):
                     models.IM(im_draws(2, 0)[1], (40, 40), 120)
             finally:
                 integration.line_solver_2d, integration.cluster_ctas = saved
+        elif a.profile == "adjoint2d_cluster":
+            # one IM gradient (seed-0 draw 1, 2648 steps) at pts 120: the
+            # backward walk on a cluster of 8 CTAs from its stored trajectory
+            # (0.6 GB)
+            draws = im_draws(2, 0)
+            eng = batch.Batch2D((120,), NS)
+            eng.loglik_and_grad(draws[1:2], torch.ones(41, 41, dtype=torch.float64,
+                                                       device="cuda"), 1.0)
         elif a.profile == "adjointnd_batch":
             # 8 three-population gradients at pts 32 as one batch (every
             # step's density recorded: about 1.5 GB), every sweep launch over
@@ -948,7 +979,7 @@ def main():
     ap.add_argument("--profile", default=None,
                     choices=["epilogue", "sweep3d", "adjoint2d", "adjointnd", "batchnd",
                              "fromphind", "thomas3d", "part3d", "adjointnd_batch",
-                             "cluster2d"],
+                             "cluster2d", "adjoint2d_cluster"],
                     help="run a small case of another kernel for profiler captures, then exit")
     ap.add_argument("--line-solvers", action="store_true",
                     help="time the batched N-D engine's line solvers on the growth model's "
