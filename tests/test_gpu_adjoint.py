@@ -233,3 +233,30 @@ def test_hybrid_adjoint_with_clusters(cuda_lib, golden):
     g_seg, g_hyb = g_seg.cpu().numpy(), g_hyb.cpu().numpy()
     assert int(st.abs().sum()) == 0 and np.all(np.isfinite(g_hyb))
     assert _close(g_hyb, g_seg) < 1e-10
+
+
+def test_cluster_walk_rejects_what_it_does_not_solve(cuda_lib):
+    """dgb_adjoint2d_part with a cluster size: sizes other than 2, 4, 8, 16
+    or no trajectory are DGB_ERR_ARG, grids outside 24-128 points or 3-16
+    rows per CTA DGB_ERR_UNSUPPORTED, all before any launch."""
+    import ctypes
+    import torch
+    from dadi_gb300 import _lib
+    lib = cuda_lib
+    buf = torch.zeros(1024, dtype=torch.float64, device="cuda")
+    p = _lib.dptr(buf)
+    st = _lib.settings_struct()
+    ws, nws = _lib.workspace(torch, 4096)
+
+    def call(Ls, cluster, traj=True):
+        arr = (ctypes.c_int * len(Ls))(*Ls)
+        t = p if traj else None
+        return lib.dgb_adjoint2d_part(p, 1, arr, len(Ls), p, p, p, p, p, p, p, 1, t, t, t, p,
+                                      p, p, 1, 0, cluster, ctypes.byref(st), _lib.dptr(ws), nws,
+                                      _lib.stream_handle(torch))
+
+    assert call([40], 3) == _lib.DGB_ERR_ARG
+    assert call([40], 8, traj=False) == _lib.DGB_ERR_ARG
+    for Ls, c in (([20], 8), ([130], 16), ([40], 2), ([30], 16), ([40, 20], 8)):
+        assert call(Ls, c) == _lib.DGB_ERR_UNSUPPORTED, (Ls, c)
+    torch.cuda.synchronize()

@@ -369,3 +369,34 @@ def test_autotune_sample_spans_the_cost_quantiles():
     idx = [int(np.nonzero(rec["T"] == t)[0][0]) for t in smp["T"]]
     assert idx == sorted(idx)
     assert len(autotune._sample(rec[:50], 100)) == 50
+
+
+def test_cluster_adjoint_rule():
+    """Batch2D's choice of a cluster per work item for the trajectory-mode
+    backward walk: only when every item can have its cluster at once
+    (instances x grids x CTAs <= SMs), every grid has 3-16 rows per CTA
+    within 24-128 points, and the delj trick is off."""
+    from dadi_gb300 import _lib, batch
+    eng = batch.Batch2D.__new__(batch.Batch2D)
+    st = _lib.settings_struct()
+    ctx = lambda n, s=st: {"n": n, "st": s}
+    eng.pts_l = (100, 110, 120)
+    eng.cluster_adjoint = 8
+    assert eng._cluster_adjoint_ctas(ctx(1), 152) == 8
+    assert eng._cluster_adjoint_ctas(ctx(6), 152) == 8      # 144 CTAs
+    assert eng._cluster_adjoint_ctas(ctx(7), 152) == 0      # 168 > 152
+    assert eng._cluster_adjoint_ctas(ctx(1, _lib.settings_struct(use_delj_trick=True)),
+                                     152) == 0
+    eng.cluster_adjoint = 0
+    assert eng._cluster_adjoint_ctas(ctx(1), 152) == 0
+    eng.cluster_adjoint = 4                                  # 120 > 16 x 4 rows
+    assert eng._cluster_adjoint_ctas(ctx(1), 152) == 0
+    eng.cluster_adjoint = 16
+    assert eng._cluster_adjoint_ctas(ctx(3), 152) == 16
+    eng.pts_l = (20, 25, 30)                                 # below 24 points
+    eng.cluster_adjoint = 8
+    assert eng._cluster_adjoint_ctas(ctx(1), 152) == 0
+    eng.pts_l = (30, 40, 50)
+    assert eng._cluster_adjoint_ctas(ctx(1), 152) == 8
+    eng.cluster_adjoint = 16                                 # 30 < 3 x 16 rows
+    assert eng._cluster_adjoint_ctas(ctx(1), 152) == 0
