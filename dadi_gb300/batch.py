@@ -469,9 +469,19 @@ class Batch2D:
         d_seed = _lib.to_device(torch, seeds.view(np.uint8), np.uint8)
         drows = torch.empty(max(int(table.numel() // 11), 1) * 60, dtype=torch.float64,
                             device="cuda")
-        _lib.check(lib.dgb_sched2d_deriv(_lib.dptr(d_rec), _lib.dptr(d_seed), n, ng,
-                                         _lib.dptr(self.d_dx0), ctypes.byref(st), _lib.dptr(cnt),
-                                         _lib.dptr(off), _lib.dptr(drows), sh), "dgb_sched2d_deriv")
+        # the derivative rows are for the adjoint only: their walk (serial
+        # per schedule, like the value walk) runs on a side stream beside
+        # the forward integration, joined before this returns
+        main = torch.cuda.current_stream()
+        dual = torch.cuda.Stream()
+        dual.wait_stream(main)
+        with torch.cuda.stream(dual):
+            _lib.check(lib.dgb_sched2d_deriv(_lib.dptr(d_rec), _lib.dptr(d_seed), n, ng,
+                                             _lib.dptr(self.d_dx0), ctypes.byref(st),
+                                             _lib.dptr(cnt), _lib.dptr(off), _lib.dptr(drows),
+                                             _lib.stream_handle(torch)), "dgb_sched2d_deriv")
+        for t in (d_rec, d_seed, cnt, off, drows):
+            t.record_stream(dual)
         steps = cnt.to(torch.int64).view(n, -1)
         Lsq = torch.tensor([L * L for L in self.pts_l], dtype=torch.int64, device="cuda")
         cost = (steps * Lsq[None, :]).reshape(-1)
@@ -517,6 +527,7 @@ class Batch2D:
             else:
                 fs = self.extrapolate(self.spectra(phis))
                 ll = self.loglik(fs, d, scale, mask, multinom)
+        main.wait_stream(dual)
         ctx = dict(phis=phis, ll=ll, fs=fs.detach(), table=table, off=off, cnt=cnt, drows=drows, ckpt=ckpt,
                    ck_off=ck_off, C=C, masks=d_masks, order=d_order, status=status, n=n, st=st)
         return ll, ctx

@@ -42,94 +42,109 @@ constexpr int NQ = 10;            // per-step scalars of a 2-D parameter row
 enum { Q_DT, Q_NU0, Q_NU1, Q_M01, Q_M10, Q_G0, Q_G1, Q_H0, Q_H1, Q_TH };
 
 // ------------------------------------------------------- dual numbers
+//
+// The derivative walk runs one thread per (schedule, parameter): each thread
+// carries the value and one derivative component.  The FP64 pipe takes a
+// warp instruction in the same time whether one lane or six are active, so
+// six lanes that each repeat the value chain and carry their own component
+// issue about a sixth of the FP64 instructions of one lane carrying all six
+// components.
 
-struct Dual {
-    double v;
-    double d[NPAR];
+struct D1 {
+    double v, d;
 };
 
-__device__ __forceinline__ Dual dconst(double v)
-{
-    Dual r;
-    r.v = v;
-#pragma unroll
-    for (int p = 0; p < NPAR; p++)
-        r.d[p] = 0;
-    return r;
-}
+// Per-instance constants of one parametric form for one derivative
+// component k: the reciprocals, logarithms and seed combinations that do not
+// change along the walk.
+struct PfK {
+    int kind;
+    double a, inv_a, inv_c, da, dc, s1, s2;
+};
 
-__device__ __forceinline__ Dual dseed(double v, const double *d)
+__device__ PfK pf_prepare(const dgb_pform &f, const double *da, const double *db,
+                          const double *dc, int k)
 {
-    Dual r;
-    r.v = v;
-#pragma unroll
-    for (int p = 0; p < NPAR; p++)
-        r.d[p] = d[p];
-    return r;
-}
-
-// d of a parametric form value f(t) with coefficient seeds (a, b, c) and t.
-__device__ Dual pform_dual(const dgb_pform &f, const double *da, const double *db,
-                           const double *dc, const Dual &t)
-{
-    Dual r;
-    r.v = pform_eval(f, t.v);
-    const double a = f.a, b = f.b, c = f.c;
+    PfK c;
+    c.kind = f.kind;
+    c.a = f.a;
+    c.inv_a = 1.0 / f.a;
+    c.inv_c = 1.0 / f.c;
+    c.da = da[k];
+    c.dc = dc[k];
+    c.s1 = 0;
+    c.s2 = 0;
     switch (f.kind) {
     case DGB_PF_EXPGROW: {
-        // a (b/a)^(t/c)
-        double q = b / a, y = t.v / c, p = pow(q, y), lq = log(q);
-#pragma unroll
-        for (int k = 0; k < NPAR; k++) {
-            double dq = (db[k] - q * da[k]) / a;
-            double dy = (t.d[k] - y * dc[k]) / c;
-            r.d[k] = da[k] * p + a * p * (y * dq / q + lq * dy);
-        }
+        // a q^(t/c), q = b/a: s1 = (dq/dtheta)/q, s2 = log q
+        const double q = f.b / f.a;
+        c.s1 = (db[k] - q * da[k]) / f.a / q;
+        c.s2 = log(q);
+        break;
+    }
+    case DGB_PF_EXPLOG:
+        // a exp(log(b/a) t / c): s1 = d log(b/a) / dtheta, s2 = log(b/a)
+        c.s1 = db[k] / f.b - da[k] / f.a;
+        c.s2 = log(f.b / f.a);
+        break;
+    case DGB_PF_LINEAR:
+        // a + b t: s1 = db/dtheta, s2 = b
+        c.s1 = db[k];
+        c.s2 = f.b;
+        break;
+    default:
+        break;
+    }
+    return c;
+}
+
+// A parametric form's value at t (as pform_eval gives it) and its derivative
+// along component k, with t's own derivative t.d.
+__device__ __forceinline__ D1 pform_d1(const dgb_pform &f, const PfK &c, const D1 &t)
+{
+    D1 r;
+    r.v = pform_eval(f, t.v);
+    switch (c.kind) {
+    case DGB_PF_EXPGROW: {
+        // p = q^y = value / a, y = t / c
+        const double p = r.v * c.inv_a, y = t.v * c.inv_c;
+        const double dy = (t.d - y * c.dc) * c.inv_c;
+        r.d = p * (c.da + c.a * (y * c.s1 + c.s2 * dy));
         break;
     }
     case DGB_PF_EXPLOG: {
-        // a exp(log(b/a) t / c)
-        double L0 = log(b / a), z = L0 * t.v / c, e = exp(z);
-#pragma unroll
-        for (int k = 0; k < NPAR; k++) {
-            double dL = db[k] / b - da[k] / a;
-            double dz = (dL * t.v + L0 * t.d[k]) / c - z * dc[k] / c;
-            r.d[k] = da[k] * e + a * e * dz;
-        }
+        // e = exp(z) = value / a, z = log(b/a) t / c
+        const double e = r.v * c.inv_a, z = c.s2 * t.v * c.inv_c;
+        const double dz = (c.s1 * t.v + c.s2 * t.d) * c.inv_c - z * c.dc * c.inv_c;
+        r.d = e * (c.da + c.a * dz);
         break;
     }
     case DGB_PF_LINEAR:
-#pragma unroll
-        for (int k = 0; k < NPAR; k++)
-            r.d[k] = da[k] + db[k] * t.v + b * t.d[k];
+        r.d = c.da + c.s1 * t.v + c.s2 * t.d;
         break;
     default:
-#pragma unroll
-        for (int k = 0; k < NPAR; k++)
-            r.d[k] = da[k];
+        r.d = c.da;
     }
     return r;
 }
 
 // Derivative of compute_dt (dadi/Integration.py:147-176) along the branch the
 // value takes; the value itself is compute_dt's.
-__device__ Dual compute_dt_dual(const Dual &nu, const Dual &msum, const Dual &gamma,
-                                const Dual &h, const dgb_settings &s, double dx0)
+__device__ D1 compute_dt_d1(const D1 &nu, const D1 &msum, const D1 &gamma, const D1 &h,
+                            const dgb_settings &s, double dx0)
 {
-    Dual r;
+    D1 r;
     r.v = compute_dt(nu.v, msum.v, gamma.v, h.v, s, dx0);
-#pragma unroll
-    for (int k = 0; k < NPAR; k++)
-        r.d[k] = 0;
+    r.d = 0;
     if (s.use_old_timestep)
         return r;
-    double v1 = 0.25 / nu.v;
-    double t1 = fabs(h.v + (1 - 2 * h.v) * 0.5) * 0.5 * (1 - 0.5);
-    double u2 = h.v + (1 - 2 * h.v) * 0.25;
-    double t2 = fabs(u2) * 0.25 * (1 - 0.25);
-    bool use_t2 = t2 > t1;
-    double tm = use_t2 ? t2 : t1;
-    double v3 = fabs(gamma.v) * 2 * tm;
+    const double v1 = 0.25 / nu.v;
+    const double t1 = fabs(h.v + (1 - 2 * h.v) * 0.5) * 0.5 * (1 - 0.5);
+    const double u2 = h.v + (1 - 2 * h.v) * 0.25;
+    const double t2 = fabs(u2) * 0.25 * (1 - 0.25);
+    const bool use_t2 = t2 > t1;
+    const double tm = use_t2 ? t2 : t1;
+    const double v3 = fabs(gamma.v) * 2 * tm;
     int branch = 0;
     double mx = v1;
     if (msum.v > mx) {
@@ -142,73 +157,75 @@ __device__ Dual compute_dt_dual(const Dual &nu, const Dual &msum, const Dual &ga
     }
     if (!(mx > 0))
         return r;
-    double sg = gamma.v >= 0 ? 1.0 : -1.0, su = u2 >= 0 ? 1.0 : -1.0;
-#pragma unroll
-    for (int k = 0; k < NPAR; k++) {
-        double dmx;
-        if (branch == 0)
-            dmx = -0.25 * nu.d[k] / (nu.v * nu.v);
-        else if (branch == 1)
-            dmx = msum.d[k];
-        else {
-            double dtm = use_t2 ? su * 0.5 * h.d[k] * 0.25 * (1 - 0.25) : 0.0;
-            dmx = sg * gamma.d[k] * 2 * tm + fabs(gamma.v) * 2 * dtm;
-        }
-        r.d[k] = -s.timescale_factor * dmx / (mx * mx);
+    double dmx;
+    if (branch == 0)
+        dmx = -0.25 * nu.d / (nu.v * nu.v);
+    else if (branch == 1)
+        dmx = msum.d;
+    else {
+        const double sg = gamma.v >= 0 ? 1.0 : -1.0, su = u2 >= 0 ? 1.0 : -1.0;
+        const double dtm = use_t2 ? su * 0.5 * h.d * 0.25 * (1 - 0.25) : 0.0;
+        dmx = sg * gamma.d * 2 * tm + fabs(gamma.v) * 2 * dtm;
     }
+    r.d = -s.timescale_factor * dmx / (mx * mx);
     return r;
 }
 
-// The schedule walk of sched2d (dgb_integrate2d.cu) with derivatives, for
-// exactly nrows steps; writes NQ x NPAR derivative doubles per step.
-__device__ void sched2d_walk_dual(const dgb_inst2d &I, const dgb_seed2d &S,
-                                  const dgb_settings &st, double dx0, int nrows, double *drows)
+// The schedule walk of sched2d (dgb_integrate2d.cu) with component k of the
+// derivatives, for exactly nrows steps: writes d(q)/dtheta_k of the NQ row
+// quantities per step (stride NPAR, interleaved with the other components).
+__device__ void sched2d_walk_d1(const dgb_inst2d &I, const dgb_seed2d &S,
+                                const dgb_settings &st, double dx0, int nrows, int k,
+                                double *drows)
 {
     const dgb_pform *F[9] = {&I.nu[0], &I.nu[1], &I.m12, &I.m21, &I.gamma[0],
                              &I.gamma[1], &I.h[0], &I.h[1], &I.theta0};
-    Dual cur = dseed(I.initial_t, S.dt0);
-    Dual T = dseed(I.T, S.dT);
-    Dual P[9];
+    PfK c[9];
+#pragma unroll
+    for (int f = 0; f < 9; f++)
+        c[f] = pf_prepare(*F[f], S.dform[f][0], S.dform[f][1], S.dform[f][2], k);
+    D1 cur = {I.initial_t, S.dt0[k]};
+    const D1 T = {I.T, S.dT[k]};
+    D1 P[9];
+#pragma unroll
     for (int f = 0; f < 8; f++)
-        P[f] = pform_dual(*F[f], S.dform[f][0], S.dform[f][1], S.dform[f][2], cur);
+        P[f] = pform_d1(*F[f], c[f], cur);
     for (int n = 0; n < nrows; n++) {
-        Dual d0 = compute_dt_dual(P[0], P[2], P[4], P[6], st, dx0);
-        Dual d1 = compute_dt_dual(P[1], P[3], P[5], P[7], st, dx0);
-        Dual dtm = (d1.v < d0.v) ? d1 : d0;
-        Dual rem;
-        rem.v = T.v - cur.v;
+        const D1 d0 = compute_dt_d1(P[0], P[2], P[4], P[6], st, dx0);
+        const D1 d1 = compute_dt_d1(P[1], P[3], P[5], P[7], st, dx0);
+        const D1 dtm = (d1.v < d0.v) ? d1 : d0;
+        const D1 rem = {T.v - cur.v, T.d - cur.d};
+        const D1 dt = (rem.v < dtm.v) ? rem : dtm;
+        const D1 next = {cur.v + dt.v, cur.d + dt.d};
 #pragma unroll
-        for (int k = 0; k < NPAR; k++)
-            rem.d[k] = T.d[k] - cur.d[k];
-        Dual dt = (rem.v < dtm.v) ? rem : dtm;
-        Dual next;
-        next.v = cur.v + dt.v;
-#pragma unroll
-        for (int k = 0; k < NPAR; k++)
-            next.d[k] = cur.d[k] + dt.d[k];
         for (int f = 0; f < 9; f++)
-            P[f] = pform_dual(*F[f], S.dform[f][0], S.dform[f][1], S.dform[f][2], next);
-        double *o = drows + (size_t)n * NQ * NPAR;
-        const Dual *q[NQ] = {&dt, &P[0], &P[1], &P[2], &P[3], &P[4], &P[5], &P[6], &P[7], &P[8]};
-        for (int j = 0; j < NQ; j++)
+            P[f] = pform_d1(*F[f], c[f], next);
+        double *o = drows + (size_t)n * NQ * NPAR + k;
+        o[0] = dt.d;
 #pragma unroll
-            for (int k = 0; k < NPAR; k++)
-                o[j * NPAR + k] = q[j]->d[k];
+        for (int f = 0; f < 9; f++)
+            o[(f + 1) * NPAR] = P[f].d;
         cur = next;
     }
 }
+
+// Eight lanes per schedule (instance, or instance x grid with
+// use_old_timestep), the first NPAR of them each carrying one derivative
+// component.
+constexpr int SD_LANES = 8;
 
 __global__ void k_sched2d_dual(const dgb_inst2d *insts, const dgb_seed2d *seeds, int nsched,
                                int ngrids, int per_grid, const double *dx0s, dgb_settings st,
                                const int *row_cnt, const long *row_off, double *drows)
 {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nsched)
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = t / SD_LANES, k = t % SD_LANES;
+    if (s >= nsched || k >= NPAR)
         return;
-    int inst = per_grid ? s / ngrids : s;
-    double dx0 = dx0s[per_grid ? s % ngrids : 0];
-    sched2d_walk_dual(insts[inst], seeds[inst], st, dx0, row_cnt[s],
-                      drows + row_off[s] * NQ * NPAR);
+    const int inst = per_grid ? s / ngrids : s;
+    const double dx0 = dx0s[per_grid ? s % ngrids : 0];
+    sched2d_walk_d1(insts[inst], seeds[inst], st, dx0, row_cnt[s], k,
+                    drows + row_off[s] * NQ * NPAR);
 }
 
 // ------------------------------------------------------- adjoint kernel
@@ -800,7 +817,8 @@ extern "C" int dgb_sched2d_deriv(const dgb_inst2d *insts, const dgb_seed2d *seed
         return DGB_ERR_ARG;
     int per_grid = settings->use_old_timestep ? 1 : 0;
     int nsched = per_grid ? ninst * ngrids : ninst;
-    dgb::k_sched2d_dual<<<(nsched + 31) / 32, 32, 0, (cudaStream_t)stream>>>(
+    const long nthreads = (long)nsched * dgb::SD_LANES;
+    dgb::k_sched2d_dual<<<(unsigned)((nthreads + 63) / 64), 64, 0, (cudaStream_t)stream>>>(
         insts, seeds, nsched, ngrids, per_grid, dx0s, *settings, row_cnt, row_off, drows);
     return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
 }

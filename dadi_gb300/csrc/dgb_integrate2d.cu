@@ -575,24 +575,97 @@ __host__ __device__ inline long sched2d_walk(const dgb_inst2d &I, const dgb_sett
     return n;
 }
 
-// One thread per schedule (instance, or instance x grid with
-// use_old_timestep).  fill == 0: count rows; fill == 1: write rows at
-// row_off[s] and the status bits.
+// sched2d_walk on two lanes of a warp: lane p evaluates population p's
+// forms and timestep (lane 0 also theta0), the two exchange their timesteps
+// by shuffle and so take the same steps, and each writes its population's
+// entries of the rows.  The FP64 pipe takes a warp instruction in the same
+// time whatever the number of active lanes, so the per-step chain (one
+// pow and one timestep per population) issues half the FP64 instructions of
+// one lane doing both.  The same functions give the same rows and status as
+// sched2d_walk.
+__device__ long sched2d_walk_pair(const dgb_inst2d &I, const dgb_settings &st, double dx0,
+                                  long max_steps, double *rows, int *status, int p)
+{
+    const unsigned pair = 3u << (threadIdx.x & 30);
+    const dgb_pform &fnu = I.nu[p], &fm = p ? I.m21 : I.m12, &fg = I.gamma[p], &fh = I.h[p];
+    double cur = I.initial_t;
+    double nu = pform_eval(fnu, cur), m = pform_eval(fm, cur);
+    double g = pform_eval(fg, cur), h = pform_eval(fh, cur);
+    long n = 0;
+    int err = 0;
+    while (cur < I.T) {
+        if (n >= max_steps) {
+            err |= DGB_ST_STEPCAP;
+            break;
+        }
+        const double mine = compute_dt(nu, m, g, h, st, dx0);
+        const double other = __shfl_xor_sync(pair, mine, 1);
+        const double dtm = p ? pymin(other, mine) : pymin(mine, other);
+        if (dtm == 0) {
+            err |= DGB_ST_ZERODT;
+            break;
+        }
+        const double dt = pymin(dtm, I.T - cur);
+        const double next = cur + dt;
+        if (!(dt > 0) || !isfinite(next)) {
+            err |= DGB_ST_NONFINITE;
+            break;
+        }
+        nu = pform_eval(fnu, next);
+        m = pform_eval(fm, next);
+        g = pform_eval(fg, next);
+        h = pform_eval(fh, next);
+        const double theta0 = p ? 0.0 : pform_eval(I.theta0, next);
+        const bool bad = nu < 0 || m < 0 || nu == 0 || theta0 < 0;
+        if (I.T < 0 || __any_sync(pair, bad)) {
+            err |= DGB_ST_BADPARAM;
+            break;
+        }
+        if (rows) {
+            double *r = rows + n * K2_ROW;
+            if (p == 0) {
+                r[0] = dt;
+                r[1] = theta0;
+                r[2] = nu;
+                r[4] = g;
+                r[6] = h;
+                r[8] = 1.0;
+                r[9] = m; // into pop 1 from pop 2 (m12)
+            } else {
+                r[3] = nu;
+                r[5] = g;
+                r[7] = h;
+                r[10] = m; // into pop 2 from pop 1 (m21)
+            }
+        }
+        n++;
+        cur = next;
+    }
+    *status |= err;
+    return n;
+}
+
+// Two lanes per schedule (instance, or instance x grid with
+// use_old_timestep; sched2d_walk_pair).  fill == 0: count rows; fill == 1:
+// write rows at row_off[s] and the status bits.
 __global__ void k_sched2d(const dgb_inst2d *insts, int nsched, int ngrids, int per_grid,
                           const double *dx0s, dgb_settings st, long max_steps, int fill,
                           int *row_cnt, const long *row_off, double *table, int *status)
 {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = t >> 1, p = t & 1;
     if (s >= nsched)
-        return;
+        return; // both lanes of the pair
     int inst = per_grid ? s / ngrids : s;
     double dx0 = dx0s[per_grid ? s % ngrids : 0];
     int err = 0;
     // fill == 2: row_cnt holds the room reserved at row_off (an upper bound
     // on the rows); a walk that would exceed it stops with DGB_ST_STEPCAP
     const long cap = (fill == 2) ? std::min<long>(max_steps, row_cnt[s]) : max_steps;
-    long n = sched2d_walk(insts[inst], st, dx0, cap,
-                          fill ? table + row_off[s] * K2_ROW : nullptr, &err);
+    long n = sched2d_walk_pair(insts[inst], st, dx0, cap,
+                               fill ? table + row_off[s] * K2_ROW : nullptr, &err, p);
+    if (p)
+        return;
     if (fill != 1)
         row_cnt[s] = (int)n;
     if (fill && err)
@@ -931,8 +1004,11 @@ extern "C" int dgb_sched2d(const dgb_inst2d *insts, int ninst, int ngrids, const
         return DGB_ERR_ARG;
     int per_grid = settings->use_old_timestep ? 1 : 0;
     int nsched = per_grid ? ninst * ngrids : ninst;
-    int nt = 32; // one warp per block: schedules are long serial chains
-    dgb::k_sched2d<<<(nsched + nt - 1) / nt, nt, 0, (cudaStream_t)stream>>>(
+    // one warp per block (16 schedules, two lanes each): schedules are long
+    // serial chains, spread over the SMs
+    const long nthreads = 2L * nsched;
+    const int nt = 32;
+    dgb::k_sched2d<<<(unsigned)((nthreads + nt - 1) / nt), nt, 0, (cudaStream_t)stream>>>(
         insts, nsched, ngrids, per_grid, dx0s, *settings, max_steps, fill, row_cnt, row_off,
         table, status);
     return cudaGetLastError() == cudaSuccess ? DGB_OK : DGB_ERR_CUDA;
