@@ -858,7 +858,9 @@ def run_profile_case(a):
 
 def run_profile_kernel(a):
     """Small cases of the other kernels for ncu captures (each launch well
-    under 0.1 s, a few hundred MB on the device at most), run twice."""
+    under 0.1 s, a few hundred MB on the device at most), run twice --
+    except grad_request, a full-size gradient request (launches up to 1.5
+    s, 11 GB of trajectory) for the one-pass launch list only."""
     import torch
     from dadi_gb300 import adjoint_nd, batch, build, epilogue, models
     build.build()
@@ -925,6 +927,15 @@ def run_profile_kernel(a):
             eng = batch.Batch2D((120,), NS)
             eng.loglik_and_grad(draws[1:2], torch.ones(41, 41, dtype=torch.float64,
                                                        device="cuda"), 1.0)
+        elif a.profile == "grad_request":
+            # one gradient request: the longest of the first 4096 seed-0
+            # draws (19,546 steps) at pts [100,110,120] (forward and adjoint
+            # on clusters, trajectory 11 GB)
+            d4 = im_draws(NINST, 0)
+            i = int(np.argmax(batch.count_steps(batch.im_instances(d4))))
+            eng = batch.Batch2D((100, 110, 120), NS)
+            eng.loglik_and_grad(d4[i:i + 1], torch.ones(41, 41, dtype=torch.float64,
+                                                         device="cuda"), 5e4)
         elif a.profile == "adjointnd_batch":
             # 8 three-population gradients at pts 32 as one batch (every
             # step's density recorded: about 1.5 GB), every sweep launch over
@@ -979,7 +990,7 @@ def main():
     ap.add_argument("--profile", default=None,
                     choices=["epilogue", "sweep3d", "adjoint2d", "adjointnd", "batchnd",
                              "fromphind", "thomas3d", "part3d", "adjointnd_batch",
-                             "cluster2d", "adjoint2d_cluster"],
+                             "cluster2d", "adjoint2d_cluster", "grad_request"],
                     help="run a small case of another kernel for profiler captures, then exit")
     ap.add_argument("--line-solvers", action="store_true",
                     help="time the batched N-D engine's line solvers on the growth model's "
