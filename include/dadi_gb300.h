@@ -230,7 +230,9 @@ typedef struct {
  * for each step, d(q)/dtheta (DGB_AD_NPAR doubles) for q = dt, nu1, nu2, m12,
  * m21, gamma1, gamma2, h1, h2, theta0 (60 doubles per step) at
  * drows + row_off[s]*60, following the value walk branch for branch
- * (dadi/Integration.py:147-176, 355-366).  insts/seeds device arrays. */
+ * (dadi/Integration.py:147-176, 355-366).  insts/seeds device arrays.  It
+ * reads no value rows, so it may run on another stream concurrently with
+ * the forward integration (one lane per schedule and parameter). */
 int dgb_sched2d_deriv(const dgb_inst2d *insts, const dgb_seed2d *seeds, int ninst, int ngrids,
                       const double *dx0s, const dgb_settings *settings, const int *row_cnt,
                       const long *row_off, double *drows, void *stream);
