@@ -95,6 +95,27 @@ def im_seeds(n):
     return sd
 
 
+def hybrid_plan(steps, Lsq, limit, ctas, cluster_items, nsm, per_sm):
+    """How the hybrid adjoint splits work items (steps and L^2 per item):
+    order, longest (steps x L^2) first; size, each item's trajectory in
+    bytes ((2 steps + 1) L^2 doubles); k, the longest items whose
+    trajectories fit `limit` bytes (at least one, and at least one item
+    left for the segment mode); j, how many of those walk on clusters of
+    `ctas` CTAs (at most cluster_items, within a quarter of the nsm SMs; 0
+    when ctas is 0); rest, the segment-mode walk's CTAs: the SMs the
+    clusters and the other trajectory items leave at per_sm CTAs each, never
+    fewer than a quarter of the device's CTAs nor more than its items."""
+    steps = np.asarray(steps, dtype=np.int64)
+    Lsq = np.asarray(Lsq, dtype=np.int64)
+    order = np.argsort(-(steps * Lsq), kind="stable").astype(np.int32)
+    size = (2 * steps + 1) * Lsq * 8
+    k = int(np.searchsorted(np.cumsum(size[order]), limit, side="right"))
+    k = max(1, min(k, len(order) - 1))
+    j = min(k, cluster_items, nsm // (4 * ctas)) if ctas else 0
+    rest = min(len(order) - k, max(nsm * per_sm // 4, (nsm - j * ctas) * per_sm - (k - j)))
+    return order, size, k, j, max(1, rest)
+
+
 def settings_from_globals(gam_placement=0, threads=0):
     tsf, otsf, old, delj = integration.current_settings()
     return _lib.settings_struct(tsf, otsf, old, delj, gam_placement, threads)
@@ -682,7 +703,7 @@ class Batch2D:
             if self.trajectory_bytes(ctx) <= self._traj_limit():
                 trajectory = True
             else:
-                self._adjoint_hybrid(ctx, lam, part, common, nblocks, nsm, per_sm, Lmax)
+                self._adjoint_hybrid(ctx, lam, part, common, nsm, per_sm, Lmax)
                 trajectory = "hybrid"
         if trajectory == "hybrid":
             pass
@@ -749,7 +770,7 @@ class Batch2D:
     #: 7.15 s with 4).
     hybrid_cluster_items = 0
 
-    def _adjoint_hybrid(self, ctx, lam, part, common, nblocks, nsm, per_sm, Lmax):
+    def _adjoint_hybrid(self, ctx, lam, part, common, nsm, per_sm, Lmax):
         """The longest work items (while their trajectory fits traj_budget)
         in trajectory mode -- the longest hybrid_cluster_items of them on
         clusters on the current stream, the others one CTA each on a side
@@ -761,14 +782,11 @@ class Batch2D:
         n, ng, C, st = ctx["n"], len(self.pts_l), ctx["C"], ctx["st"]
         steps = self._work_steps(ctx).reshape(-1)
         Lsq = np.tile(np.array([L * L for L in self.pts_l], dtype=np.int64), n)
-        order = np.argsort(-(steps * Lsq), kind="stable").astype(np.int32)
-        size = (2 * steps + 1) * Lsq * 8
-        k = int(np.searchsorted(np.cumsum(size[order]), self._traj_limit(), side="right"))
-        k = max(1, min(k, len(order) - 1))
         c = self.cluster_adjoint
         if not c or not all(max(24, 3 * c) <= L <= min(128, 16 * c) for L in self.pts_l):
             c = 0
-        j = min(k, self.hybrid_cluster_items, nsm // (4 * c)) if c else 0
+        order, size, k, j, rest = hybrid_plan(steps, Lsq, self._traj_limit(), c,
+                                              self.hybrid_cluster_items, nsm, per_sm)
         tset = order[:k]
         t_off = np.zeros(n * ng, dtype=np.int64)
         t_off[tset] = np.concatenate([[0], np.cumsum(size[tset] // 8)[:-1]])
@@ -779,9 +797,6 @@ class Batch2D:
         keep = [traj, d_toff, d_order]
         # (first, count, CTAs, cluster) of each trajectory-mode call
         calls = [(0, j, j, c), (j, k - j, k - j, 0)]
-        # the segment-mode walk on the SMs left, but never fewer than a
-        # quarter of the device's CTAs
-        rest = min(len(order) - k, max(nsm * per_sm // 4, (nsm - j * c) * per_sm - (k - j)))
         ws_s, nws_s = _lib.workspace(torch, 256 + lib.dgb_adjoint2d_scratch_bytes(Lmax, C, 1)
                                      * rest)
         keep.append(ws_s)

@@ -400,3 +400,32 @@ def test_cluster_adjoint_rule():
     assert eng._cluster_adjoint_ctas(ctx(1), 152) == 8
     eng.cluster_adjoint = 16                                 # 30 < 3 x 16 rows
     assert eng._cluster_adjoint_ctas(ctx(1), 152) == 0
+
+
+def test_hybrid_plan():
+    """The hybrid adjoint's split: longest items first into trajectory mode
+    while their trajectories fit, at least one item each way, the clustered
+    ones within a quarter of the SMs, and the segment-mode walk never on
+    fewer than a quarter of the device's CTAs."""
+    import numpy as np
+    from dadi_gb300 import batch
+    rng = np.random.default_rng(3)
+    steps = rng.integers(10, 20000, 768)
+    Lsq = np.tile(np.array([100 ** 2, 110 ** 2, 120 ** 2]), 256)
+    size = (2 * steps + 1) * Lsq * 8
+    for limit in (0, 4 << 30, 64 << 30, 1 << 50):
+        for ctas, items in ((0, 0), (8, 4), (8, 100), (16, 2)):
+            order, sz, k, j, rest = batch.hybrid_plan(steps, Lsq, limit, ctas, items, 152, 1)
+            assert np.array_equal(sz, size)
+            cost = (steps * Lsq)[order]
+            assert np.all(cost[:-1] >= cost[1:])
+            assert 1 <= k <= len(order) - 1
+            if 1 < k < len(order) - 1:
+                assert size[order[:k]].sum() <= limit < size[order[:k + 1]].sum()
+            assert j <= min(k, items) and j * ctas <= 152 // 4
+            assert (j == 0) == (ctas == 0 or items == 0)
+            assert min(len(order) - k, 38) <= rest <= len(order) - k
+    # few items: the segment mode keeps its items even when clusters and
+    # trajectory items would take every SM
+    order, sz, k, j, rest = batch.hybrid_plan([5000] * 12, [14400] * 12, 1 << 50, 8, 4, 152, 1)
+    assert (k, j, rest) == (11, 4, 1)
