@@ -429,3 +429,71 @@ def test_hybrid_plan():
     # trajectory items would take every SM
     order, sz, k, j, rest = batch.hybrid_plan([5000] * 12, [14400] * 12, 1 << 50, 8, 4, 152, 1)
     assert (k, j, rest) == (11, 4, 1)
+
+
+def _partition_solve(a, b, c, d, bounds):
+    """The partitioned tridiagonal solve of the cluster sweeps
+    (csrc/dgb_cluster.cuh), restated in numpy: each segment [s, e) (at least
+    three points) runs its downward pass over s+1 .. e-1, giving
+    al x_s + x_i + ga x_(i+1) = de; its upward pass expresses every interior
+    point by the segment's first point x_s and last point z; the first row
+    then gives x_s = D' - A' z_prev - C' z; substituting both segments'
+    first points into each last row leaves a tridiagonal system in the
+    segments' last points, solved by Thomas; the interior points follow."""
+    import numpy as np
+    S = len(bounds)
+    x = np.zeros_like(d)
+    Ap, Cp, Dp, al_l, ga_l, de_l = (np.zeros(S) for _ in range(6))
+    rel = []
+    for q, (s, e) in enumerate(bounds):
+        al, ga, de = {}, {}, {}
+        i = s + 1
+        al[i], ga[i], de[i] = a[i] / b[i], c[i] / b[i], d[i] / b[i]
+        for i in range(s + 2, e):
+            inv = 1.0 / (b[i] - a[i] * ga[i - 1])
+            al[i], ga[i], de[i] = -a[i] * al[i - 1] * inv, c[i] * inv, (d[i] - a[i] * de[i - 1]) * inv
+        al_l[q], ga_l[q], de_l[q] = al[e - 1], ga[e - 1], de[e - 1]
+        deu, alu, gau = de[e - 2], al[e - 2], ga[e - 2]
+        up = {e - 2: (deu, alu, gau)}
+        for i in range(e - 3, s, -1):
+            deu, alu, gau = de[i] - ga[i] * deu, al[i] - ga[i] * alu, -ga[i] * gau
+            up[i] = (deu, alu, gau)
+        B = b[s] - c[s] * alu
+        Ap[q], Cp[q], Dp[q] = a[s] / B, -c[s] * gau / B, (d[s] - c[s] * deu) / B
+        rel.append(up)
+    # the system in the last points z_q
+    ra = -al_l * Ap
+    rb = 1.0 - al_l * Cp - ga_l * np.append(Ap[1:], 0.0)
+    rc = -ga_l * np.append(Cp[1:], 0.0)
+    rd = de_l - al_l * Dp - ga_l * np.append(Dp[1:], 0.0)
+    z = np.linalg.solve(np.diag(rb) + np.diag(ra[1:], -1) + np.diag(rc[:-1], 1), rd)
+    for q, (s, e) in enumerate(bounds):
+        zp = z[q - 1] if q else 0.0
+        xf = Dp[q] - Ap[q] * zp - Cp[q] * z[q]
+        x[s], x[e - 1] = xf, z[q]
+        for i, (deu, alu, gau) in rel[q].items():
+            x[i] = deu - alu * xf - gau * z[q]
+    return x
+
+
+@pytest.mark.parametrize("L,S", [(24, 8), (37, 4), (100, 8), (128, 16), (48, 16), (30, 2)])
+def test_partition_solve_matches_dense(L, S):
+    """The partition method's algebra (as the cluster kernels apply it, rows
+    of each CTA or segment as c2_rows splits them) solves random
+    diagonally dominant tridiagonal systems and their transposes to 1e-12
+    of a dense solve."""
+    import numpy as np
+    rng = np.random.default_rng(L * 100 + S)
+    base, extra = L // S, L % S
+    starts = [r * base + min(r, extra) for r in range(S)]
+    bounds = [(s0, s0 + base + (1 if r < extra else 0)) for r, s0 in enumerate(starts)]
+    assert all(e - s >= 3 for s, e in bounds)
+    a, c = rng.uniform(-1, 0, L), rng.uniform(-1, 0, L)
+    a[0], c[-1] = 0.0, 0.0
+    b = 1.0 + np.abs(a) + np.abs(c) + rng.uniform(0, 1, L)
+    d = rng.normal(size=L)
+    M = np.diag(b) + np.diag(a[1:], -1) + np.diag(c[:-1], 1)
+    for sub, diag, sup, mat in ((a, b, c, M), (np.append(0.0, c[:-1]), b, np.append(a[1:], 0.0), M.T)):
+        x = _partition_solve(sub, diag, sup, d, bounds)
+        ref = np.linalg.solve(mat, d)
+        assert np.max(np.abs(x - ref)) <= 1e-12 * np.max(np.abs(ref))
